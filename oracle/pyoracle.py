@@ -1,0 +1,212 @@
+"""ctypes bindings for the CPU oracle (liboracle.so) and the CPU reference
+build (_ref/libspectral_ref.so).
+
+TEST INFRASTRUCTURE, NOT PRODUCT.  Only tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline leg import this module.  They use it to check or
+time the GPU library, never as a fallback for it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+_dp = C.POINTER(C.c_double)
+
+
+def build(quiet: bool = True) -> str:
+    """Compile liboracle.so in place (gcc, a second or two)."""
+    out = subprocess.run(["make", "-C", HERE, "liboracle.so"],
+                         capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
+    return os.path.join(HERE, "liboracle.so")
+
+
+def build_ref(ref_dir: str = "/root/reference") -> bool:
+    """Compile _ref/ from the reference sources if they are present."""
+    if not os.path.isdir(os.path.join(ref_dir, "src")):
+        return False
+    out = subprocess.run(["make", "-C", HERE, "ref", f"REF={ref_dir}"],
+                         capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("reference build failed:\n" + out.stdout + out.stderr)
+    return True
+
+
+def _p(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_dp)
+
+
+def lib() -> C.CDLL:
+    global _LIB
+    if _LIB is None:
+        path = os.path.join(HERE, "liboracle.so")
+        if not os.path.exists(path):
+            build()
+        L = C.CDLL(path)
+        i, d = C.c_int, C.c_double
+        sigs = {
+            "oracle_grid_0d": (None, [i, d, _dp, _dp]),
+            "oracle_grid_1d": (None, [i, d, _dp, _dp]),
+            "oracle_fft3d": (None, [i, d, _dp, _dp, _dp, _dp, i]),
+            "oracle_compute_qhat": (None, [i, d, _dp, _dp, _dp, _dp, _dp, _dp,
+                                           _dp, _dp, _dp, i]),
+            "oracle_computeQ": (None, [i, d, _dp, _dp, _dp, _dp, _dp, _dp, i]),
+            "oracle_computeQ_maxPreserve": (None, [i, d, _dp, _dp, _dp, _dp, _dp,
+                                                   _dp, d, d, i]),
+            "oracle_density": (d, [i, _dp, _dp, d]),
+            "oracle_bulk_velocity": (None, [i, _dp, _dp, d, d, _dp]),
+            "oracle_temperature": (d, [i, _dp, _dp, _dp, d, d, d]),
+            "oracle_ghat_integral": (d, [d, d, d, d, d]),
+            "oracle_gauss_legendre": (None, [i, _dp, _dp]),
+            "oracle_weights_iso": (None, [i, _dp, d, d, d, d, d, d, i, i, _dp, i]),
+            "oracle_run_0d": (None, [i, d, _dp, _dp, d, d, i, i, i, _dp, i]),
+            "oracle_init_bkw": (None, [i, _dp, d, _dp]),
+            "oracle_conserve_batch1": (None, [C.c_void_p, _dp, i]),
+            "oracle_conservation_init": (i, [C.c_void_p, i, d, _dp, _dp, i]),
+        }
+        for name, (res, args) in sigs.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _LIB = L
+    return _LIB
+
+
+class Grid:
+    """Velocity and Fourier grids of the reference (initializer.c:66-82 for
+    0D, :256-266 for 1D)."""
+
+    def __init__(self, N: int, L_v: float, kind: str = "0d"):
+        self.N, self.L_v, self.kind = N, float(L_v), kind
+        self.v = np.zeros(N)
+        self.zeta = np.zeros(N)
+        fn = lib().oracle_grid_0d if kind == "0d" else lib().oracle_grid_1d
+        fn(N, self.L_v, _p(self.v), _p(self.zeta))
+        self.n3 = N ** 3
+
+
+def fft3d(g: Grid, x: np.ndarray, invert: int) -> np.ndarray:
+    """fft3D (collisions.c:232-283) on a complex N^3 array."""
+    a = np.ascontiguousarray(np.asarray(x, dtype=np.complex128).reshape(-1))
+    ai = a.view(np.float64)
+    out = np.zeros(2 * g.n3)
+    lib().oracle_fft3d(g.N, g.L_v, _p(g.v), _p(g.zeta), _p(ai), _p(out), invert)
+    return out.view(np.complex128)
+
+
+def compute_qhat(g: Grid, W: np.ndarray, f: np.ndarray, gg: np.ndarray,
+                 nthreads: int = 0):
+    """Returns (Q, fhat, ghat, qhat) of compute_Qhat (collisions.c:108-169)."""
+    n3 = g.n3
+    W = np.ascontiguousarray(W, dtype=np.float64).reshape(n3, n3)
+    q = np.zeros(n3)
+    fh, gh, qh = np.zeros(2 * n3), np.zeros(2 * n3), np.zeros(2 * n3)
+    lib().oracle_compute_qhat(g.N, g.L_v, _p(g.v), _p(g.zeta), _p(W),
+                              _p(np.ascontiguousarray(f, dtype=np.float64)),
+                              _p(np.ascontiguousarray(gg, dtype=np.float64)),
+                              _p(q), _p(fh), _p(gh), _p(qh), nthreads)
+    return q, fh.view(np.complex128), gh.view(np.complex128), qh.view(np.complex128)
+
+
+def computeQ(g: Grid, W, f, gg=None, nthreads: int = 0) -> np.ndarray:
+    gg = f if gg is None else gg
+    Q = np.zeros(g.n3)
+    W = np.ascontiguousarray(W, dtype=np.float64)
+    lib().oracle_computeQ(g.N, g.L_v, _p(g.v), _p(g.zeta), _p(W),
+                          _p(np.ascontiguousarray(f, dtype=np.float64)),
+                          _p(np.ascontiguousarray(gg, dtype=np.float64)),
+                          _p(Q), nthreads)
+    return Q
+
+
+def computeQ_maxPreserve(g: Grid, W, f, gg=None, mass=1.0, KB=1.0,
+                         nthreads: int = 0) -> np.ndarray:
+    gg = f if gg is None else gg
+    Q = np.zeros(g.n3)
+    W = np.ascontiguousarray(W, dtype=np.float64)
+    lib().oracle_computeQ_maxPreserve(
+        g.N, g.L_v, _p(g.v), _p(g.zeta), _p(W),
+        _p(np.ascontiguousarray(f, dtype=np.float64)),
+        _p(np.ascontiguousarray(gg, dtype=np.float64)), _p(Q), mass, KB,
+        nthreads)
+    return Q
+
+
+class _Cons(C.Structure):
+    _fields_ = [("N", C.c_int), ("Ns", C.c_int), ("dv", C.c_double),
+                ("v", C.c_void_p), ("mass", C.c_double * 4),
+                ("CCt", (C.c_double * 8) * 8), ("pivot", C.c_int * 8)]
+
+
+class Conservation:
+    """initialize_conservation + conserveAllMoments (conserve.c) for one
+    species."""
+
+    def __init__(self, g: Grid, mass: float = 1.0):
+        self._v = g.v  # keep alive: the struct points at it
+        self.c = _Cons()
+        m = np.array([mass])
+        rc = lib().oracle_conservation_init(C.byref(self.c), g.N,
+                                            float(g.v[1] - g.v[0]), _p(g.v),
+                                            _p(m), 1)
+        if rc != 0:
+            raise ValueError("singular CC^T")
+        self.n3 = g.n3
+
+    def __call__(self, Q: np.ndarray) -> np.ndarray:
+        Q = np.array(Q, dtype=np.float64, copy=True)
+        B = Q.size // self.n3
+        lib().oracle_conserve_batch1(C.byref(self.c), _p(Q.reshape(-1)), B)
+        return Q
+
+
+def moments(g: Grid, f: np.ndarray, mass: float = 1.0, KB: float = 1.0):
+    """(rho, u[3], T) as momentRoutines.c computes them."""
+    f = np.ascontiguousarray(f, dtype=np.float64)
+    L = lib()
+    rho = L.oracle_density(g.N, _p(g.v), _p(f), mass)
+    u = np.zeros(3)
+    L.oracle_bulk_velocity(g.N, _p(g.v), _p(f), rho, mass, _p(u))
+    T = L.oracle_temperature(g.N, _p(g.v), _p(f), _p(u), rho, mass, KB)
+    return rho, u, T
+
+
+def weights_iso(g: Grid, lam: float, rows=None, d_i=2.0, d_j=2.0, m_i=1.0,
+                m_j=1.0, nthreads: int = 0) -> np.ndarray:
+    """Rows of the isotropic weights (weights.c:265-281); default all."""
+    n3 = g.n3
+    r0, r1 = (0, n3) if rows is None else rows
+    W = np.zeros((r1 - r0, n3))
+    lib().oracle_weights_iso(g.N, _p(g.zeta), g.L_v, float(lam), d_i, d_j,
+                             m_i, m_j, r0, r1, _p(W), nthreads)
+    return W
+
+
+def gauss_legendre(n: int):
+    x, w = np.zeros(n), np.zeros(n)
+    lib().oracle_gauss_legendre(n, _p(x), _p(w))
+    return x, w
+
+
+def init_bkw(g: Grid, K: float = 0.0) -> np.ndarray:
+    f = np.zeros(g.n3)
+    lib().oracle_init_bkw(g.N, _p(g.v), float(K), _p(f))
+    return f
+
+
+def run_0d(N, L_v, W, f0, dt, Kn, nT, order, maxpreserve=True,
+           nthreads: int = 0) -> np.ndarray:
+    """0D time loop of boltz.c:186-250; returns the write_streams rows."""
+    rows = np.zeros((nT + 1, 6 + N))
+    f = np.array(f0, dtype=np.float64, copy=True)
+    lib().oracle_run_0d(N, float(L_v), _p(np.ascontiguousarray(W, dtype=np.float64)),
+                        _p(f), float(dt), float(Kn), nT, order,
+                        1 if maxpreserve else 0, _p(rows), nthreads)
+    return rows

@@ -1,0 +1,660 @@
+/*
+ * spectral_oracle.c -- CPU restatement of the SpectralBTE collision path.
+ *
+ * TEST INFRASTRUCTURE, NOT PRODUCT.  It checks and times the GPU library and
+ * never runs inside it.  See spectral_oracle.h for the conventions.
+ *
+ * Build with -ffp-contract=off so that x86 and aarch64 round the same way.
+ * Expressions keep the reference's operand order.
+ */
+#include "spectral_oracle.h"
+#include "dft3.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#ifndef M_PI
+#define M_PI 3.14159265358979323846
+#endif
+
+static void trap_weights(int N, double *wt)
+{
+    /* collisions.c:48-54, conserve.c:35-39, momentRoutines.c:14-18 */
+    wt[0] = 0.5;
+    for (int i = 1; i < N - 1; i++) wt[i] = 1.0;
+    wt[N - 1] = 0.5;
+}
+
+/* ------------------------------------------------------------------ grids */
+void oracle_grid_0d(int N, double L_v, double *v, double *zeta)
+{
+    /* initializer.c:66-82 */
+    double dv = 2 * L_v / (N - 1);
+    for (int i = 0; i < N; i++) v[i] = -L_v + i * dv;
+    double deta = (2 * M_PI / N) / dv;
+    double L_eta = ((N % 2) == 0) ? 0.5 * N * deta : 0.5 * (N - 1) * deta;
+    for (int i = 0; i < N; i++) zeta[i] = -L_eta + i * deta;
+}
+
+void oracle_grid_1d(int N, double L_v, double *v, double *zeta)
+{
+    /* initializer.c:256-266 */
+    double dv = 2 * L_v / (N - 1);
+    for (int i = 0; i < N; i++) v[i] = -L_v + i * dv;
+    double L_eta = 0.5 * (N - 1) * M_PI / L_v;
+    double deta = M_PI * (N - 1) / (N * L_v);
+    for (int i = 0; i < N; i++) zeta[i] = -L_eta + i * deta;
+}
+
+/* -------------------------------------------------------------------- FFT */
+void oracle_fft3d(int N, double L_v, const double *v, const double *eta,
+                  const double *in, double *out, int invert)
+{
+    /* Module state of initialize_coll, collisions.c:36-46. */
+    double dv = v[1] - v[0];
+    double deta = eta[1] - eta[0];
+    double L_eta = -eta[0];
+    double scale3 = pow(1.0 / sqrt(2.0 * M_PI), 3.0);
+    double *wtN = (double *)malloc(sizeof(double) * N);
+    trap_weights(N, wtN);
+
+    double delta, L_start, L_end, sign;
+    const double *varr;
+    int dir;
+    if (!invert) { /* collisions.c:238-245 */
+        delta = dv; L_start = L_eta; L_end = L_v; varr = eta; sign = 1.0;
+        dir = -1; /* FFTW_FORWARD */
+    } else {       /* collisions.c:246-253 */
+        delta = deta; L_start = L_v; L_end = L_eta; varr = v; sign = -1.0;
+        dir = +1; /* FFTW_BACKWARD */
+    }
+    double prefactor = scale3 * delta * delta * delta;
+    long n3 = (long)N * N * N;
+    double *temp = (double *)malloc(sizeof(double) * 2 * n3);
+
+    /* pre-shift, collisions.c:257-268 */
+    for (long index = 0; index < n3; index++) {
+        int i = (int)(index / ((long)N * N));
+        int j = (int)((index - (long)i * N * N) / N);
+        int k = (int)(index - (long)N * (j + (long)i * N));
+        double sum = sign * (double)(i + j + k) * L_start * delta;
+        double factor = prefactor * wtN[i] * wtN[j] * wtN[k];
+        double c = cos(sum), s = sin(sum);
+        temp[2 * index] = factor * (c * in[2 * index] - s * in[2 * index + 1]);
+        temp[2 * index + 1] =
+            factor * (c * in[2 * index + 1] + s * in[2 * index]);
+    }
+    /* fftw_execute, collisions.c:270 */
+    oracle_dft3(N, N, N, temp, dir);
+    /* post-shift, collisions.c:273-281 */
+    for (long index = 0; index < n3; index++) {
+        int i = (int)(index / ((long)N * N));
+        int j = (int)((index - (long)i * N * N) / N);
+        int k = (int)(index - (long)N * (j + (long)i * N));
+        double sum = sign * L_end * (varr[i] + varr[j] + varr[k]);
+        double c = cos(sum), s = sin(sum);
+        double tr = temp[2 * index], ti = temp[2 * index + 1];
+        out[2 * index] = c * tr - s * ti;
+        out[2 * index + 1] = c * ti + s * tr;
+    }
+    free(temp);
+    free(wtN);
+}
+
+/* ------------------------------------------------------------ convolution */
+void oracle_compute_qhat(int N, double L_v, const double *v,
+                         const double *zeta, const double *W,
+                         const double *f, const double *g, double *q,
+                         double *fhat_out, double *ghat_out,
+                         double *qhat_out, int nthreads)
+{
+    long n3 = (long)N * N * N;
+    double *fin = (double *)malloc(sizeof(double) * 2 * n3);
+    double *gin = (double *)malloc(sizeof(double) * 2 * n3);
+    double *fo = (double *)malloc(sizeof(double) * 2 * n3);
+    double *go = (double *)malloc(sizeof(double) * 2 * n3);
+    double *qh = (double *)malloc(sizeof(double) * 2 * n3);
+    /* collisions.c:112-119 */
+    for (long index = 0; index < n3; index++) {
+        qh[2 * index] = 0.0; qh[2 * index + 1] = 0.0;
+        fin[2 * index] = f[index]; fin[2 * index + 1] = 0.0;
+        gin[2 * index] = g[index]; gin[2 * index + 1] = 0.0;
+    }
+    /* collisions.c:122-123 */
+    oracle_fft3d(N, L_v, v, zeta, fin, fo, 0);
+    oracle_fft3d(N, L_v, v, zeta, gin, go, 0);
+
+    /* collisions.c:127-165: rows of zeta in parallel, xi sequential */
+    int n2 = N / 2;
+#ifdef _OPENMP
+    int nt = nthreads > 0 ? nthreads : omp_get_max_threads();
+#pragma omp parallel for num_threads(nt) schedule(static)
+#else
+    (void)nthreads;
+#endif
+    for (long zeta_i = 0; zeta_i < n3; zeta_i++) {
+        int zx = (int)(zeta_i / ((long)N * N));
+        int zy = (int)((zeta_i - (long)zx * N * N) / N);
+        int zz = (int)(zeta_i - (long)N * (zy + (long)zx * N));
+        const double *row = W + zeta_i * n3;
+        double acc_re = 0.0, acc_im = 0.0;
+        for (long xi = 0; xi < n3; xi++) {
+            int xx = (int)(xi / ((long)N * N));
+            int xy = (int)((xi - (long)xx * N * N) / N);
+            int xz = (int)(xi - (long)N * (xy + (long)xx * N));
+            int x = zx + n2 - xx, y = zy + n2 - xy, z = zz + n2 - xz;
+            if (x < 0) x = N + x; else if (x > N - 1) x = x - N;
+            if (y < 0) y = N + y; else if (y > N - 1) y = y - N;
+            if (z < 0) z = N + z; else if (z > N - 1) z = z - N;
+            long index = z + (long)N * (y + (long)N * x);
+            acc_re += row[xi] * (go[2 * xi] * fo[2 * index] -
+                                 go[2 * xi + 1] * fo[2 * index + 1]);
+            acc_im += row[xi] * (go[2 * xi] * fo[2 * index + 1] +
+                                 go[2 * xi + 1] * fo[2 * index]);
+        }
+        qh[2 * zeta_i] = acc_re;
+        qh[2 * zeta_i + 1] = acc_im;
+    }
+    if (fhat_out) memcpy(fhat_out, fo, sizeof(double) * 2 * n3);
+    if (ghat_out) memcpy(ghat_out, go, sizeof(double) * 2 * n3);
+    if (qhat_out) memcpy(qhat_out, qh, sizeof(double) * 2 * n3);
+    if (q) {
+        /* collisions.c:168 then :218-220 */
+        oracle_fft3d(N, L_v, v, zeta, qh, fo, 1);
+        for (long index = 0; index < n3; index++) q[index] = fo[2 * index];
+    }
+    free(fin); free(gin); free(fo); free(go); free(qh);
+}
+
+void oracle_computeQ(int N, double L_v, const double *v, const double *zeta,
+                     const double *W, const double *f, const double *g,
+                     double *Q, int nthreads)
+{
+    oracle_compute_qhat(N, L_v, v, zeta, W, f, g, Q, NULL, NULL, NULL,
+                        nthreads);
+}
+
+/* ---------------------------------------------------------------- moments */
+double oracle_density(int N, const double *v, const double *in, double mass)
+{
+    /* momentRoutines.c:58-69 */
+    double dv = v[1] - v[0], dv3 = dv * dv * dv, result = 0.0;
+    double *wtN = (double *)malloc(sizeof(double) * N);
+    trap_weights(N, wtN);
+    for (int i = 0; i < N; i++)
+        for (int j = 0; j < N; j++)
+            for (int k = 0; k < N; k++)
+                result += dv3 * wtN[i] * wtN[j] * wtN[k] * in[k + N * (j + N * i)];
+    free(wtN);
+    return mass * result;
+}
+
+void oracle_bulk_velocity(int N, const double *v, const double *in,
+                          double rho, double mass, double *out)
+{
+    /* momentRoutines.c:116-141 */
+    double dv = v[1] - v[0], dv3 = dv * dv * dv;
+    double *wtN = (double *)malloc(sizeof(double) * N);
+    trap_weights(N, wtN);
+    out[0] = out[1] = out[2] = 0.0;
+    for (int i = 0; i < N; i++)
+        for (int j = 0; j < N; j++)
+            for (int k = 0; k < N; k++) {
+                double t1 = v[i] * dv3 * wtN[i] * wtN[j] * wtN[k] / rho;
+                double t2 = v[j] * dv3 * wtN[i] * wtN[j] * wtN[k] / rho;
+                double t3 = v[k] * dv3 * wtN[i] * wtN[j] * wtN[k] / rho;
+                double x = in[k + N * (j + N * i)];
+                out[0] += t1 * x; out[1] += t2 * x; out[2] += t3 * x;
+            }
+    out[0] = mass * out[0]; out[1] = mass * out[1]; out[2] = mass * out[2];
+    free(wtN);
+}
+
+double oracle_temperature(int N, const double *v, const double *in,
+                          const double *bulkV, double rho, double mass,
+                          double KB)
+{
+    /* momentRoutines.c:168-183 */
+    double dv = v[1] - v[0], dv3 = dv * dv * dv, result = 0.0;
+    double *wtN = (double *)malloc(sizeof(double) * N);
+    trap_weights(N, wtN);
+    for (int i = 0; i < N; i++)
+        for (int j = 0; j < N; j++)
+            for (int k = 0; k < N; k++) {
+                double temp = (v[i] - bulkV[0]) * (v[i] - bulkV[0]) +
+                              (v[j] - bulkV[1]) * (v[j] - bulkV[1]) +
+                              (v[k] - bulkV[2]) * (v[k] - bulkV[2]);
+                result += temp * dv3 * wtN[i] * wtN[j] * wtN[k] *
+                          in[k + N * (j + N * i)] / (3.0 * rho);
+            }
+    free(wtN);
+    return (mass * mass / KB) * result;
+}
+
+void oracle_energy(int N, const double *v, const double *in, double *out)
+{
+    /* momentRoutines.c:146-165 */
+    double dv = v[1] - v[0], dv3 = dv * dv * dv, pos = 0.0, neg = 0.0;
+    double *wtN = (double *)malloc(sizeof(double) * N);
+    trap_weights(N, wtN);
+    for (int i = 0; i < N; i++)
+        for (int j = 0; j < N; j++)
+            for (int k = 0; k < N; k++) {
+                double e = dv3 * wtN[i] * wtN[j] * wtN[k] * in[k + N * (j + N * i)] *
+                           (v[i] * v[i] + v[j] * v[j] + v[k] * v[k]);
+                if (e > 0) pos += e; else neg -= e;
+            }
+    out[0] = pos; out[1] = neg;
+    free(wtN);
+}
+
+/* --------------------------------------------------------- maxPreserve */
+static void find_maxwellian(int N, const double *v, const double *mat,
+                            double mass, double KB, double *M)
+{
+    /* collisions.c:95-103 (the g part is formed by the caller) */
+    double vel[3];
+    double rho = oracle_density(N, v, mat, mass);
+    oracle_bulk_velocity(N, v, mat, rho, mass, vel);
+    double T = oracle_temperature(N, v, mat, vel, rho, mass, KB);
+    double prefactor = rho * pow(0.5 / (M_PI * T), 1.5);
+    for (long index = 0; index < (long)N * N * N; index++) {
+        int i = (int)(index / (N * N));
+        int j = (int)((index - (long)i * N * N) / N);
+        int k = (int)(index - (long)N * (j + (long)N * i));
+        M[index] = prefactor * exp(-(0.5 / T) * ((v[i] - vel[0]) * (v[i] - vel[0]) +
+                                                 (v[j] - vel[1]) * (v[j] - vel[1]) +
+                                                 (v[k] - vel[2]) * (v[k] - vel[2])));
+    }
+}
+
+void oracle_computeQ_maxPreserve(int N, double L_v, const double *v,
+                                 const double *zeta, const double *W,
+                                 const double *f, const double *g, double *Q,
+                                 double mass, double KB, int nthreads)
+{
+    long n3 = (long)N * N * N;
+    double *Mi = (double *)malloc(sizeof(double) * n3);
+    double *Mj = (double *)malloc(sizeof(double) * n3);
+    double *gi = (double *)malloc(sizeof(double) * n3);
+    double *gj = (double *)malloc(sizeof(double) * n3);
+    double *t = (double *)malloc(sizeof(double) * n3);
+    /* collisions.c:181-182; both g's subtract M_i (collisions.c:104) */
+    find_maxwellian(N, v, f, mass, KB, Mi);
+    for (long x = 0; x < n3; x++) gi[x] = f[x] - Mi[x];
+    find_maxwellian(N, v, g, mass, KB, Mj);
+    for (long x = 0; x < n3; x++) gj[x] = g[x] - Mi[x];
+    /* collisions.c:184-200 */
+    oracle_compute_qhat(N, L_v, v, zeta, W, Mi, gj, t, 0, 0, 0, nthreads);
+    for (long x = 0; x < n3; x++) Q[x] = t[x];
+    oracle_compute_qhat(N, L_v, v, zeta, W, gi, Mj, t, 0, 0, 0, nthreads);
+    for (long x = 0; x < n3; x++) Q[x] += t[x];
+    oracle_compute_qhat(N, L_v, v, zeta, W, gi, gj, t, 0, 0, 0, nthreads);
+    for (long x = 0; x < n3; x++) Q[x] += t[x];
+    free(Mi); free(Mj); free(gi); free(gj); free(t);
+}
+
+/* ----------------------------------------------------------- conservation */
+static int factor_lu(oracle_cons *c, int nElem)
+{
+    /* factorMatrixIntoLU, conserve.c:89-168 (scaled pivoting after
+       Atkinson; the pivot row is the first row whose scaled entry beats the
+       running best, and only columns >= k are exchanged). */
+    double s[ORACLE_MAX_NS + 4], cc[ORACLE_MAX_NS + 4], m[ORACLE_MAX_NS + 4];
+    for (int i = 0; i < nElem; i++) {
+        s[i] = fabs(c->CCt[i][0]);
+        for (int j = 0; j < nElem; j++)
+            if (s[i] < fabs(c->CCt[i][j])) s[i] = fabs(c->CCt[i][j]);
+    }
+    for (int k = 0; k < nElem - 1; k++) {
+        cc[k] = fabs(c->CCt[k][k] / s[k]);
+        int ctr = 0, i0 = k;
+        for (int i = k; i < nElem; i++) {
+            if (cc[k] < fabs(c->CCt[i][k] / s[i])) {
+                cc[k] = fabs(c->CCt[i][k] / s[i]);
+                if (ctr != 1) { i0 = i; ctr = 1; }
+            }
+        }
+        c->pivot[k] = i0;
+        if (cc[k] == 0.0) return -1;
+        if (i0 != k) {
+            for (int j = k; j < nElem; j++) {
+                double t = c->CCt[k][j];
+                c->CCt[k][j] = c->CCt[i0][j];
+                c->CCt[i0][j] = t;
+            }
+            double t = s[k]; s[k] = s[i0]; s[i0] = t;
+        }
+        for (int i = k + 1; i < nElem; i++) {
+            m[i] = c->CCt[i][k] / c->CCt[k][k];
+            c->CCt[i][k] = m[i];
+            for (int j = k + 1; j < nElem; j++) c->CCt[i][j] -= m[i] * c->CCt[k][j];
+        }
+    }
+    return 0;
+}
+
+int oracle_conservation_init(oracle_cons *c, int N, double dv,
+                             const double *v, const double *mass, int Ns)
+{
+    /* initialize_conservation + createCCtAndPivot, conserve.c:17-43, 268-317 */
+    memset(c, 0, sizeof(*c));
+    c->N = N; c->Ns = Ns; c->dv = dv; c->v = v;
+    for (int m = 0; m < Ns; m++) c->mass[m] = mass[m];
+    int ne = Ns + 4;
+    long n3 = (long)N * N * N;
+    double *wtN = (double *)malloc(sizeof(double) * N);
+    trap_weights(N, wtN);
+    /* C[m][row][x] */
+    double *C = (double *)calloc((size_t)Ns * ne * n3, sizeof(double));
+    for (int m = 0; m < Ns; m++)
+        for (int i = 0; i < N; i++)
+            for (int j = 0; j < N; j++)
+                for (int k = 0; k < N; k++) {
+                    long x = k + N * (j + (long)N * i);
+                    double prefactor = wtN[i] * wtN[j] * wtN[k] * dv * dv * dv * mass[m];
+                    double *Cm = C + (long)m * ne * n3;
+                    for (int n = 0; n < Ns; n++) Cm[n * n3 + x] = 0;
+                    Cm[m * n3 + x] = prefactor;
+                    Cm[(Ns) * n3 + x] = prefactor * v[i];
+                    Cm[(Ns + 1) * n3 + x] = prefactor * v[j];
+                    Cm[(Ns + 2) * n3 + x] = prefactor * v[k];
+                    Cm[(Ns + 3) * n3 + x] =
+                        prefactor * 0.5 * (v[i] * v[i] + v[j] * v[j] + v[k] * v[k]);
+                }
+    for (int i = 0; i < ne; i++)
+        for (int j = 0; j < ne; j++) {
+            double acc = 0.0;
+            for (int m = 0; m < Ns; m++) {
+                const double *Cm = C + (long)m * ne * n3;
+                for (long k = 0; k < n3; k++) acc += Cm[i * n3 + k] * Cm[j * n3 + k];
+            }
+            c->CCt[i][j] = acc;
+        }
+    free(C);
+    free(wtN);
+    return factor_lu(c, ne);
+}
+
+void oracle_solve_cct(const oracle_cons *c, double *b)
+{
+    /* solveWithCCt, conserve.c:173-202 */
+    int nElem = c->Ns + 4;
+    for (int k = 0; k < nElem - 1; k++) {
+        int i = c->pivot[k];
+        if (c->pivot[k] != k) { double t = b[i]; b[i] = b[k]; b[k] = t; }
+        for (i = k + 1; i < nElem; i++) b[i] -= c->CCt[i][k] * b[k];
+    }
+    b[nElem - 1] = b[nElem - 1] / c->CCt[nElem - 1][nElem - 1];
+    for (int i = nElem - 2; i >= 0; i--) {
+        double sum = 0.0;
+        for (int j = i + 1; j < nElem; j++) sum += c->CCt[i][j] * b[j];
+        b[i] = 1.0 / c->CCt[i][i] * (b[i] - sum);
+    }
+}
+
+void oracle_conserve(const oracle_cons *c, double **Q)
+{
+    /* conserveAllMoments, conserve.c:207-264 */
+    int N = c->N, Ns = c->Ns;
+    double dv = c->dv;
+    const double *v = c->v;
+    double masterQ[ORACLE_MAX_NS + 4], tc[ORACLE_MAX_NS + 4];
+    double wtN[4096];
+    trap_weights(N, wtN);
+    for (int l = 0; l < Ns + 4; l++) masterQ[l] = 0.0;
+    memset(tc, 0, sizeof(tc));
+    for (int m = 0; m < Ns; m++)
+        for (int i = 0; i < N; i++)
+            for (int j = 0; j < N; j++)
+                for (int k = 0; k < N; k++) {
+                    double prefact = wtN[i] * wtN[j] * wtN[k] * dv * dv * dv * c->mass[m];
+                    tc[m] = prefact;
+                    tc[Ns] = prefact * v[i];
+                    tc[Ns + 1] = prefact * v[j];
+                    tc[Ns + 2] = prefact * v[k];
+                    tc[Ns + 3] = prefact * 0.5 * (v[i] * v[i] + v[j] * v[j] + v[k] * v[k]);
+                    long x = k + N * (j + (long)N * i);
+                    for (int n = 0; n < Ns; n++) {
+                        double q = Q[n * Ns + m][x];
+                        masterQ[m] += q * tc[m];
+                        masterQ[Ns] += q * tc[Ns];
+                        masterQ[Ns + 1] += q * tc[Ns + 1];
+                        masterQ[Ns + 2] += q * tc[Ns + 2];
+                        masterQ[Ns + 3] += q * tc[Ns + 3];
+                    }
+                }
+    oracle_solve_cct(c, masterQ);
+    for (int m = 0; m < Ns; m++)
+        for (int i = 0; i < N; i++)
+            for (int j = 0; j < N; j++)
+                for (int k = 0; k < N; k++) {
+                    double prefact = wtN[i] * wtN[j] * wtN[k] * dv * dv * dv * c->mass[m] / Ns;
+                    tc[m] = prefact;
+                    tc[Ns] = prefact * v[i];
+                    tc[Ns + 1] = prefact * v[j];
+                    tc[Ns + 2] = prefact * v[k];
+                    tc[Ns + 3] = prefact * 0.5 * (v[i] * v[i] + v[j] * v[j] + v[k] * v[k]);
+                    long x = k + N * (j + (long)N * i);
+                    for (int n = 0; n < Ns; n++)
+                        Q[n * Ns + m][x] -= (tc[m] * masterQ[m] + tc[Ns] * masterQ[Ns] +
+                                             tc[Ns + 1] * masterQ[Ns + 1] +
+                                             tc[Ns + 2] * masterQ[Ns + 2] +
+                                             tc[Ns + 3] * masterQ[Ns + 3]);
+                }
+}
+
+void oracle_conserve_batch1(const oracle_cons *c, double *Q, int B)
+{
+    long n3 = (long)c->N * c->N * c->N;
+    for (int b = 0; b < B; b++) {
+        double *p = Q + (long)b * n3;
+        oracle_conserve(c, &p);
+    }
+}
+
+/* ------------------------------------------------------------- quadrature */
+void oracle_gauss_legendre(int n, double *x, double *w)
+{
+    /* Newton iteration on the three-term Legendre recurrence
+       (k+1) P_{k+1} = (2k+1) x P_k - k P_{k-1}, started from
+       cos(pi (i - 1/4) / (n + 1/2)); w = 2 / ((1 - x^2) P_n'(x)^2).
+       Nodes come out in decreasing order and are stored ascending. */
+    for (int i = 1; i <= (n + 1) / 2; i++) {
+        double z = cos(M_PI * (i - 0.25) / (n + 0.5)), pp = 0.0;
+        for (int it = 0; it < 100; it++) {
+            double p1 = 1.0, p2 = 0.0;
+            for (int k = 1; k <= n; k++) {
+                double p3 = p2;
+                p2 = p1;
+                p1 = ((2.0 * k - 1.0) * z * p2 - (k - 1.0) * p3) / k;
+            }
+            pp = n * (z * p1 - p2) / (z * z - 1.0);
+            double z1 = z;
+            z = z1 - p1 / pp;
+            if (fabs(z - z1) <= 1e-16) {
+                /* one more evaluation at the converged node */
+                p1 = 1.0; p2 = 0.0;
+                for (int k = 1; k <= n; k++) {
+                    double p3 = p2;
+                    p2 = p1;
+                    p1 = ((2.0 * k - 1.0) * z * p2 - (k - 1.0) * p3) / k;
+                }
+                pp = n * (z * p1 - p2) / (z * z - 1.0);
+                break;
+            }
+        }
+        x[n - i] = z;
+        x[i - 1] = -z;
+        w[i - 1] = w[n - i] = 2.0 / ((1.0 - z * z) * pp * pp);
+    }
+}
+
+#define ORACLE_GL_POINTS 16
+int oracle_quad_panels(double L_v, double omega)
+{
+    /* With 16 nodes per panel and omega*h <= 6 rad, the truncation error of
+       a panel is below (3)^32/32! ~ 1e-20 of the integrand scale. */
+    int K = (int)ceil(omega * L_v / 6.0);
+    if (K < 4) K = 4;
+    return K;
+}
+
+static double sinc_ref(double x)
+{
+    /* weights.c:136-143 */
+    return (x != 0.0) ? sin(x) / x : 1.0;
+}
+
+double oracle_ghat_integral(double a0, double a1, double a2, double lambda,
+                            double L_v)
+{
+    /* Integral of ghat (weights.c:156-160) over [0, L_v]; the reference uses
+       gsl_integration_qag with the 21-point rule to 1e-8 (weights.c:203).
+       This uses composite 16-point Gauss-Legendre, converged to round-off. */
+    static double gx[ORACLE_GL_POINTS], gw[ORACLE_GL_POINTS];
+    static int init = 0;
+    if (!init) {
+#ifdef _OPENMP
+#pragma omp critical(oracle_gl_init)
+#endif
+        {
+            if (!init) { oracle_gauss_legendre(ORACLE_GL_POINTS, gx, gw); init = 1; }
+        }
+    }
+    double omega = a0 + a2 > a1 ? a0 + a2 : a1;
+    int K = oracle_quad_panels(L_v, omega);
+    double h = L_v / K, result = 0.0;
+    for (int p = 0; p < K; p++) {
+        double mid = (p + 0.5) * h, part = 0.0;
+        for (int q = 0; q < ORACLE_GL_POINTS; q++) {
+            double r = mid + 0.5 * h * gx[q];
+            double val = pow(r, lambda + 2) *
+                         (sinc_ref(r * a0) * sinc_ref(r * a2) - sinc_ref(r * a1));
+            part += gw[q] * val;
+        }
+        result += 0.5 * h * part;
+    }
+    return result;
+}
+
+void oracle_weights_iso(int N, const double *zeta, double L_v, double lambda,
+                        double d_i, double d_j, double m_i, double m_j,
+                        int row_begin, int row_end, double *W, int nthreads)
+{
+    /* initialize_weights (weights.c:41-49) and generate_conv_weights_iso
+       (weights.c:265-281) with gHat3 (weights.c:181-262) */
+    double deta = zeta[1] - zeta[0];
+    double prefactor = 16.0 * M_PI * M_PI * deta * deta * deta / pow(2.0 * M_PI, 1.5) / (4.0 * M_PI);
+    double mu = m_j / (m_i + m_j);
+    double *wtN = (double *)malloc(sizeof(double) * N);
+    trap_weights(N, wtN);
+    long n3 = (long)N * N * N;
+    double dfac = 0.25 * pow(0.5 * (d_i + d_j), 2);
+    (void)dfac;
+#ifdef _OPENMP
+    int nt = nthreads > 0 ? nthreads : omp_get_max_threads();
+#pragma omp parallel for num_threads(nt) schedule(dynamic)
+#else
+    (void)nthreads;
+#endif
+    for (long row = row_begin; row < row_end; row++) {
+        int i = (int)(row / ((long)N * N));
+        int j = (int)((row / N) % N);
+        int k = (int)(row % N);
+        double z1 = zeta[i], z2 = zeta[j], z3 = zeta[k];
+        for (long col = 0; col < n3; col++) {
+            int l = (int)(col / ((long)N * N));
+            int m = (int)((col / N) % N);
+            int n = (int)(col % N);
+            double k1 = zeta[l], k2 = zeta[m], k3 = zeta[n];
+            double a0 = mu * sqrt(z1 * z1 + z2 * z2 + z3 * z3);
+            double a1 = sqrt(k1 * k1 + k2 * k2 + k3 * k3);
+            double a2 = sqrt((k1 - mu * z1) * (k1 - mu * z1) + (k2 - mu * z2) * (k2 - mu * z2) +
+                             (k3 - mu * z3) * (k3 - mu * z3));
+            double g = prefactor * oracle_ghat_integral(a0, a1, a2, lambda, L_v);
+            W[(row - row_begin) * n3 + col] =
+                wtN[l] * wtN[m] * wtN[n] * 0.25 * pow(0.5 * (d_i + d_j), 2) * g;
+        }
+    }
+    free(wtN);
+}
+
+/* -------------------------------------------------------------- 0D driver */
+void oracle_init_bkw(int N, const double *v, double K, double *f)
+{
+    /* initializer.c:123-135 */
+    double Temp = 1.0;
+    if (!(K > 0)) K = 1 - exp(-5.5 / 6.0);
+    for (int i = 0; i < N; i++)
+        for (int j = 0; j < N; j++)
+            for (int k = 0; k < N; k++) {
+                double v2 = v[i] * v[i] + v[j] * v[j] + v[k] * v[k];
+                f[k + N * (j + N * i)] =
+                    (exp(-(v2) / (2 * K * Temp * Temp))) / (2.0 * pow(2 * M_PI * K * Temp * Temp, 1.5)) *
+                    ((5 * K - 3) / K + (1 - K) * (v2) / (K * K * Temp * Temp));
+            }
+}
+
+static void stream_row(int N, const double *v, const double *f, double time,
+                       double *row)
+{
+    /* write_streams, output.c:159-213 (mass 1, KB 1) */
+    double bulkV[3], energy[2];
+    double density = oracle_density(N, v, f, 1.0);
+    oracle_bulk_velocity(N, v, f, density, 1.0, bulkV);
+    double kinTemp = oracle_temperature(N, v, f, bulkV, density, 1.0, 1.0);
+    oracle_energy(N, v, f, energy);
+    row[0] = time;
+    row[1] = density;
+    row[2] = bulkV[0];
+    row[3] = kinTemp;
+    row[4] = density * kinTemp;
+    row[5] = energy[1] / energy[0];
+    for (int l = 0; l < N; l++) row[6 + l] = f[N / 2 + N * (N / 2 + N * l)];
+}
+
+void oracle_run_0d(int N, double L_v, const double *W, double *f, double dt,
+                   double Kn, int nT, int order, int maxpreserve,
+                   double *rows, int nthreads)
+{
+    /* boltz.c:186-250 for one species of mass 1 */
+    long n3 = (long)N * N * N;
+    double *v = (double *)malloc(sizeof(double) * N);
+    double *zeta = (double *)malloc(sizeof(double) * N);
+    oracle_grid_0d(N, L_v, v, zeta);
+    double *Q = (double *)malloc(sizeof(double) * n3);
+    double *f1 = (double *)malloc(sizeof(double) * n3);
+    oracle_cons cons;
+    double mass = 1.0;
+    oracle_conservation_init(&cons, N, v[1] - v[0], v, &mass, 1);
+    int stride = 6 + N;
+    stream_row(N, v, f, 0.0, rows);
+    for (int t = 0; t < nT; t++) {
+        if (maxpreserve)
+            oracle_computeQ_maxPreserve(N, L_v, v, zeta, W, f, f, Q, 1.0, 1.0, nthreads);
+        else
+            oracle_computeQ(N, L_v, v, zeta, W, f, f, Q, nthreads);
+        oracle_conserve(&cons, &Q);
+        if (order == 1) {
+            for (long x = 0; x < n3; x++) f[x] += dt * Q[x] / Kn;
+        } else {
+            for (long x = 0; x < n3; x++) { f1[x] = f[x]; f1[x] += dt * Q[x] / Kn; }
+            if (maxpreserve)
+                oracle_computeQ_maxPreserve(N, L_v, v, zeta, W, f1, f1, Q, 1.0, 1.0, nthreads);
+            else
+                oracle_computeQ(N, L_v, v, zeta, W, f1, f1, Q, nthreads);
+            oracle_conserve(&cons, &Q);
+            for (long x = 0; x < n3; x++) {
+                f[x] = 0.5 * (f[x] + f1[x]);
+                f[x] += 0.5 * dt * Q[x] / Kn;
+            }
+        }
+        stream_row(N, v, f, dt * (t + 1), rows + (long)(t + 1) * stride);
+    }
+    free(v); free(zeta); free(Q); free(f1);
+}
