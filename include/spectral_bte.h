@@ -1,0 +1,208 @@
+/*
+ * spectral_bte.h -- C ABI of the GB300 spectral-Lagrangian collision library
+ * (libspectral_gb300.so).
+ *
+ * Part 1 exports the reference's own collision-path symbols with identical
+ * signatures.  The reference's C host (boltz.c, initializer.c, output.c,
+ * transportroutines.c, ...) links against this library instead of
+ * collisions.c, conserve.c and weights.c, and runs unchanged.  Each
+ * declaration cites the reference declaration it replaces.
+ *
+ * Part 2 adds batched entry points that keep f, fhat and Q resident in
+ * device memory.  They replace the caller-side loop over cells
+ * (boltz.c:285-345) and over independent 0D instances.
+ *
+ * Conventions kept from the reference:
+ *   - index (i,j,k) -> k + N*(j + N*i), i slowest (collisions.c:99-102);
+ *   - W is N^3 rows (zeta) of N^3 columns (xi), FP64 (weights.c:61-63);
+ *   - Weights/ cache files are raw native-endian float64, N^3 rows x N^3,
+ *     no header, named as in weights.c:68,70,73.
+ * Errors: the reference's entry points return void and exit() on failure.
+ * Here they record a status that spectral_last_error() returns and print
+ * one line to stderr.  They never exit and never trap on the device.
+ */
+#ifndef SPECTRAL_BTE_H
+#define SPECTRAL_BTE_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* fftw_complex layout (interleaved re, im), without FFTW. */
+#if !defined(FFTW3_H) && !defined(ORACLE_STUB_FFTW3_H) && !defined(SPECTRAL_HAVE_FFTW_COMPLEX)
+#define SPECTRAL_HAVE_FFTW_COMPLEX
+typedef double fftw_complex[2];
+#endif
+
+/* Layout-compatible with the reference's species (species.h:11-26); same
+   include guard so the two headers coexist. */
+#ifndef _SPECIES_H
+#define _SPECIES_H
+typedef struct {
+    size_t id;
+    size_t num_levels;
+    size_t *lev_id;
+    double Rgas;
+    double mass;
+    double mm;
+    double d_ref;
+    double T_ref;
+    double mu_ref;
+    double omega;
+    double E0;
+    double *Ei;
+    double *gi;
+    char name[80];
+} species;
+#endif
+
+/* ===================== Part 1: reference symbols ====================== */
+
+/* collisions.h:27 (defined collisions.c:33) */
+void initialize_coll(int nodes, double length, double *vel, double *zeta);
+/* collisions.h:33 (collisions.c:81) */
+void dealloc_coll(void);
+/* collisions.h:38 (collisions.c:212): Q = Re(IFFT(Qhat(f, g))), FP64 */
+void ComputeQ(double *f, double *g, double *Q, double **conv_weights);
+/* collisions.h:40 (collisions.c:178): Q(M_i,g_j) + Q(g_i,M_j) + Q(g_i,g_j) */
+void ComputeQ_maxPreserve(double *f, double *g, double *Q,
+                          double **conv_weights);
+/* collisions.h:42 (collisions.c:232) */
+void fft3D(fftw_complex *in, fftw_complex *out, int invert);
+
+/* conserve.h:6 (conserve.c:17) */
+void initialize_conservation(int nodes, double h_v, double *vel, species *mix,
+                             int num_spec);
+/* conserve.h:8 (conserve.c:45) */
+void initialize_conservation_fast(int nodes, double h_v, double *vel);
+/* conserve.h:10 (conserve.c:76) */
+void dealloc_conservation(void);
+/* conserve.h:12 (conserve.c:89); det is unused, as in the reference */
+void factorMatrixIntoLU(int nElem, double det);
+/* conserve.h:14 (conserve.c:173) */
+void solveWithCCt(int nElem, double *b);
+/* conserve.h:16 (conserve.c:207) */
+void conserveAllMoments(double **Q);
+/* conserve.h:18 (conserve.c:268) */
+void createCCtAndPivot(void);
+
+/* weights.h:12 (weights.c:26) */
+void alloc_weights(int N, double ****conv_weights, int total_species);
+/* weights.h:37 (weights.c:33): load Weights/<name>.wts or generate it on
+   the GPU and store it; also keeps a device copy keyed by conv_weights */
+void initialize_weights(int nodes, double *eta, double Lv, double lam,
+                        int weightFlag, int isoFlag, double **conv_weights,
+                        species species_i, species species_j);
+/* weights.h:45 (weights.c:127) */
+void dealloc_weights(int N, double **conv_weights);
+/* weights.h:43 (weights.c:265): GPU quadrature into conv_weights rows */
+void generate_conv_weights_iso(double **conv_weights);
+/* weights.h:47 (weights.c:156): the integrand, on the host */
+double ghat(double r, void *args);
+/* weights.h:49 (weights.c:181): one weight's integral times prefactor */
+double gHat3(double ki1, double ki2, double ki3, double zeta1, double zeta2,
+             double zeta3);
+
+/* ===================== Part 2: batched device API ===================== */
+
+/* Status codes (returned by spectral_* and spectral_last_error). */
+#define SPECTRAL_OK 0
+#define SPECTRAL_ERR_CUDA 1
+#define SPECTRAL_ERR_ARG 2
+#define SPECTRAL_ERR_NOT_INIT 3
+#define SPECTRAL_ERR_WEIGHTS 4
+#define SPECTRAL_ERR_SINGULAR 5
+#define SPECTRAL_ERR_UNSUPPORTED 6
+#define SPECTRAL_ERR_DEVICE_TIMEOUT 7
+#define SPECTRAL_ERR_NONFINITE 8
+#define SPECTRAL_ERR_NOMEM 9
+
+/* Flags for spectral_computeQ_*. */
+#define SPECTRAL_FP64 0        /* plain FP64 operator (parity path) */
+#define SPECTRAL_FP32 1        /* batched FP32 convolution + FFTs */
+#define SPECTRAL_MAXPRESERVE 2 /* ComputeQ_maxPreserve semantics */
+#define SPECTRAL_CONSERVE 4    /* apply conserveAllMoments (FP64) */
+
+int spectral_last_error(void);
+const char *spectral_last_error_message(void);
+const char *spectral_version(void);
+
+typedef struct spectral_plan_s spectral_plan;
+
+/* A plan holds one velocity grid (N nodes on [-L_v, L_v]; v and zeta as
+   the reference's initializer builds them), its device weights, the
+   conservation factors for one species and scratch for up to max_batch
+   instances.  It uses the CUDA device current at creation. */
+int spectral_plan_create(spectral_plan **plan, int N, double L_v,
+                         const double *v, const double *zeta, int max_batch);
+int spectral_plan_destroy(spectral_plan *plan);
+
+/* Weights: from host rows (reference layout), from one flat row-major
+   [N^3][N^3] array (host or device), or generated on the GPU by the
+   isotropic quadrature (weights.c:265-281).  Species diameters and masses
+   as species.c defaults: d = 2, m = 1. */
+int spectral_plan_set_weights_rows(spectral_plan *plan, double **rows);
+int spectral_plan_set_weights(spectral_plan *plan, const double *W,
+                              int on_device);
+int spectral_plan_generate_weights_iso(spectral_plan *plan, double lambda,
+                                       double d_i, double d_j, double m_i,
+                                       double m_j);
+int spectral_plan_get_weights(spectral_plan *plan, double *W_host,
+                              long long row0, long long nrows);
+/* Conservation factors for one species of the given mass
+   (initialize_conservation with Ns = 1). */
+int spectral_plan_set_conservation(spectral_plan *plan, double mass);
+
+/* Q for B instances.  f and Q are [B][N^3] FP64 in device memory; for
+   flag SPECTRAL_FP32 the transforms and the convolution run in FP32 and
+   moments, Maxwellian split and conservation stay FP64.  stream may be
+   NULL (the plan's stream).  Asynchronous. */
+int spectral_computeQ_device(spectral_plan *plan, const double *f_dev,
+                             double *Q_dev, int B, int flags, void *stream);
+/* Same with host arrays: copies in, computes, copies out, synchronises. */
+int spectral_computeQ_host(spectral_plan *plan, const double *f_host,
+                           double *Q_host, int B, int flags);
+/* conserveAllMoments on [B][N^3] device arrays, FP64, in place. */
+int spectral_conserve_device(spectral_plan *plan, double *Q_dev, int B,
+                             void *stream);
+/* One time step of the homogeneous solver (boltz.c:193-241) for B
+   instances held on the device: order 1 (Euler) or 2 (RK2), f updated in
+   place.  Conservation is always applied, as boltz.c does. */
+int spectral_step_device(spectral_plan *plan, double *f_dev, int B,
+                         double dt, double Kn, int order, int flags,
+                         void *stream);
+
+/* FP32 convolution tuning: bg = instances per CTA (32, 64, 128),
+   stages = copy pipeline depth, flush = xi-rows per FP64 flush.  The
+   autotuner times the supported shapes on B instances and keeps the
+   fastest; *chosen (optional, 3 ints) receives it. */
+int spectral_plan_set_tuning(spectral_plan *plan, int bg, int stages,
+                             int flush);
+int spectral_plan_autotune(spectral_plan *plan, int B, int flags,
+                           int *chosen);
+
+/* Device status word of the last call: bit 0 = a bounded device wait gave
+   up, bit 1 = non-finite output.  Cleared by the read. */
+int spectral_plan_status(spectral_plan *plan, unsigned int *status);
+
+/* Convolution-kernel timing: with profiling on, every convolution launch
+   is bracketed by CUDA events on its own stream; spectral_plan_conv_time
+   returns the summed device time (ms) and the number of launches since
+   the last query, then resets. */
+int spectral_plan_set_profiling(spectral_plan *plan, int on);
+int spectral_plan_conv_time(spectral_plan *plan, double *total_ms,
+                            int *launches);
+
+/* Synchronise the plan's stream. */
+int spectral_plan_sync(spectral_plan *plan);
+
+/* Number of kernels the library launched since load (monotonic). */
+long long spectral_kernel_launches(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPECTRAL_BTE_H */

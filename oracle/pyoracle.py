@@ -70,6 +70,7 @@ def lib() -> C.CDLL:
             "oracle_init_bkw": (None, [i, _dp, d, _dp]),
             "oracle_conserve_batch1": (None, [C.c_void_p, _dp, i]),
             "oracle_conservation_init": (i, [C.c_void_p, i, d, _dp, _dp, i]),
+            "oracle_qhat_rows": (None, [i, _dp, i, i, _dp, _dp, _dp, i]),
         }
         for name, (res, args) in sigs.items():
             fn = getattr(L, name)
@@ -176,6 +177,18 @@ def moments(g: Grid, f: np.ndarray, mass: float = 1.0, KB: float = 1.0):
     L.oracle_bulk_velocity(g.N, _p(g.v), _p(f), rho, mass, _p(u))
     T = L.oracle_temperature(g.N, _p(g.v), _p(f), _p(u), rho, mass, KB)
     return rho, u, T
+
+
+def qhat_rows(g: Grid, W_rows: np.ndarray, row0: int, fhat: np.ndarray,
+              ghat: np.ndarray, nthreads: int = 0) -> np.ndarray:
+    """compute_Qhat's convolution for zeta rows [row0, row0 + len(W_rows))."""
+    W_rows = np.ascontiguousarray(W_rows, dtype=np.float64)
+    nrows = W_rows.shape[0]
+    fh = np.ascontiguousarray(fhat, dtype=np.complex128).view(np.float64)
+    gh = np.ascontiguousarray(ghat, dtype=np.complex128).view(np.float64)
+    out = np.zeros(2 * nrows)
+    lib().oracle_qhat_rows(g.N, _p(W_rows), row0, nrows, _p(fh), _p(gh), _p(out), nthreads)
+    return out.view(np.complex128)
 
 
 def weights_iso(g: Grid, lam: float, rows=None, d_i=2.0, d_j=2.0, m_i=1.0,

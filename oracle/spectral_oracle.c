@@ -170,6 +170,43 @@ void oracle_compute_qhat(int N, double L_v, const double *v,
     free(fin); free(gin); free(fo); free(go); free(qh);
 }
 
+void oracle_qhat_rows(int N, const double *W_rows, int row0, int nrows,
+                      const double *fo, const double *go, double *qh,
+                      int nthreads)
+{
+    /* collisions.c:127-165 restricted to zeta in [row0, row0+nrows) */
+    long n3 = (long)N * N * N;
+    int n2 = N / 2;
+#ifdef _OPENMP
+    int nt = nthreads > 0 ? nthreads : omp_get_max_threads();
+#pragma omp parallel for num_threads(nt) schedule(static)
+#else
+    (void)nthreads;
+#endif
+    for (long r = 0; r < nrows; r++) {
+        long zeta_i = row0 + r;
+        int zx = (int)(zeta_i / ((long)N * N));
+        int zy = (int)((zeta_i - (long)zx * N * N) / N);
+        int zz = (int)(zeta_i - (long)N * (zy + (long)zx * N));
+        const double *row = W_rows + r * n3;
+        double acc_re = 0.0, acc_im = 0.0;
+        for (long xi = 0; xi < n3; xi++) {
+            int xx = (int)(xi / ((long)N * N));
+            int xy = (int)((xi - (long)xx * N * N) / N);
+            int xz = (int)(xi - (long)N * (xy + (long)xx * N));
+            int x = zx + n2 - xx, y = zy + n2 - xy, z = zz + n2 - xz;
+            if (x < 0) x = N + x; else if (x > N - 1) x = x - N;
+            if (y < 0) y = N + y; else if (y > N - 1) y = y - N;
+            if (z < 0) z = N + z; else if (z > N - 1) z = z - N;
+            long index = z + (long)N * (y + (long)N * x);
+            acc_re += row[xi] * (go[2 * xi] * fo[2 * index] - go[2 * xi + 1] * fo[2 * index + 1]);
+            acc_im += row[xi] * (go[2 * xi] * fo[2 * index + 1] + go[2 * xi + 1] * fo[2 * index]);
+        }
+        qh[2 * r] = acc_re;
+        qh[2 * r + 1] = acc_im;
+    }
+}
+
 void oracle_computeQ(int N, double L_v, const double *v, const double *zeta,
                      const double *W, const double *f, const double *g,
                      double *Q, int nthreads)

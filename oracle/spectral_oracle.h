@@ -50,6 +50,14 @@ void oracle_compute_qhat(int N, double L_v, const double *v,
                          double *fhat_out, double *ghat_out,
                          double *qhat_out, int nthreads);
 
+/* The inner loop of compute_Qhat (collisions.c:127-165) for zeta rows
+   [row0, row0+nrows) only: qhat[zeta - row0] from precomputed transforms
+   fhat, ghat (interleaved complex N^3) and W rows W[(zeta-row0)*N^3 + xi].
+   Used to time a bounded sample of the convolution on the CPU. */
+void oracle_qhat_rows(int N, const double *W_rows, int row0, int nrows,
+                      const double *fhat, const double *ghat, double *qhat,
+                      int nthreads);
+
 /* ComputeQ (collisions.c:212-221). */
 void oracle_computeQ(int N, double L_v, const double *v, const double *zeta,
                      const double *W, const double *f, const double *g,

@@ -1,0 +1,400 @@
+"""spectralbte_gb300 -- Python host mirror of the GB300 collision library.
+
+The compute runs in libspectral_gb300.so (hand-written CUDA for sm_103a).
+This module binds its C ABI (include/spectral_bte.h) with ctypes.
+
+* ``ReferenceAPI`` mirrors the reference's collisions.h, conserve.h and
+  weights.h entry points one for one: initialize_coll, ComputeQ,
+  ComputeQ_maxPreserve, fft3D, initialize_conservation, conserveAllMoments,
+  alloc_weights, initialize_weights and dealloc_weights.  Each takes numpy
+  arrays.
+* ``Plan`` wraps the batched device API.  f and Q stay in device memory,
+  either torch CUDA tensors or raw device pointers.
+
+There is no CPU fallback.  If the shared library is missing, or no GPU is
+present, loading or calling it raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libspectral_gb300.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "spectral_bte.h")
+
+FP64 = 0
+FP32 = 1
+MAXPRESERVE = 2
+CONSERVE = 4
+
+_dp = C.POINTER(C.c_double)
+_LIB: Optional[C.CDLL] = None
+
+
+class SpectralError(RuntimeError):
+    pass
+
+
+class Species(C.Structure):
+    """Layout of the reference's species struct (species.h:11-26)."""
+    _fields_ = [("id", C.c_size_t), ("num_levels", C.c_size_t),
+                ("lev_id", C.c_void_p), ("Rgas", C.c_double),
+                ("mass", C.c_double), ("mm", C.c_double),
+                ("d_ref", C.c_double), ("T_ref", C.c_double),
+                ("mu_ref", C.c_double), ("omega", C.c_double),
+                ("E0", C.c_double), ("Ei", C.c_void_p), ("gi", C.c_void_p),
+                ("name", C.c_char * 80)]
+
+    @classmethod
+    def default(cls, mass: float = 1.0, d_ref: float = 2.0, name: bytes = b"default",
+                sid: int = 0) -> "Species":
+        """species.c:28-42 defaults."""
+        s = cls()
+        s.id, s.num_levels = sid, 0
+        s.Rgas, s.mass, s.mm = 1.0, mass, 1.0
+        s.d_ref, s.T_ref, s.mu_ref, s.E0 = d_ref, 1.0, 1.0, 0.0
+        s.name = name
+        return s
+
+
+def grid_0d(N: int, L_v: float):
+    """(v, zeta) of the homogeneous solver (initializer.c:66-82)."""
+    dv = 2 * L_v / (N - 1)
+    v = np.array([-L_v + i * dv for i in range(N)])
+    deta = (2 * np.pi / N) / dv
+    L_eta = 0.5 * N * deta if N % 2 == 0 else 0.5 * (N - 1) * deta
+    zeta = np.array([-L_eta + i * deta for i in range(N)])
+    return v, zeta
+
+
+def grid_1d(N: int, L_v: float):
+    """(v, zeta) of the inhomogeneous solver (initializer.c:256-266)."""
+    dv = 2 * L_v / (N - 1)
+    v = np.array([-L_v + i * dv for i in range(N)])
+    L_eta = 0.5 * (N - 1) * np.pi / L_v
+    deta = np.pi * (N - 1) / (N * L_v)
+    zeta = np.array([-L_eta + i * deta for i in range(N)])
+    return v, zeta
+
+
+def build(force: bool = False) -> str:
+    from . import builder as _b
+    return _b.build(force=force)
+
+
+def lib() -> C.CDLL:
+    """Load libspectral_gb300.so; raises if it has not been built."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(LIB_PATH):
+        raise SpectralError(
+            f"{LIB_PATH} is missing: build it with spectralbte_gb300.build() "
+            "(there is no CPU fallback)")
+    L = C.CDLL(LIB_PATH)
+    i, d, v, p = C.c_int, C.c_double, C.c_void_p, C.c_void_p
+    pp = C.POINTER(C.c_void_p)
+    sigs = {
+        # reference ABI
+        "initialize_coll": (None, [i, d, _dp, _dp]),
+        "dealloc_coll": (None, []),
+        "ComputeQ": (None, [_dp, _dp, _dp, C.POINTER(_dp)]),
+        "ComputeQ_maxPreserve": (None, [_dp, _dp, _dp, C.POINTER(_dp)]),
+        "fft3D": (None, [_dp, _dp, i]),
+        "initialize_conservation": (None, [i, d, _dp, C.POINTER(Species), i]),
+        "initialize_conservation_fast": (None, [i, d, _dp]),
+        "dealloc_conservation": (None, []),
+        "conserveAllMoments": (None, [C.POINTER(_dp)]),
+        "solveWithCCt": (None, [i, _dp]),
+        "alloc_weights": (None, [i, v, i]),
+        "initialize_weights": (None, [i, _dp, d, d, i, i, C.POINTER(_dp), Species, Species]),
+        "dealloc_weights": (None, [i, C.POINTER(_dp)]),
+        "generate_conv_weights_iso": (None, [C.POINTER(_dp)]),
+        "gHat3": (d, [d, d, d, d, d, d]),
+        # batched API
+        "spectral_last_error": (i, []),
+        "spectral_last_error_message": (C.c_char_p, []),
+        "spectral_version": (C.c_char_p, []),
+        "spectral_kernel_launches": (C.c_longlong, []),
+        "spectral_plan_create": (i, [pp, i, d, _dp, _dp, i]),
+        "spectral_plan_destroy": (i, [v]),
+        "spectral_plan_set_weights": (i, [v, v, i]),
+        "spectral_plan_generate_weights_iso": (i, [v, d, d, d, d, d]),
+        "spectral_plan_get_weights": (i, [v, _dp, C.c_longlong, C.c_longlong]),
+        "spectral_plan_set_conservation": (i, [v, d]),
+        "spectral_computeQ_device": (i, [v, v, v, i, i, v]),
+        "spectral_computeQ_host": (i, [v, _dp, _dp, i, i]),
+        "spectral_conserve_device": (i, [v, v, i, v]),
+        "spectral_step_device": (i, [v, v, i, d, d, i, i, v]),
+        "spectral_plan_set_tuning": (i, [v, i, i, i]),
+        "spectral_plan_autotune": (i, [v, i, i, C.POINTER(C.c_int)]),
+        "spectral_plan_status": (i, [v, C.POINTER(C.c_uint)]),
+        "spectral_plan_sync": (i, [v]),
+        "spectral_plan_set_profiling": (i, [v, i]),
+        "spectral_plan_conv_time": (i, [v, _dp, C.POINTER(C.c_int)]),
+    }
+    for name, (res, args) in sigs.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = L
+    return L
+
+
+def _check(rc: int, what: str):
+    if rc != 0:
+        msg = lib().spectral_last_error_message().decode(errors="replace")
+        raise SpectralError(f"{what} failed ({rc}): {msg}")
+
+
+def _p(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_dp)
+
+
+def _legacy_check(what: str):
+    rc = lib().spectral_last_error()
+    if rc != 0:
+        msg = lib().spectral_last_error_message().decode(errors="replace")
+        raise SpectralError(f"{what}: {msg}")
+
+
+def declared_symbols(header: str = HEADER) -> list[str]:
+    """Function names declared in include/spectral_bte.h."""
+    import re
+    txt = open(header).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    names = re.findall(r"^[A-Za-z_][\w \*]*?\b([A-Za-z_]\w*)\s*\(", txt, flags=re.M)
+    skip = {"if", "defined", "typedef", "struct"}
+    return sorted({n for n in names if n not in skip})
+
+
+# --------------------------------------------------------------------------
+class ReferenceAPI:
+    """One-for-one mirror of the reference's C entry points.
+
+    Like the reference, the library keeps one collision grid, one set of
+    conservation factors and per-table weights as module state.
+    """
+
+    def __init__(self):
+        self.L = lib()
+        self._keep = []
+        self._tables = {}
+
+    def reset_error(self):
+        # spectral_last_error is sticky; reading it does not clear, so the
+        # mirror compares before/after codes through fresh calls only.
+        pass
+
+    def initialize_coll(self, N: int, L_v: float, v: np.ndarray, zeta: np.ndarray):
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        zeta = np.ascontiguousarray(zeta, dtype=np.float64)
+        self._keep += [v, zeta]
+        self.N, self.n3 = N, N ** 3
+        self.L.initialize_coll(N, float(L_v), _p(v), _p(zeta))
+
+    def dealloc_coll(self):
+        self.L.dealloc_coll()
+
+    def rows(self, W: np.ndarray):
+        """A double** over the rows of a [N^3][N^3] array (kept alive)."""
+        W = np.ascontiguousarray(W, dtype=np.float64)
+        n3 = W.shape[0]
+        ptrs = (_dp * n3)(*[C.cast(W.ctypes.data + 8 * n3 * r, _dp) for r in range(n3)])
+        self._tables[C.addressof(ptrs)] = (W, ptrs)
+        return ptrs
+
+    def ComputeQ(self, f, g, W_rows) -> np.ndarray:
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        g = f if g is None else np.ascontiguousarray(g, dtype=np.float64)
+        Q = np.zeros(self.n3)
+        self.L.ComputeQ(_p(f), _p(g), _p(Q), W_rows)
+        return Q
+
+    def ComputeQ_maxPreserve(self, f, g, W_rows) -> np.ndarray:
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        g = f if g is None else np.ascontiguousarray(g, dtype=np.float64)
+        Q = np.zeros(self.n3)
+        self.L.ComputeQ_maxPreserve(_p(f), _p(g), _p(Q), W_rows)
+        return Q
+
+    def fft3D(self, x, invert: int) -> np.ndarray:
+        a = np.ascontiguousarray(np.asarray(x, dtype=np.complex128)).view(np.float64)
+        out = np.zeros_like(a)
+        self.L.fft3D(_p(a), _p(out), int(invert))
+        return out.view(np.complex128)
+
+    def initialize_conservation(self, N, h_v, v, masses=(1.0,)):
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        self._keep.append(v)
+        sp = (Species * len(masses))(*[Species.default(mass=m) for m in masses])
+        self._keep.append(sp)
+        self.L.initialize_conservation(N, float(h_v), _p(v), sp, len(masses))
+
+    def conserveAllMoments(self, Qs):
+        """Qs: list of Ns*Ns arrays of N^3 (modified copies returned)."""
+        arrs = [np.array(q, dtype=np.float64, copy=True) for q in Qs]
+        ptrs = (_dp * len(arrs))(*[_p(a) for a in arrs])
+        self.L.conserveAllMoments(ptrs)
+        return arrs
+
+    def alloc_weights(self, N, total_species=1):
+        """weights.c:26-31; returns the double** table of each species pair."""
+        out = C.c_void_p()
+        self.L.alloc_weights(N, C.byref(out), total_species)
+        tbl = C.cast(out, C.POINTER(C.POINTER(_dp)))  # double***
+        self._keep.append(out)
+        return [tbl[i] for i in range(total_species)]
+
+    def initialize_weights(self, N, zeta, L_v, lam, weightFlag, isoFlag, table,
+                           sp_i=None, sp_j=None):
+        zeta = np.ascontiguousarray(zeta, dtype=np.float64)
+        self._keep.append(zeta)
+        sp_i = sp_i or Species.default()
+        sp_j = sp_j or Species.default()
+        self.L.initialize_weights(N, _p(zeta), float(L_v), float(lam), int(weightFlag),
+                                  int(isoFlag), table, sp_i, sp_j)
+
+    def table_to_numpy(self, table, N) -> np.ndarray:
+        n3 = N ** 3
+        W = np.empty((n3, n3))
+        for r in range(n3):
+            C.memmove(W[r].ctypes.data, table[r], 8 * n3)
+        return W
+
+    def dealloc_weights(self, N, table):
+        self.L.dealloc_weights(N, table)
+
+
+# --------------------------------------------------------------------------
+def _ptr(x) -> int:
+    """Device pointer of a torch CUDA tensor, or an int address."""
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        if not x.is_cuda:
+            raise SpectralError("expected a CUDA tensor")
+        if not x.is_contiguous() or x.dtype.itemsize != 8:
+            raise SpectralError("expected a contiguous float64 tensor")
+        return x.data_ptr()
+    raise SpectralError(f"cannot take a device pointer of {type(x)}")
+
+
+def _stream(stream) -> Optional[int]:
+    """The CUDA stream to launch on: the given handle, else torch's current
+    stream, so the library's work is ordered with the caller's torch ops."""
+    if stream:
+        return int(stream)
+    try:
+        import torch
+        if torch.cuda.is_available():
+            return int(torch.cuda.current_stream().cuda_stream) or None
+    except Exception:
+        pass
+    return None
+
+
+class Plan:
+    """Batched device operator for one velocity grid (spectral_plan).
+
+    Device calls run on the caller's stream (torch's current stream unless
+    one is given) and are asynchronous like any CUDA launch.
+    """
+
+    def __init__(self, N: int, L_v: float, v: np.ndarray, zeta: np.ndarray,
+                 max_batch: int = 1):
+        self.L = lib()
+        self.N, self.n3, self.L_v = N, N ** 3, float(L_v)
+        self.v = np.ascontiguousarray(v, dtype=np.float64)
+        self.zeta = np.ascontiguousarray(zeta, dtype=np.float64)
+        h = C.c_void_p()
+        _check(self.L.spectral_plan_create(C.byref(h), N, self.L_v, _p(self.v),
+                                           _p(self.zeta), max_batch),
+               "spectral_plan_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.spectral_plan_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_weights(self, W):
+        if isinstance(W, np.ndarray):
+            W = np.ascontiguousarray(W, dtype=np.float64)
+            _check(self.L.spectral_plan_set_weights(self.h, W.ctypes.data, 0), "set_weights")
+        else:
+            _check(self.L.spectral_plan_set_weights(self.h, _ptr(W), 1), "set_weights")
+
+    def generate_weights_iso(self, lam: float, d_i=2.0, d_j=2.0, m_i=1.0, m_j=1.0):
+        _check(self.L.spectral_plan_generate_weights_iso(self.h, float(lam), d_i, d_j, m_i, m_j),
+               "generate_weights_iso")
+
+    def get_weights(self, row0: int = 0, nrows: Optional[int] = None) -> np.ndarray:
+        nrows = self.n3 - row0 if nrows is None else nrows
+        W = np.empty((nrows, self.n3))
+        _check(self.L.spectral_plan_get_weights(self.h, _p(W), row0, nrows), "get_weights")
+        return W
+
+    def set_conservation(self, mass: float = 1.0):
+        _check(self.L.spectral_plan_set_conservation(self.h, float(mass)), "set_conservation")
+
+    def computeQ_device(self, f, Q, B: int, flags: int = FP64, stream: int = 0):
+        _check(self.L.spectral_computeQ_device(self.h, _ptr(f), _ptr(Q), B, flags,
+                                               _stream(stream)), "computeQ_device")
+
+    def computeQ_host(self, f: np.ndarray, flags: int = FP64) -> np.ndarray:
+        f = np.ascontiguousarray(f, dtype=np.float64).reshape(-1, self.n3)
+        Q = np.empty_like(f)
+        _check(self.L.spectral_computeQ_host(self.h, _p(f), _p(Q), f.shape[0], flags),
+               "computeQ_host")
+        return Q
+
+    def conserve_device(self, Q, B: int, stream: int = 0):
+        _check(self.L.spectral_conserve_device(self.h, _ptr(Q), B, _stream(stream)),
+               "conserve_device")
+
+    def step_device(self, f, B: int, dt: float, Kn: float, order: int, flags: int = FP64,
+                    stream: int = 0):
+        _check(self.L.spectral_step_device(self.h, _ptr(f), B, float(dt), float(Kn), order,
+                                           flags, _stream(stream)), "step_device")
+
+    def set_tuning(self, bg: int, stages: int, flush: int):
+        _check(self.L.spectral_plan_set_tuning(self.h, bg, stages, flush), "set_tuning")
+
+    def autotune(self, B: int, flags: int = FP32) -> tuple:
+        out = (C.c_int * 3)()
+        _check(self.L.spectral_plan_autotune(self.h, B, flags, out), "autotune")
+        return tuple(out)
+
+    def status(self) -> int:
+        s = C.c_uint()
+        _check(self.L.spectral_plan_status(self.h, C.byref(s)), "status")
+        return s.value
+
+    def sync(self):
+        _check(self.L.spectral_plan_sync(self.h), "sync")
+
+    def set_profiling(self, on: bool):
+        _check(self.L.spectral_plan_set_profiling(self.h, 1 if on else 0), "set_profiling")
+
+    def conv_time(self) -> tuple:
+        """(summed convolution-kernel ms, launches) since the last query."""
+        ms = C.c_double()
+        n = C.c_int()
+        _check(self.L.spectral_plan_conv_time(self.h, C.byref(ms), C.byref(n)), "conv_time")
+        return ms.value, n.value
+
+
+def kernel_launches() -> int:
+    return int(lib().spectral_kernel_launches())

@@ -1,0 +1,1417 @@
+// capi.cu -- the C ABI of libspectral_gb300.so (include/spectral_bte.h).
+//
+// Part 1 keeps the reference's module state (collisions.c:11-24,
+// conserve.c:7-15, weights.c:11-24) as process-wide statics, exactly as the
+// reference does, and runs every collision computation on the GPU.  The
+// caller's host arrays are copied in and out per call, so an unmodified
+// boltz.c runs against this library.
+// Part 2 (spectral_plan) keeps everything resident on the device.
+#include "common.cuh"
+#include "kernels.h"
+#include "../../include/spectral_bte.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+namespace sbte {
+
+// ------------------------------------------------------------- errors ---
+static int g_last_error = 0;
+static char g_last_msg[512] = "";
+static std::atomic<long long> g_launches{0};
+
+void set_error(int code, const char *fmt, ...)
+{
+    g_last_error = code;
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_last_msg, sizeof(g_last_msg), fmt, ap);
+    va_end(ap);
+}
+int last_error() { return g_last_error; }
+const char *last_message() { return g_last_msg; }
+
+static void count(int n) { g_launches += n; }
+
+#define SBTE_TRY(expr)                                                     \
+    do {                                                                   \
+        int rc_ = (expr);                                                  \
+        if (rc_ != kOk) return rc_;                                        \
+    } while (0)
+
+#define SBTE_LAUNCH(call, nk)                                              \
+    do {                                                                   \
+        cudaError_t e_ = (call);                                           \
+        if (e_ != cudaSuccess) {                                           \
+            set_error(kErrCuda, "%s:%d %s: %s", __FILE__, __LINE__, #call,  \
+                      cudaGetErrorString(e_));                             \
+            return kErrCuda;                                               \
+        }                                                                  \
+        count(nk);                                                         \
+    } while (0)
+
+static int ensure_device()
+{
+    static int ready = -1;
+    if (ready == 1) return kOk;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+        set_error(kErrCuda,
+                  "no CUDA device available (%s); this library has no CPU path",
+                  e != cudaSuccess ? cudaGetErrorString(e) : "count 0");
+        return kErrCuda;
+    }
+    SBTE_CUDA(cudaFree(0));
+    ready = 1;
+    return kOk;
+}
+
+template <typename T>
+static int dalloc(T **p, size_t count_elems)
+{
+    *p = nullptr;
+    if (count_elems == 0) return kOk;
+    cudaError_t e = cudaMalloc((void **)p, count_elems * sizeof(T));
+    if (e != cudaSuccess) {
+        set_error(kErrNoMem, "cudaMalloc of %zu bytes failed: %s",
+                  count_elems * sizeof(T), cudaGetErrorString(e));
+        *p = nullptr;
+        return kErrNoMem;
+    }
+    return kOk;
+}
+
+template <typename T> static void dfree(T *&p)
+{
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+static inline double trap_wt(int i, int N) { return (i == 0 || i == N - 1) ? 0.5 : 1.0; }
+
+// --------------------------------------------- host-side math helpers ---
+
+// The phase-shifted axis matrix of fft3D (see kernels.h), transposed:
+// Dt[n*N + k] = D[k][n].  Module quantities as initialize_coll derives them
+// (collisions.c:36-46): dv = v[1]-v[0], deta = zeta[1]-zeta[0],
+// L_eta = -zeta[0], scale3 = (2 pi)^(-3/2).
+static void build_axis_matrix(int N, double L_v, const double *v,
+                              const double *zeta, bool inverse,
+                              std::vector<double2> &Dt, double &prefactor)
+{
+    const double dv = v[1] - v[0], deta = zeta[1] - zeta[0], L_eta = -zeta[0];
+    const double scale3 = pow(1.0 / sqrt(2.0 * M_PI), 3.0);
+    double delta, L_start, L_end, sign, fsign;
+    const double *varr;
+    if (!inverse) {  // collisions.c:238-245, FFTW_FORWARD
+        delta = dv; L_start = L_eta; L_end = L_v; varr = zeta; sign = 1.0; fsign = -1.0;
+    } else {         // collisions.c:246-253, FFTW_BACKWARD
+        delta = deta; L_start = L_v; L_end = L_eta; varr = v; sign = -1.0; fsign = 1.0;
+    }
+    prefactor = scale3 * delta * delta * delta;
+    Dt.assign((size_t)N * N, make_double2(0, 0));
+    for (int k = 0; k < N; k++) {
+        const double ap = sign * L_end * varr[k];
+        for (int n = 0; n < N; n++) {
+            const double aq = sign * (double)n * L_start * delta;
+            const double ad = fsign * 2.0 * M_PI * (double)(((long long)n * k) % N) / (double)N;
+            // e^{i ap} e^{i ad} e^{i aq} wt[n]
+            double cr = cos(ap), ci = sin(ap);
+            double tr = cos(ad), ti = sin(ad);
+            double r1 = cr * tr - ci * ti, i1 = cr * ti + ci * tr;
+            double ur = cos(aq), ui = sin(aq);
+            double r2 = r1 * ur - i1 * ui, i2 = r1 * ui + i1 * ur;
+            const double w = trap_wt(n, N);
+            Dt[(size_t)n * N + k] = make_double2(w * r2, w * i2);
+        }
+    }
+}
+
+// Gauss-Legendre nodes/weights on [-1, 1] by Newton iteration on the
+// three-term Legendre recurrence (Davis & Rabinowitz).
+static void gl_nodes(int n, std::vector<double> &x, std::vector<double> &w)
+{
+    x.assign(n, 0.0);
+    w.assign(n, 0.0);
+    for (int i = 1; i <= (n + 1) / 2; i++) {
+        double z = cos(M_PI * (i - 0.25) / (n + 0.5)), dp = 1.0;
+        for (int it = 0; it < 100; it++) {
+            double p0 = 1.0, p1 = z;
+            for (int k = 2; k <= n; k++) {
+                const double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+                p0 = p1;
+                p1 = p2;
+            }
+            dp = n * (z * p1 - p0) / (z * z - 1.0);
+            const double dz = p1 / dp;
+            z -= dz;
+            if (fabs(dz) < 1e-16) break;
+        }
+        double p0 = 1.0, p1 = z;
+        for (int k = 2; k <= n; k++) {
+            const double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+            p0 = p1;
+            p1 = p2;
+        }
+        dp = n * (z * p1 - p0) / (z * z - 1.0);
+        x[i - 1] = -z;
+        x[n - i] = z;
+        w[i - 1] = w[n - i] = 2.0 / ((1.0 - z * z) * dp * dp);
+    }
+}
+
+// CC^T of createCCtAndPivot (conserve.c:268-317) and its LU factors by the
+// scaled-pivot elimination of factorMatrixIntoLU (conserve.c:89-168):
+// the pivot row is the first row whose scaled entry beats the running
+// best, and only columns >= k are exchanged.
+static int build_conservation(ConsParams &cp, int N, double dv, const double *v,
+                              const double *mass, int Ns)
+{
+    memset(&cp, 0, sizeof(cp));
+    cp.N = N;
+    cp.Ns = Ns;
+    cp.dv = dv;
+    for (int m = 0; m < Ns; m++) cp.mass[m] = mass[m];
+    const int ne = Ns + 4;
+    double A[8][8] = {};
+    for (int m = 0; m < Ns; m++)
+        for (int i = 0; i < N; i++)
+            for (int j = 0; j < N; j++)
+                for (int k = 0; k < N; k++) {
+                    const double pre =
+                        trap_wt(i, N) * trap_wt(j, N) * trap_wt(k, N) * dv * dv * dv * mass[m];
+                    double c[8] = {};
+                    c[m] = pre;
+                    c[Ns] = pre * v[i];
+                    c[Ns + 1] = pre * v[j];
+                    c[Ns + 2] = pre * v[k];
+                    c[Ns + 3] = pre * 0.5 * (v[i] * v[i] + v[j] * v[j] + v[k] * v[k]);
+                    for (int a = 0; a < ne; a++)
+                        for (int b = 0; b < ne; b++) A[a][b] += c[a] * c[b];
+                }
+    double s[8], cc[8];
+    for (int i = 0; i < ne; i++) {
+        s[i] = fabs(A[i][0]);
+        for (int j = 0; j < ne; j++)
+            if (s[i] < fabs(A[i][j])) s[i] = fabs(A[i][j]);
+    }
+    for (int k = 0; k < ne - 1; k++) {
+        cc[k] = fabs(A[k][k] / s[k]);
+        int ctr = 0, i0 = k;
+        for (int i = k; i < ne; i++) {
+            if (cc[k] < fabs(A[i][k] / s[i])) {
+                cc[k] = fabs(A[i][k] / s[i]);
+                if (ctr != 1) {
+                    i0 = i;
+                    ctr = 1;
+                }
+            }
+        }
+        cp.pivot[k] = i0;
+        if (cc[k] == 0.0) {
+            set_error(kErrSingular, "conservation matrix CC^T is singular");
+            return kErrSingular;
+        }
+        if (i0 != k) {
+            for (int j = k; j < ne; j++) std::swap(A[k][j], A[i0][j]);
+            std::swap(s[k], s[i0]);
+        }
+        for (int i = k + 1; i < ne; i++) {
+            const double mult = A[i][k] / A[k][k];
+            A[i][k] = mult;
+            for (int j = k + 1; j < ne; j++) A[i][j] -= mult * A[k][j];
+        }
+    }
+    for (int a = 0; a < 8; a++)
+        for (int b = 0; b < 8; b++) cp.CCt[a][b] = A[a][b];
+    return kOk;
+}
+
+static void solve_cct_host(const ConsParams &cp, double *b, int n)
+{
+    for (int k = 0; k < n - 1; k++) {
+        const int i = cp.pivot[k];
+        if (i != k) std::swap(b[i], b[k]);
+        for (int r = k + 1; r < n; r++) b[r] -= cp.CCt[r][k] * b[k];
+    }
+    b[n - 1] = b[n - 1] / cp.CCt[n - 1][n - 1];
+    for (int i = n - 2; i >= 0; i--) {
+        double sum = 0.0;
+        for (int j = i + 1; j < n; j++) sum += cp.CCt[i][j] * b[j];
+        b[i] = 1.0 / cp.CCt[i][i] * (b[i] - sum);
+    }
+}
+
+// ------------------------------------------------------------- weights ---
+struct WeightsDev {
+    int N = 0;
+    double *w64 = nullptr;  // row-major [N^3][N^3]
+    float *w32 = nullptr;   // tiled FP32 (built on first FP32 use)
+    void release()
+    {
+        dfree(w64);
+        dfree(w32);
+        N = 0;
+    }
+};
+
+// Device W from a flat host or device array, or from host row pointers.
+static int upload_weights(WeightsDev &wd, int N, const double *flat,
+                          double **rows, bool flat_on_device, cudaStream_t st)
+{
+    const long long n3 = (long long)N * N * N;
+    if (wd.N != N || !wd.w64) {
+        wd.release();
+        SBTE_TRY(dalloc(&wd.w64, (size_t)(n3 * n3)));
+        wd.N = N;
+    }
+    dfree(wd.w32);
+    if (flat) {
+        SBTE_CUDA(cudaMemcpyAsync(wd.w64, flat, sizeof(double) * n3 * n3,
+                                  flat_on_device ? cudaMemcpyDeviceToDevice
+                                                 : cudaMemcpyHostToDevice,
+                                  st));
+        SBTE_CUDA(cudaStreamSynchronize(st));
+        return kOk;
+    }
+    // rows: stage through a pinned buffer of up to 64 MiB
+    const long long chunk_rows = std::max<long long>(1, (64ll << 20) / (8 * n3));
+    double *stage = nullptr;
+    SBTE_CUDA(cudaMallocHost((void **)&stage, sizeof(double) * chunk_rows * n3));
+    for (long long r0 = 0; r0 < n3; r0 += chunk_rows) {
+        const long long nr = std::min(chunk_rows, n3 - r0);
+        SBTE_CUDA(cudaStreamSynchronize(st));
+        for (long long r = 0; r < nr; r++)
+            memcpy(stage + r * n3, rows[r0 + r], sizeof(double) * n3);
+        cudaError_t e = cudaMemcpyAsync(wd.w64 + r0 * n3, stage, sizeof(double) * nr * n3,
+                                        cudaMemcpyHostToDevice, st);
+        if (e != cudaSuccess) {
+            cudaFreeHost(stage);
+            set_error(kErrCuda, "weight upload: %s", cudaGetErrorString(e));
+            return kErrCuda;
+        }
+    }
+    SBTE_CUDA(cudaStreamSynchronize(st));
+    cudaFreeHost(stage);
+    return kOk;
+}
+
+static int ensure_w32(WeightsDev &wd, cudaStream_t st)
+{
+    if (wd.w32) return kOk;
+    const long long n3 = (long long)wd.N * wd.N * wd.N;
+    SBTE_TRY(dalloc(&wd.w32, (size_t)(n3 * n3)));
+    SBTE_LAUNCH(weights_to_tiled_f32(wd.w64, wd.w32, wd.N, st), 1);
+    SBTE_CUDA(cudaStreamSynchronize(st));
+    return kOk;
+}
+
+struct IsoWeightSpec {
+    int N = 0;
+    double L_v = 0, lambda = 0, d_i = 2, d_j = 2, m_i = 1, m_j = 1;
+    std::vector<double> zeta;
+};
+
+// Quadrature on the GPU into wd.w64.
+static int generate_iso_device(WeightsDev &wd, const IsoWeightSpec &s,
+                               cudaStream_t st)
+{
+    const int N = s.N;
+    const long long n3 = (long long)N * N * N;
+    if (wd.N != N || !wd.w64) {
+        wd.release();
+        SBTE_TRY(dalloc(&wd.w64, (size_t)(n3 * n3)));
+        wd.N = N;
+    }
+    dfree(wd.w32);
+    WeightParams wp;
+    wp.N = N;
+    wp.L_v = s.L_v;
+    wp.lambda = s.lambda;
+    wp.mu = s.m_j / (s.m_i + s.m_j);  // weights.c:190
+    wp.dfac = 0.25 * pow(0.5 * (s.d_i + s.d_j), 2);  // weights.c:277
+    const double deta = s.zeta[1] - s.zeta[0];
+    wp.prefactor = 16.0 * M_PI * M_PI * deta * deta * deta / pow(2.0 * M_PI, 1.5) /
+                   (4.0 * M_PI);  // weights.c:44
+    wp.zmax = std::max(fabs(s.zeta[0]), fabs(s.zeta[N - 1]));
+    if (weights_panels_needed(wp) > kWeightMaxPanels) {
+        set_error(kErrUnsupported, "weight quadrature: grid too wide (N=%d, L_v=%g)",
+                  N, s.L_v);
+        return kErrUnsupported;
+    }
+    std::vector<double> gx, gw;
+    gl_nodes(16, gx, gw);
+    double *d_zeta = nullptr, *d_gx = nullptr, *d_gw = nullptr, *d_loss = nullptr;
+    int rc = kOk;
+    if ((rc = dalloc(&d_zeta, N)) || (rc = dalloc(&d_gx, 16)) || (rc = dalloc(&d_gw, 16)) ||
+        (rc = dalloc(&d_loss, (size_t)n3))) {
+        dfree(d_zeta); dfree(d_gx); dfree(d_gw); dfree(d_loss);
+        return rc;
+    }
+    cudaMemcpyAsync(d_zeta, s.zeta.data(), sizeof(double) * N, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(d_gx, gx.data(), sizeof(double) * 16, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(d_gw, gw.data(), sizeof(double) * 16, cudaMemcpyHostToDevice, st);
+    // rows in chunks so that no single launch runs for long
+    const int chunk = 4096;
+    for (long long r0 = 0; r0 < n3 && rc == kOk; r0 += chunk) {
+        const int nr = (int)std::min<long long>(chunk, n3 - r0);
+        cudaError_t e = weights_iso(wd.w64 + r0 * n3, (int)r0, nr, d_zeta, wp, d_gx, d_gw,
+                                    d_loss, st);
+        if (e != cudaSuccess) {
+            set_error(kErrCuda, "weights_iso: %s", cudaGetErrorString(e));
+            rc = kErrCuda;
+        } else {
+            count(2);
+        }
+    }
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (rc == kOk && e != cudaSuccess) {
+        set_error(kErrCuda, "weights_iso: %s", cudaGetErrorString(e));
+        rc = kErrCuda;
+    }
+    dfree(d_zeta); dfree(d_gx); dfree(d_gw); dfree(d_loss);
+    return rc;
+}
+
+}  // namespace sbte
+
+using namespace sbte;
+
+// ================================================================ plan ===
+struct spectral_plan_s {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int N = 0;
+    long long n3 = 0;
+    double L_v = 0;
+    std::vector<double> v, zeta;
+    double *d_v = nullptr;
+    double2 *Dfwd64 = nullptr, *Dinv64 = nullptr;
+    float2 *Dfwd32 = nullptr, *Dinv32 = nullptr;
+    double pf_fwd = 0, pf_inv = 0;
+    WeightsDev W;
+    ConsParams cons{};
+    bool cons_ready = false;
+    double mom_mass = 1.0, mom_KB = 1.0;
+    ConvF32Config tune{64, 3, 16};
+    unsigned int *d_status = nullptr;
+    // FP64 scratch: capacity cap64 instances
+    int cap64 = 0;
+    double2 *c64[6] = {};  // fhat, ghat, R, S(=Mhat), T, qhat
+    double2 *tmp64 = nullptr;
+    double *r64[4] = {};   // Mi, gi, Mj, gj
+    // FP32 scratch: capacity cap32 instances (padded to 128)
+    int cap32 = 0;
+    float2 *c32[4] = {};   // P, R, S, T (bg-interleaved)
+    double2 *qacc = nullptr;
+    float2 *tmp32 = nullptr;
+    double *r32[2] = {};   // M, g
+    // time-step scratch
+    int capstep = 0;
+    double *sQ = nullptr, *sf1 = nullptr;
+    // CUDA-event timing of the dominant (convolution) kernel
+    bool profiling = false;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_events;
+    size_t prof_used = 0;
+    // host staging for spectral_computeQ_host
+    int caphost = 0;
+    double *d_fh = nullptr, *d_Qh = nullptr;
+
+    ~spectral_plan_s()
+    {
+        if (device >= 0) cudaSetDevice(device);
+        dfree(d_v);
+        dfree(Dfwd64); dfree(Dinv64); dfree(Dfwd32); dfree(Dinv32);
+        W.release();
+        dfree(d_status);
+        for (auto &p : c64) dfree(p);
+        dfree(tmp64);
+        for (auto &p : r64) dfree(p);
+        for (auto &p : c32) dfree(p);
+        dfree(qacc); dfree(tmp32);
+        for (auto &p : r32) dfree(p);
+        dfree(sQ); dfree(sf1); dfree(d_fh); dfree(d_Qh);
+        for (auto &ev : prof_events) {
+            cudaEventDestroy(ev.first);
+            cudaEventDestroy(ev.second);
+        }
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace sbte {
+
+static int plan_init(spectral_plan_s *p, int N, double L_v, const double *v,
+                     const double *zeta)
+{
+    if (N < 2 || N > 64) {
+        set_error(kErrArg, "N=%d outside the supported range 2..64", N);
+        return kErrArg;
+    }
+    SBTE_TRY(ensure_device());
+    SBTE_CUDA(cudaGetDevice(&p->device));
+    SBTE_CUDA(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
+    p->N = N;
+    p->n3 = (long long)N * N * N;
+    p->L_v = L_v;
+    p->v.assign(v, v + N);
+    p->zeta.assign(zeta, zeta + N);
+    SBTE_TRY(dalloc(&p->d_v, N));
+    SBTE_CUDA(cudaMemcpy(p->d_v, v, sizeof(double) * N, cudaMemcpyHostToDevice));
+    std::vector<double2> Df, Di;
+    build_axis_matrix(N, L_v, v, zeta, false, Df, p->pf_fwd);
+    build_axis_matrix(N, L_v, v, zeta, true, Di, p->pf_inv);
+    std::vector<float2> Df32(Df.size()), Di32(Di.size());
+    for (size_t i = 0; i < Df.size(); i++) {
+        Df32[i] = make_float2((float)Df[i].x, (float)Df[i].y);
+        Di32[i] = make_float2((float)Di[i].x, (float)Di[i].y);
+    }
+    SBTE_TRY(dalloc(&p->Dfwd64, Df.size()));
+    SBTE_TRY(dalloc(&p->Dinv64, Di.size()));
+    SBTE_TRY(dalloc(&p->Dfwd32, Df.size()));
+    SBTE_TRY(dalloc(&p->Dinv32, Di.size()));
+    SBTE_CUDA(cudaMemcpy(p->Dfwd64, Df.data(), sizeof(double2) * Df.size(), cudaMemcpyHostToDevice));
+    SBTE_CUDA(cudaMemcpy(p->Dinv64, Di.data(), sizeof(double2) * Di.size(), cudaMemcpyHostToDevice));
+    SBTE_CUDA(cudaMemcpy(p->Dfwd32, Df32.data(), sizeof(float2) * Df.size(), cudaMemcpyHostToDevice));
+    SBTE_CUDA(cudaMemcpy(p->Dinv32, Di32.data(), sizeof(float2) * Di.size(), cudaMemcpyHostToDevice));
+    SBTE_TRY(dalloc(&p->d_status, 2));
+    SBTE_CUDA(cudaMemset(p->d_status, 0, 2 * sizeof(unsigned)));
+    const double mass = 1.0;
+    SBTE_TRY(build_conservation(p->cons, N, v[1] - v[0], v, &mass, 1));
+    p->cons_ready = true;
+    return kOk;
+}
+
+static int ensure64(spectral_plan_s *p, int B)
+{
+    if (B <= p->cap64) return kOk;
+    for (auto &q : p->c64) dfree(q);
+    dfree(p->tmp64);
+    for (auto &q : p->r64) dfree(q);
+    p->cap64 = 0;
+    const size_t n = (size_t)B * p->n3;
+    for (auto &q : p->c64) SBTE_TRY(dalloc(&q, n));
+    SBTE_TRY(dalloc(&p->tmp64, n));
+    for (auto &q : p->r64) SBTE_TRY(dalloc(&q, n));
+    SBTE_CUDA(cudaDeviceSynchronize());
+    p->cap64 = B;
+    return kOk;
+}
+
+static int ensure32(spectral_plan_s *p, int B)
+{
+    const int padB = (B + 127) / 128 * 128;
+    if (padB <= p->cap32) return kOk;
+    for (auto &q : p->c32) dfree(q);
+    dfree(p->qacc); dfree(p->tmp32);
+    for (auto &q : p->r32) dfree(q);
+    p->cap32 = 0;
+    const size_t n = (size_t)padB * p->n3;
+    for (auto &q : p->c32) {
+        SBTE_TRY(dalloc(&q, n));
+        SBTE_CUDA(cudaMemset(q, 0, n * sizeof(float2)));
+    }
+    SBTE_TRY(dalloc(&p->qacc, n));
+    SBTE_TRY(dalloc(&p->tmp32, (size_t)B * p->n3));
+    for (auto &q : p->r32) SBTE_TRY(dalloc(&q, (size_t)B * p->n3));
+    SBTE_CUDA(cudaDeviceSynchronize());
+    p->cap32 = padB;
+    return kOk;
+}
+
+static int ensure_step(spectral_plan_s *p, int B)
+{
+    if (B <= p->capstep) return kOk;
+    dfree(p->sQ); dfree(p->sf1);
+    p->capstep = 0;
+    SBTE_TRY(dalloc(&p->sQ, (size_t)B * p->n3));
+    SBTE_TRY(dalloc(&p->sf1, (size_t)B * p->n3));
+    SBTE_CUDA(cudaDeviceSynchronize());
+    p->capstep = B;
+    return kOk;
+}
+
+// Event pair bracketing one convolution launch when profiling is on.
+static std::pair<cudaEvent_t, cudaEvent_t> *prof_slot(spectral_plan_s *p)
+{
+    if (!p->profiling) return nullptr;
+    if (p->prof_used == p->prof_events.size()) {
+        cudaEvent_t a, b;
+        if (cudaEventCreate(&a) != cudaSuccess) return nullptr;
+        if (cudaEventCreate(&b) != cudaSuccess) {
+            cudaEventDestroy(a);
+            return nullptr;
+        }
+        p->prof_events.emplace_back(a, b);
+    }
+    return &p->prof_events[p->prof_used++];
+}
+
+// Complex add out = a + b over n complex values (FP64), via the axpy
+// kernel on interleaved doubles.
+static int cadd64(double2 *out, const double2 *a, const double2 *b, long long n,
+                  cudaStream_t st)
+{
+    SBTE_CUDA(cudaMemcpyAsync(out, a, sizeof(double2) * n, cudaMemcpyDeviceToDevice, st));
+    SBTE_LAUNCH(axpy_update((double *)out, (const double *)b, nullptr, 1.0, 1.0, 0.0,
+                            2 * n, st), 1);
+    return kOk;
+}
+
+// Q for B instances in FP64 (plain operator).  fdev/gdev: [B][N^3]; when
+// gdev == fdev the second transform is skipped.  Q_dev receives Re(IFFT).
+static int q_fp64(spectral_plan_s *p, const WeightsDev &W, const double *fdev,
+                  const double *gdev, double *Qdev, int B, bool maxpreserve,
+                  cudaStream_t st)
+{
+    SBTE_TRY(ensure64(p, B));
+    const int N = p->N;
+    const long long n3 = p->n3;
+    double2 *A = p->c64[0], *Bh = p->c64[1], *R = p->c64[2], *S = p->c64[3],
+            *T = p->c64[4], *qh = p->c64[5];
+    if (!maxpreserve) {
+        SBTE_LAUNCH(dft3_f64(fdev, DftIn::kRealF64, 1, p->tmp64, A, DftOut::kComplexF64, 1,
+                             p->Dfwd64, p->pf_fwd, N, B, st), 2);
+        const double2 *G = A;
+        if (gdev != fdev) {
+            SBTE_LAUNCH(dft3_f64(gdev, DftIn::kRealF64, 1, p->tmp64, Bh,
+                                 DftOut::kComplexF64, 1, p->Dfwd64, p->pf_fwd, N, B, st), 2);
+            G = Bh;
+        }
+        // qhat[zeta] = sum W ghat[xi] fhat[idx]  (collisions.c:162-163)
+        auto *ev = prof_slot(p);
+        if (ev) cudaEventRecord(ev->first, st);
+        SBTE_LAUNCH(conv_f64(W.w64, G, A, nullptr, nullptr, qh, N, B, st), 1);
+        if (ev) cudaEventRecord(ev->second, st);
+    } else {
+        double *Mi = p->r64[0], *gi = p->r64[1], *Mj = p->r64[2], *gj = p->r64[3];
+        // find_maxwellians (collisions.c:181-182): both g's subtract M_i
+        SBTE_LAUNCH(maxwellian_split(fdev, Mi, gi, nullptr, B, N, p->d_v, p->mom_mass,
+                                     p->mom_KB, nullptr, st), 1);
+        SBTE_LAUNCH(maxwellian_split(gdev, Mj, gj, Mi, B, N, p->d_v, p->mom_mass,
+                                     p->mom_KB, nullptr, st), 1);
+        // Q(M_i,g_j) + Q(g_i,M_j) + Q(g_i,g_j) in one W pass:
+        //   sum W [ghat_j (Mhat_i + ghat_i)[idx] + Mhat_j ghat_i[idx]]
+        SBTE_LAUNCH(dft3_f64(Mi, DftIn::kRealF64, 1, p->tmp64, A, DftOut::kComplexF64, 1,
+                             p->Dfwd64, p->pf_fwd, N, B, st), 2);   // Mhat_i
+        SBTE_LAUNCH(dft3_f64(gi, DftIn::kRealF64, 1, p->tmp64, T, DftOut::kComplexF64, 1,
+                             p->Dfwd64, p->pf_fwd, N, B, st), 2);   // ghat_i
+        SBTE_LAUNCH(dft3_f64(Mj, DftIn::kRealF64, 1, p->tmp64, S, DftOut::kComplexF64, 1,
+                             p->Dfwd64, p->pf_fwd, N, B, st), 2);   // Mhat_j
+        SBTE_LAUNCH(dft3_f64(gj, DftIn::kRealF64, 1, p->tmp64, Bh, DftOut::kComplexF64, 1,
+                             p->Dfwd64, p->pf_fwd, N, B, st), 2);   // ghat_j
+        SBTE_TRY(cadd64(R, A, T, (long long)B * n3, st));
+        auto *ev = prof_slot(p);
+        if (ev) cudaEventRecord(ev->first, st);
+        SBTE_LAUNCH(conv_f64(W.w64, Bh, R, S, T, qh, N, B, st), 1);
+        if (ev) cudaEventRecord(ev->second, st);
+    }
+    SBTE_LAUNCH(dft3_f64(qh, DftIn::kComplexF64, 1, p->tmp64, Qdev, DftOut::kRealF64, 1,
+                         p->Dinv64, p->pf_inv, N, B, st), 2);
+    return kOk;
+}
+
+// Q for B instances with the FP32 batched convolution and FP32 transforms
+// (f = g).  Moments, Maxwellian split and conservation stay FP64.
+static int q_fp32(spectral_plan_s *p, const double *fdev, double *Qdev, int B,
+                  bool maxpreserve, cudaStream_t st)
+{
+    SBTE_TRY(ensure32(p, B));
+    SBTE_TRY(ensure_w32(p->W, st));
+    const int N = p->N;
+    ConvF32Config cfg = p->tune;
+    if (!conv_f32_supported(N, cfg, maxpreserve)) {
+        // the two-pair form stages twice the rows: fall back to a narrower
+        // instance group that fits in shared memory
+        const ConvF32Config fallback[] = {{64, 2, cfg.flush}, {32, 2, cfg.flush}};
+        bool found = false;
+        for (const auto &c : fallback)
+            if (!found && conv_f32_supported(N, c, maxpreserve)) {
+                cfg = c;
+                found = true;
+            }
+        if (!found) {
+            set_error(kErrUnsupported, "FP32 convolution supports N in {8,16,24,32}; N=%d", N);
+            return kErrUnsupported;
+        }
+    }
+    const int bg = cfg.bg;
+    const int groups = (B + bg - 1) / bg;
+    const float pf_f = (float)p->pf_fwd, pf_i = (float)p->pf_inv;
+    float2 *P = p->c32[0], *R = p->c32[1], *S = p->c32[2];
+    if (!maxpreserve) {
+        SBTE_LAUNCH(dft3_f32(fdev, DftIn::kRealF64, 1, p->tmp32, P, DftOut::kComplexF32, bg,
+                             p->Dfwd32, pf_f, N, B, st), 2);
+        SBTE_CUDA(cudaMemsetAsync(p->qacc, 0, sizeof(double2) * (size_t)groups * bg * p->n3, st));
+        auto *ev = prof_slot(p);
+        if (ev) cudaEventRecord(ev->first, st);
+        SBTE_LAUNCH(conv_f32_batched(p->W.w32, P, P, nullptr, nullptr, p->qacc, N, B, cfg,
+                                     p->d_status, st), 1);
+        if (ev) cudaEventRecord(ev->second, st);
+    } else {
+        double *M = p->r32[0], *g = p->r32[1];
+        SBTE_LAUNCH(maxwellian_split(fdev, M, g, nullptr, B, N, p->d_v, p->mom_mass,
+                                     p->mom_KB, nullptr, st), 1);
+        // P = ghat, R = fhat (= Mhat + ghat), S = Mhat, T = ghat
+        SBTE_LAUNCH(dft3_f32(g, DftIn::kRealF64, 1, p->tmp32, P, DftOut::kComplexF32, bg,
+                             p->Dfwd32, pf_f, N, B, st), 2);
+        SBTE_LAUNCH(dft3_f32(fdev, DftIn::kRealF64, 1, p->tmp32, R, DftOut::kComplexF32, bg,
+                             p->Dfwd32, pf_f, N, B, st), 2);
+        SBTE_LAUNCH(dft3_f32(M, DftIn::kRealF64, 1, p->tmp32, S, DftOut::kComplexF32, bg,
+                             p->Dfwd32, pf_f, N, B, st), 2);
+        SBTE_CUDA(cudaMemsetAsync(p->qacc, 0, sizeof(double2) * (size_t)groups * bg * p->n3, st));
+        auto *ev = prof_slot(p);
+        if (ev) cudaEventRecord(ev->first, st);
+        SBTE_LAUNCH(conv_f32_batched(p->W.w32, P, R, S, P, p->qacc, N, B, cfg, p->d_status,
+                                     st), 1);
+        if (ev) cudaEventRecord(ev->second, st);
+    }
+    SBTE_LAUNCH(dft3_f32(p->qacc, DftIn::kComplexF64, bg, p->tmp32, Qdev, DftOut::kRealF64, 1,
+                         p->Dinv32, pf_i, N, B, st), 2);
+    return kOk;
+}
+
+static int computeQ_dev(spectral_plan_s *p, const double *f, double *Q, int B,
+                        int flags, cudaStream_t st)
+{
+    if (!p || !f || !Q || B < 1) {
+        set_error(kErrArg, "computeQ: bad arguments");
+        return kErrArg;
+    }
+    if (!p->W.w64) {
+        set_error(kErrWeights, "computeQ: the plan has no weights");
+        return kErrWeights;
+    }
+    SBTE_CUDA(cudaSetDevice(p->device));
+    const bool mp = (flags & SPECTRAL_MAXPRESERVE) != 0;
+    if (flags & SPECTRAL_FP32)
+        SBTE_TRY(q_fp32(p, f, Q, B, mp, st));
+    else
+        SBTE_TRY(q_fp64(p, p->W, f, f, Q, B, mp, st));
+    if (flags & SPECTRAL_CONSERVE) SBTE_LAUNCH(conserve_batch(Q, B, p->d_v, p->cons, st), 1);
+    return kOk;
+}
+
+}  // namespace sbte
+
+// ====================================================== Part 2 (C API) ===
+extern "C" {
+
+int spectral_last_error(void) { return sbte::last_error(); }
+const char *spectral_last_error_message(void) { return sbte::last_message(); }
+const char *spectral_version(void) { return "spectralbte_gb300 0.1 (sm_103a)"; }
+long long spectral_kernel_launches(void) { return sbte::g_launches.load(); }
+
+int spectral_plan_create(spectral_plan **plan, int N, double L_v,
+                         const double *v, const double *zeta, int max_batch)
+{
+    if (!plan || !v || !zeta) {
+        set_error(kErrArg, "spectral_plan_create: null argument");
+        return kErrArg;
+    }
+    *plan = nullptr;
+    auto *p = new spectral_plan_s();
+    int rc = plan_init(p, N, L_v, v, zeta);
+    (void)max_batch;  // scratch grows on first use
+    if (rc != kOk) {
+        delete p;
+        return rc;
+    }
+    *plan = p;
+    return kOk;
+}
+
+int spectral_plan_destroy(spectral_plan *plan)
+{
+    delete plan;
+    return kOk;
+}
+
+int spectral_plan_set_weights_rows(spectral_plan *p, double **rows)
+{
+    if (!p || !rows) return set_error(kErrArg, "null argument"), kErrArg;
+    return upload_weights(p->W, p->N, nullptr, rows, false, p->stream);
+}
+
+int spectral_plan_set_weights(spectral_plan *p, const double *W, int on_device)
+{
+    if (!p || !W) return set_error(kErrArg, "null argument"), kErrArg;
+    return upload_weights(p->W, p->N, W, nullptr, on_device != 0, p->stream);
+}
+
+int spectral_plan_generate_weights_iso(spectral_plan *p, double lambda, double d_i,
+                                       double d_j, double m_i, double m_j)
+{
+    if (!p) return set_error(kErrArg, "null plan"), kErrArg;
+    IsoWeightSpec s;
+    s.N = p->N;
+    s.L_v = p->L_v;
+    s.lambda = lambda;
+    s.d_i = d_i;
+    s.d_j = d_j;
+    s.m_i = m_i;
+    s.m_j = m_j;
+    s.zeta = p->zeta;
+    return generate_iso_device(p->W, s, p->stream);
+}
+
+int spectral_plan_get_weights(spectral_plan *p, double *W_host, long long row0,
+                              long long nrows)
+{
+    if (!p || !W_host || !p->W.w64 || row0 < 0 || row0 + nrows > p->n3)
+        return set_error(kErrArg, "get_weights: bad arguments"), kErrArg;
+    SBTE_CUDA(cudaMemcpy(W_host, p->W.w64 + row0 * p->n3, sizeof(double) * nrows * p->n3,
+                         cudaMemcpyDeviceToHost));
+    return kOk;
+}
+
+int spectral_plan_set_conservation(spectral_plan *p, double mass)
+{
+    if (!p) return set_error(kErrArg, "null plan"), kErrArg;
+    int rc = build_conservation(p->cons, p->N, p->v[1] - p->v[0], p->v.data(), &mass, 1);
+    p->cons_ready = (rc == kOk);
+    p->mom_mass = mass;
+    p->mom_KB = (mass == 1.0) ? 1.0 : 1.380658e-23;  // momentRoutines.c:23-28
+    return rc;
+}
+
+int spectral_computeQ_device(spectral_plan *p, const double *f_dev, double *Q_dev,
+                             int B, int flags, void *stream)
+{
+    cudaStream_t st = stream ? (cudaStream_t)stream : (p ? p->stream : nullptr);
+    return computeQ_dev(p, f_dev, Q_dev, B, flags, st);
+}
+
+int spectral_computeQ_host(spectral_plan *p, const double *f_host, double *Q_host,
+                           int B, int flags)
+{
+    if (!p || !f_host || !Q_host || B < 1) return set_error(kErrArg, "bad arguments"), kErrArg;
+    SBTE_CUDA(cudaSetDevice(p->device));
+    if (B > p->caphost) {
+        dfree(p->d_fh);
+        dfree(p->d_Qh);
+        p->caphost = 0;
+        SBTE_TRY(dalloc(&p->d_fh, (size_t)B * p->n3));
+        SBTE_TRY(dalloc(&p->d_Qh, (size_t)B * p->n3));
+        p->caphost = B;
+    }
+    const size_t bytes = sizeof(double) * (size_t)B * p->n3;
+    SBTE_CUDA(cudaMemcpyAsync(p->d_fh, f_host, bytes, cudaMemcpyHostToDevice, p->stream));
+    SBTE_TRY(computeQ_dev(p, p->d_fh, p->d_Qh, B, flags, p->stream));
+    SBTE_CUDA(cudaMemcpyAsync(Q_host, p->d_Qh, bytes, cudaMemcpyDeviceToHost, p->stream));
+    SBTE_CUDA(cudaStreamSynchronize(p->stream));
+    return kOk;
+}
+
+int spectral_conserve_device(spectral_plan *p, double *Q_dev, int B, void *stream)
+{
+    if (!p || !Q_dev || B < 1) return set_error(kErrArg, "bad arguments"), kErrArg;
+    cudaStream_t st = stream ? (cudaStream_t)stream : p->stream;
+    SBTE_LAUNCH(conserve_batch(Q_dev, B, p->d_v, p->cons, st), 1);
+    return kOk;
+}
+
+int spectral_step_device(spectral_plan *p, double *f, int B, double dt, double Kn,
+                         int order, int flags, void *stream)
+{
+    if (!p || !f || B < 1 || (order != 1 && order != 2))
+        return set_error(kErrArg, "step: bad arguments"), kErrArg;
+    cudaStream_t st = stream ? (cudaStream_t)stream : p->stream;
+    SBTE_TRY(ensure_step(p, B));
+    const long long n = (long long)B * p->n3;
+    const int fl = flags | SPECTRAL_CONSERVE;
+    SBTE_TRY(computeQ_dev(p, f, p->sQ, B, fl, st));
+    if (order == 1) {
+        // f += dt*Q/Kn  (boltz.c:208-211)
+        SBTE_LAUNCH(axpy_update(f, nullptr, p->sQ, 1.0, 0.0, dt / Kn, n, st), 1);
+        return kOk;
+    }
+    // f1 = f + dt*Q/Kn; Q = Q(f1); f = 0.5 (f + f1) + 0.5 dt Q / Kn
+    // (boltz.c:216-240)
+    SBTE_CUDA(cudaMemcpyAsync(p->sf1, f, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+    SBTE_LAUNCH(axpy_update(p->sf1, nullptr, p->sQ, 1.0, 0.0, dt / Kn, n, st), 1);
+    SBTE_TRY(computeQ_dev(p, p->sf1, p->sQ, B, fl, st));
+    SBTE_LAUNCH(axpy_update(f, p->sf1, p->sQ, 0.5, 0.5, 0.5 * dt / Kn, n, st), 1);
+    return kOk;
+}
+
+int spectral_plan_set_tuning(spectral_plan *p, int bg, int stages, int flush)
+{
+    if (!p) return set_error(kErrArg, "null plan"), kErrArg;
+    ConvF32Config c{bg, stages, flush};
+    if (!conv_f32_supported(p->N, c, false))
+        return set_error(kErrUnsupported, "unsupported FP32 tuning bg=%d stages=%d", bg, stages),
+               kErrUnsupported;
+    p->tune = c;
+    return kOk;
+}
+
+int spectral_plan_autotune(spectral_plan *p, int B, int flags, int *chosen)
+{
+    if (!p || B < 1) return set_error(kErrArg, "bad arguments"), kErrArg;
+    if (!p->W.w64) return set_error(kErrWeights, "autotune: no weights"), kErrWeights;
+    SBTE_CUDA(cudaSetDevice(p->device));
+    SBTE_TRY(ensure32(p, B));
+    SBTE_TRY(ensure_w32(p->W, p->stream));
+    const bool two = (flags & SPECTRAL_MAXPRESERVE) != 0;
+    const ConvF32Config cands[] = {{32, 2, 16}, {32, 3, 16}, {64, 2, 16},
+                                   {64, 3, 16}, {128, 2, 16}};
+    cudaEvent_t e0, e1;
+    SBTE_CUDA(cudaEventCreate(&e0));
+    SBTE_CUDA(cudaEventCreate(&e1));
+    float best = 1e30f;
+    ConvF32Config bestc = p->tune;
+    for (const auto &c : cands) {
+        if (!conv_f32_supported(p->N, c, two)) continue;
+        float2 *P = p->c32[0], *R = p->c32[1], *S = p->c32[2];
+        float ms_total = 0.f;
+        for (int rep = 0; rep < 3; rep++) {
+            cudaEventRecord(e0, p->stream);
+            cudaError_t e = conv_f32_batched(p->W.w32, P, R, two ? S : nullptr,
+                                             two ? P : nullptr, p->qacc, p->N, B, c,
+                                             p->d_status, p->stream);
+            cudaEventRecord(e1, p->stream);
+            if (e != cudaSuccess) {
+                cudaEventDestroy(e0);
+                cudaEventDestroy(e1);
+                set_error(kErrCuda, "autotune launch: %s", cudaGetErrorString(e));
+                return kErrCuda;
+            }
+            count(1);
+            SBTE_CUDA(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (rep > 0) ms_total += ms;  // first run is warm-up
+        }
+        if (ms_total < best) {
+            best = ms_total;
+            bestc = c;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    p->tune = bestc;
+    if (chosen) {
+        chosen[0] = bestc.bg;
+        chosen[1] = bestc.stages;
+        chosen[2] = bestc.flush;
+    }
+    return kOk;
+}
+
+int spectral_plan_status(spectral_plan *p, unsigned int *status)
+{
+    if (!p || !status) return set_error(kErrArg, "bad arguments"), kErrArg;
+    SBTE_CUDA(cudaStreamSynchronize(p->stream));
+    SBTE_CUDA(cudaMemcpy(status, p->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    SBTE_CUDA(cudaMemset(p->d_status, 0, sizeof(unsigned)));
+    return kOk;
+}
+
+int spectral_plan_set_profiling(spectral_plan *p, int on)
+{
+    if (!p) return set_error(kErrArg, "null plan"), kErrArg;
+    SBTE_CUDA(cudaDeviceSynchronize());
+    p->profiling = (on != 0);
+    p->prof_used = 0;
+    return kOk;
+}
+
+int spectral_plan_conv_time(spectral_plan *p, double *total_ms, int *launches)
+{
+    if (!p || !total_ms || !launches) return set_error(kErrArg, "bad arguments"), kErrArg;
+    double tot = 0.0;
+    for (size_t i = 0; i < p->prof_used; i++) {
+        SBTE_CUDA(cudaEventSynchronize(p->prof_events[i].second));
+        float ms = 0.f;
+        SBTE_CUDA(cudaEventElapsedTime(&ms, p->prof_events[i].first, p->prof_events[i].second));
+        tot += ms;
+    }
+    *total_ms = tot;
+    *launches = (int)p->prof_used;
+    p->prof_used = 0;
+    return kOk;
+}
+
+int spectral_plan_sync(spectral_plan *p)
+{
+    if (!p) return set_error(kErrArg, "null plan"), kErrArg;
+    SBTE_CUDA(cudaStreamSynchronize(p->stream));
+    return kOk;
+}
+
+}  // extern "C"
+
+// ================================================ Part 1 (reference ABI) ===
+namespace sbte {
+
+// Module state mirroring collisions.c:11-24 and conserve.c:7-15.
+struct LegacyColl {
+    spectral_plan_s *plan = nullptr;
+    int N = 0;
+    double *d_f = nullptr, *d_g = nullptr, *d_Q = nullptr;
+    double2 *d_c = nullptr;
+};
+struct LegacyCons {
+    bool ready = false;
+    int N = 0, Ns = 0;
+    double dv = 0;
+    std::vector<double> v, mass;
+    ConsParams cp{};
+    double *d_v = nullptr;
+    double *d_Q = nullptr;
+    double **d_ptrs = nullptr;
+    size_t capQ = 0;
+};
+struct LegacyWeights {
+    std::map<double **, WeightsDev> dev;
+    IsoWeightSpec last;  // module state of weights.c:11-24
+    double prefactor = 0;
+};
+
+static LegacyColl g_coll;
+static LegacyCons g_cons;
+static LegacyWeights g_w;
+static std::mutex g_mu;
+
+static void report(const char *where)
+{
+    fprintf(stderr, "spectralbte_gb300: %s failed: %s\n", where, last_message());
+}
+
+static WeightsDev *weights_for(double **cw, int N, cudaStream_t st)
+{
+    auto it = g_w.dev.find(cw);
+    if (it != g_w.dev.end() && it->second.N == N && it->second.w64) return &it->second;
+    WeightsDev &wd = g_w.dev[cw];
+    if (upload_weights(wd, N, nullptr, cw, false, st) != kOk) return nullptr;
+    return &wd;
+}
+
+static int legacy_q(double *f, double *g, double *Q, double **cw, bool mp)
+{
+    if (!g_coll.plan) {
+        set_error(kErrNotInit, "initialize_coll has not been called");
+        return kErrNotInit;
+    }
+    spectral_plan_s *p = g_coll.plan;
+    SBTE_CUDA(cudaSetDevice(p->device));
+    cudaStream_t st = p->stream;
+    WeightsDev *W = weights_for(cw, p->N, st);
+    if (!W) return last_error();
+    const size_t bytes = sizeof(double) * p->n3;
+    SBTE_CUDA(cudaMemcpyAsync(g_coll.d_f, f, bytes, cudaMemcpyHostToDevice, st));
+    const double *gd = g_coll.d_f;
+    if (g != f) {
+        SBTE_CUDA(cudaMemcpyAsync(g_coll.d_g, g, bytes, cudaMemcpyHostToDevice, st));
+        gd = g_coll.d_g;
+    }
+    if (g_cons.ready && !g_cons.mass.empty()) {
+        p->mom_mass = g_cons.mass[0];
+        p->mom_KB = (g_cons.mass[0] == 1.0) ? 1.0 : 1.380658e-23;  // momentRoutines.c:23-28
+    }
+    SBTE_TRY(q_fp64(p, *W, g_coll.d_f, gd, g_coll.d_Q, 1, mp, st));
+    SBTE_CUDA(cudaMemcpyAsync(Q, g_coll.d_Q, bytes, cudaMemcpyDeviceToHost, st));
+    SBTE_CUDA(cudaStreamSynchronize(st));
+    return kOk;
+}
+
+static void weights_file_name(char *buf, size_t n, int N, double L_v, double lam,
+                              int isoFlag, const species &si, const species &sj)
+{
+    // weights.c:66-75
+    if (!isoFlag) {
+        if (strcmp(si.name, "default") == 0)
+            snprintf(buf, n, "Weights/N%d_isotropic_L_v%g_lambda%g.wts", N, L_v, lam);
+        else
+            snprintf(buf, n, "Weights/N%d_isotropic_L_v%g_HS_%s_%zu_%s_%zu.wts", N, L_v,
+                     si.name, si.id, sj.name, sj.id);
+    } else {
+        snprintf(buf, n, "Weights/N%d_AnIso_L_v%g_lambda%g_Landau.wts", N, L_v, lam);
+    }
+}
+
+// GPU quadrature into both the device registry entry and the host rows.
+static int generate_into_rows(double **cw)
+{
+    const IsoWeightSpec &s = g_w.last;
+    const long long n3 = (long long)s.N * s.N * s.N;
+    SBTE_TRY(ensure_device());
+    cudaStream_t st = g_coll.plan ? g_coll.plan->stream : nullptr;
+    WeightsDev &wd = g_w.dev[cw];
+    SBTE_TRY(generate_iso_device(wd, s, st));
+    const long long chunk_rows = std::max<long long>(1, (64ll << 20) / (8 * n3));
+    double *stage = nullptr;
+    SBTE_CUDA(cudaMallocHost((void **)&stage, sizeof(double) * chunk_rows * n3));
+    for (long long r0 = 0; r0 < n3; r0 += chunk_rows) {
+        const long long nr = std::min(chunk_rows, n3 - r0);
+        cudaError_t e = cudaMemcpy(stage, wd.w64 + r0 * n3, sizeof(double) * nr * n3,
+                                   cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) {
+            cudaFreeHost(stage);
+            set_error(kErrCuda, "weights D2H: %s", cudaGetErrorString(e));
+            return kErrCuda;
+        }
+        for (long long r = 0; r < nr; r++) memcpy(cw[r0 + r], stage + r * n3, sizeof(double) * n3);
+    }
+    cudaFreeHost(stage);
+    return kOk;
+}
+
+static double host_sinc(double x) { return (x != 0.0) ? sin(x) / x : 1.0; }
+
+}  // namespace sbte
+
+extern "C" {
+
+void initialize_coll(int nodes, double length, double *vel, double *zeta)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (g_coll.plan) {
+        delete g_coll.plan;
+        g_coll.plan = nullptr;
+    }
+    auto *p = new spectral_plan_s();
+    int rc = plan_init(p, nodes, length, vel, zeta);
+    if (rc == kOk) rc = ensure64(p, 1);
+    if (rc == kOk) {
+        g_coll.plan = p;
+        g_coll.N = nodes;
+        dfree(g_coll.d_f); dfree(g_coll.d_g); dfree(g_coll.d_Q); dfree(g_coll.d_c);
+        const size_t n3 = (size_t)nodes * nodes * nodes;
+        if ((rc = dalloc(&g_coll.d_f, n3)) == kOk && (rc = dalloc(&g_coll.d_g, n3)) == kOk &&
+            (rc = dalloc(&g_coll.d_Q, n3)) == kOk)
+            rc = dalloc(&g_coll.d_c, 2 * n3);
+    } else {
+        delete p;
+    }
+    if (rc != kOk) report("initialize_coll");
+}
+
+void dealloc_coll(void)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    delete g_coll.plan;
+    g_coll.plan = nullptr;
+    dfree(g_coll.d_f); dfree(g_coll.d_g); dfree(g_coll.d_Q); dfree(g_coll.d_c);
+}
+
+void ComputeQ(double *f, double *g, double *Q, double **conv_weights)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (legacy_q(f, g, Q, conv_weights, false) != kOk) report("ComputeQ");
+}
+
+void ComputeQ_maxPreserve(double *f, double *g, double *Q, double **conv_weights)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (legacy_q(f, g, Q, conv_weights, true) != kOk) report("ComputeQ_maxPreserve");
+}
+
+void fft3D(fftw_complex *in, fftw_complex *out, int invert)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    spectral_plan_s *p = g_coll.plan;
+    if (!p) {
+        set_error(kErrNotInit, "initialize_coll has not been called");
+        report("fft3D");
+        return;
+    }
+    const size_t bytes = sizeof(double2) * p->n3;
+    cudaStream_t st = p->stream;
+    double2 *dout = (double2 *)g_coll.d_c;
+    int rc = kOk;
+    if (cudaMemcpyAsync(dout, in, bytes, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        dft3_f64(dout, DftIn::kComplexF64, 1, p->tmp64, p->c64[0], DftOut::kComplexF64, 1,
+                 invert ? p->Dinv64 : p->Dfwd64, invert ? p->pf_inv : p->pf_fwd, p->N, 1,
+                 st) != cudaSuccess ||
+        cudaMemcpyAsync(out, p->c64[0], bytes, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess) {
+        set_error(kErrCuda, "fft3D: %s", cudaGetErrorString(cudaGetLastError()));
+        rc = kErrCuda;
+    } else {
+        count(2);
+    }
+    if (rc != kOk) report("fft3D");
+}
+
+static void cons_init(int nodes, double h_v, double *vel, const double *mass, int Ns)
+{
+    g_cons.ready = false;
+    if (Ns < 1 || Ns > 4) {
+        set_error(kErrUnsupported, "conservation supports 1..4 species, got %d", Ns);
+        report("initialize_conservation");
+        return;
+    }
+    g_cons.N = nodes;
+    g_cons.Ns = Ns;
+    g_cons.dv = h_v;
+    g_cons.v.assign(vel, vel + nodes);
+    g_cons.mass.assign(mass, mass + Ns);
+    if (build_conservation(g_cons.cp, nodes, h_v, vel, mass, Ns) != kOk) {
+        report("initialize_conservation");
+        return;
+    }
+    if (ensure_device() != kOk) {
+        report("initialize_conservation");
+        return;
+    }
+    dfree(g_cons.d_v);
+    if (dalloc(&g_cons.d_v, nodes) != kOk ||
+        cudaMemcpy(g_cons.d_v, vel, sizeof(double) * nodes, cudaMemcpyHostToDevice) != cudaSuccess) {
+        report("initialize_conservation");
+        return;
+    }
+    g_cons.ready = true;
+}
+
+void initialize_conservation(int nodes, double h_v, double *vel, species *mix, int num_spec)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    std::vector<double> m(num_spec > 0 ? num_spec : 1, 1.0);
+    for (int i = 0; i < num_spec; i++) m[i] = mix[i].mass;
+    cons_init(nodes, h_v, vel, m.data(), num_spec);
+}
+
+void initialize_conservation_fast(int nodes, double h_v, double *vel)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    const double m = 1.0;  // conserve.c:51-54
+    cons_init(nodes, h_v, vel, &m, 1);
+}
+
+void dealloc_conservation(void)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_cons.ready = false;
+    dfree(g_cons.d_v);
+    dfree(g_cons.d_Q);
+    dfree(g_cons.d_ptrs);
+    g_cons.capQ = 0;
+}
+
+void factorMatrixIntoLU(int nElem, double det)
+{
+    (void)det;
+    std::lock_guard<std::mutex> lk(g_mu);
+    // The factors are built by initialize_conservation; rebuilding them
+    // from the stored grid keeps repeated calls idempotent.
+    if (g_cons.N > 0 && nElem == g_cons.Ns + 4)
+        build_conservation(g_cons.cp, g_cons.N, g_cons.dv, g_cons.v.data(),
+                           g_cons.mass.data(), g_cons.Ns);
+}
+
+void createCCtAndPivot(void)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (g_cons.N > 0)
+        build_conservation(g_cons.cp, g_cons.N, g_cons.dv, g_cons.v.data(),
+                           g_cons.mass.data(), g_cons.Ns);
+}
+
+void solveWithCCt(int nElem, double *b)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!g_cons.ready || nElem != g_cons.Ns + 4) {
+        set_error(kErrNotInit, "solveWithCCt: conservation not initialised for %d", nElem);
+        report("solveWithCCt");
+        return;
+    }
+    solve_cct_host(g_cons.cp, b, nElem);
+}
+
+void conserveAllMoments(double **Q)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!g_cons.ready) {
+        set_error(kErrNotInit, "initialize_conservation has not been called");
+        report("conserveAllMoments");
+        return;
+    }
+    const int Ns = g_cons.Ns;
+    const size_t n3 = (size_t)g_cons.N * g_cons.N * g_cons.N;
+    const size_t need = (size_t)Ns * Ns * n3;
+    cudaStream_t st = g_coll.plan ? g_coll.plan->stream : nullptr;
+    int rc = kOk;
+    if (need > g_cons.capQ) {
+        dfree(g_cons.d_Q);
+        dfree(g_cons.d_ptrs);
+        g_cons.capQ = 0;
+        if ((rc = dalloc(&g_cons.d_Q, need)) == kOk &&
+            (rc = dalloc(&g_cons.d_ptrs, (size_t)Ns * Ns)) == kOk)
+            g_cons.capQ = need;
+    }
+    std::vector<double *> ptrs(Ns * Ns);
+    for (int a = 0; a < Ns * Ns && rc == kOk; a++) {
+        ptrs[a] = g_cons.d_Q + a * n3;
+        if (cudaMemcpyAsync(ptrs[a], Q[a], sizeof(double) * n3, cudaMemcpyHostToDevice, st) !=
+            cudaSuccess)
+            rc = kErrCuda;
+    }
+    if (rc == kOk) {
+        cudaError_t e;
+        if (Ns == 1) {
+            e = conserve_batch(g_cons.d_Q, 1, g_cons.d_v, g_cons.cp, st);
+        } else {
+            e = cudaMemcpyAsync(g_cons.d_ptrs, ptrs.data(), sizeof(double *) * Ns * Ns,
+                                cudaMemcpyHostToDevice, st);
+            if (e == cudaSuccess) e = conserve_species(g_cons.d_ptrs, g_cons.d_v, g_cons.cp, st);
+        }
+        if (e != cudaSuccess) rc = kErrCuda;
+        else count(1);
+    }
+    for (int a = 0; a < Ns * Ns && rc == kOk; a++)
+        if (cudaMemcpyAsync(Q[a], ptrs[a], sizeof(double) * n3, cudaMemcpyDeviceToHost, st) !=
+            cudaSuccess)
+            rc = kErrCuda;
+    if (rc == kOk && cudaStreamSynchronize(st) != cudaSuccess) rc = kErrCuda;
+    if (rc != kOk) {
+        if (last_error() == kOk || rc == kErrCuda)
+            set_error(rc, "conserveAllMoments: %s", cudaGetErrorString(cudaGetLastError()));
+        report("conserveAllMoments");
+    }
+}
+
+void alloc_weights(int N, double ****conv_weights, int total_species)
+{
+    // weights.c:26-31
+    *conv_weights = (double ***)malloc(total_species * sizeof(double **));
+    for (int i = 0; i < total_species; i++)
+        (*conv_weights)[i] = (double **)malloc((size_t)N * N * N * sizeof(double *));
+}
+
+void initialize_weights(int nodes, double *eta, double Lv, double lam, int weightFlag,
+                        int isoFlag, double **conv_weights, species species_i,
+                        species species_j)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    const long long n3 = (long long)nodes * nodes * nodes;
+    // module state, weights.c:39-49
+    g_w.last.N = nodes;
+    g_w.last.L_v = Lv;
+    g_w.last.lambda = lam;
+    g_w.last.d_i = species_i.d_ref;
+    g_w.last.d_j = species_j.d_ref;
+    g_w.last.m_i = species_i.mass;
+    g_w.last.m_j = species_j.mass;
+    g_w.last.zeta.assign(eta, eta + nodes);
+    const double deta = eta[1] - eta[0];
+    g_w.prefactor = 16.0 * M_PI * M_PI * deta * deta * deta / pow(2.0 * M_PI, 1.5) / (4.0 * M_PI);
+    for (long long i = 0; i < n3; i++)  // weights.c:61-63
+        conv_weights[i] = (double *)malloc(sizeof(double) * n3);
+
+    char name[256];
+    weights_file_name(name, sizeof(name), nodes, Lv, lam, isoFlag, species_i, species_j);
+    FILE *fid = nullptr;
+    bool loaded = false;
+    if (weightFlag == 0 && (fid = fopen(name, "r"))) {
+        loaded = true;
+        for (long long i = 0; i < n3; i++) {
+            if ((long long)fread(conv_weights[i], sizeof(double), n3, fid) != n3) {
+                set_error(kErrWeights, "short read of weight file %s", name);
+                report("initialize_weights");
+                fclose(fid);
+                return;
+            }
+        }
+        fclose(fid);
+    }
+    if (!loaded) {
+        if (isoFlag) {
+            set_error(kErrWeights,
+                      "anisotropic weights %s not found; generate them first", name);
+            report("initialize_weights");
+            return;
+        }
+        if (generate_into_rows(conv_weights) != kOk) {
+            report("initialize_weights");
+            return;
+        }
+        fid = fopen(name, "w");
+        if (!fid) {
+            set_error(kErrWeights, "cannot open %s for writing", name);
+            report("initialize_weights");
+            return;
+        }
+        for (long long i = 0; i < n3; i++) fwrite(conv_weights[i], sizeof(double), n3, fid);
+        if (fflush(fid) != 0) {
+            set_error(kErrWeights, "storing the weights in %s failed", name);
+            report("initialize_weights");
+        }
+        fclose(fid);
+        return;  // the device copy was kept by generate_into_rows
+    }
+    cudaStream_t st = g_coll.plan ? g_coll.plan->stream : nullptr;
+    if (ensure_device() != kOk ||
+        upload_weights(g_w.dev[conv_weights], nodes, nullptr, conv_weights, false, st) != kOk)
+        report("initialize_weights");
+}
+
+void dealloc_weights(int N, double **conv_weights)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto it = g_w.dev.find(conv_weights);
+    if (it != g_w.dev.end()) {
+        it->second.release();
+        g_w.dev.erase(it);
+    }
+    for (long long i = 0; i < (long long)N * N * N; i++) free(conv_weights[i]);
+    free(conv_weights);
+}
+
+void generate_conv_weights_iso(double **conv_weights)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (g_w.last.N == 0) {
+        set_error(kErrNotInit, "initialize_weights has not set the weight grid");
+        report("generate_conv_weights_iso");
+        return;
+    }
+    if (generate_into_rows(conv_weights) != kOk) report("generate_conv_weights_iso");
+}
+
+double ghat(double r, void *args)
+{
+    // weights.c:156-160
+    const double *a = (const double *)args;
+    return pow(r, g_w.last.lambda + 2) * (host_sinc(r * a[0]) * host_sinc(r * a[2]) -
+                                          host_sinc(r * a[1]));
+}
+
+double gHat3(double ki1, double ki2, double ki3, double zeta1, double zeta2, double zeta3)
+{
+    // weights.c:181-262 with composite 16-point Gauss-Legendre in place of
+    // adaptive QAG (converged to round-off)
+    const IsoWeightSpec &s = g_w.last;
+    const double mu = s.m_j / (s.m_i + s.m_j);
+    double a[3];
+    a[0] = mu * sqrt(zeta1 * zeta1 + zeta2 * zeta2 + zeta3 * zeta3);
+    a[1] = sqrt(ki1 * ki1 + ki2 * ki2 + ki3 * ki3);
+    a[2] = sqrt((ki1 - mu * zeta1) * (ki1 - mu * zeta1) + (ki2 - mu * zeta2) * (ki2 - mu * zeta2) +
+                (ki3 - mu * zeta3) * (ki3 - mu * zeta3));
+    static std::vector<double> gx, gw;
+    if (gx.empty()) gl_nodes(16, gx, gw);
+    const double omega = std::max(a[0] + a[2], a[1]);
+    int K = (int)ceil(omega * s.L_v / 6.0);
+    if (K < 4) K = 4;
+    const double h = s.L_v / K;
+    double total = 0.0;
+    for (int p = 0; p < K; p++) {
+        double part = 0.0;
+        for (int q = 0; q < 16; q++) part += gw[q] * ghat((p + 0.5) * h + 0.5 * h * gx[q], a);
+        total += 0.5 * h * part;
+    }
+    return g_w.prefactor * total;
+}
+
+}  // extern "C"

@@ -1,0 +1,263 @@
+// conserve.cu -- FP64 device kernels for the conservation projection
+// (conserve.c:207-264), the moments and Maxwellian split of
+// find_maxwellians (collisions.c:91-106, momentRoutines.c:58-183), and the
+// Euler/RK2 updates of the time loop (boltz.c:206-241).
+#include "common.cuh"
+#include "kernels.h"
+
+namespace sbte {
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ double wt(int i, int N)
+{
+    // trapezoid weights, collisions.c:48-54
+    return (i == 0 || i == N - 1) ? 0.5 : 1.0;
+}
+
+// Block-wide sum of K doubles; result valid in every thread.
+template <int K>
+__device__ void block_sum(double (&x)[K], double *red /* >= 32*K */)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x[k] += __shfl_xor_sync(0xffffffffu, x[k], o);
+    }
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < K; k++) red[warp * K + k] = x[k];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        double s = 0.0;
+        for (int w = 0; w < nw; w++) s += red[w * K + k];
+        x[k] = s;
+    }
+    __syncthreads();
+}
+
+// solveWithCCt (conserve.c:173-202), one thread.
+__device__ void solve_cct(const ConsParams &cp, double *b)
+{
+    const int n = cp.Ns + 4;
+    for (int k = 0; k < n - 1; k++) {
+        const int i = cp.pivot[k];
+        if (i != k) {
+            const double t = b[i];
+            b[i] = b[k];
+            b[k] = t;
+        }
+        for (int r = k + 1; r < n; r++) b[r] -= cp.CCt[r][k] * b[k];
+    }
+    b[n - 1] = b[n - 1] / cp.CCt[n - 1][n - 1];
+    for (int i = n - 2; i >= 0; i--) {
+        double sum = 0.0;
+        for (int j = i + 1; j < n; j++) sum += cp.CCt[i][j] * b[j];
+        b[i] = 1.0 / cp.CCt[i][i] * (b[i] - sum);
+    }
+}
+
+// One species, one CTA per instance.
+__global__ void __launch_bounds__(kThreads)
+conserve_batch_kernel(double *__restrict__ Q, const double *__restrict__ v,
+                      ConsParams cp)
+{
+    __shared__ double red[32 * 5];
+    __shared__ double lam[8];
+    const int N = cp.N;
+    const long long n3 = (long long)N * N * N;
+    double *Qb = Q + (long long)blockIdx.x * n3;
+    const double dv = cp.dv, mass = cp.mass[0];
+    double m[5] = {0, 0, 0, 0, 0};
+    for (long long x = threadIdx.x; x < n3; x += blockDim.x) {
+        const int i = (int)(x / (N * N)), j = (int)((x / N) % N), k = (int)(x % N);
+        const double prefact = wt(i, N) * wt(j, N) * wt(k, N) * dv * dv * dv * mass;
+        const double q = Qb[x];
+        m[0] += q * prefact;
+        m[1] += q * (prefact * v[i]);
+        m[2] += q * (prefact * v[j]);
+        m[3] += q * (prefact * v[k]);
+        m[4] += q * (prefact * 0.5 * (v[i] * v[i] + v[j] * v[j] + v[k] * v[k]));
+    }
+    block_sum<5>(m, red);
+    if (threadIdx.x == 0) {
+        double b[8];
+        for (int t = 0; t < 5; t++) b[t] = m[t];
+        solve_cct(cp, b);
+        for (int t = 0; t < 5; t++) lam[t] = b[t];
+    }
+    __syncthreads();
+    const double l0 = lam[0], l1 = lam[1], l2 = lam[2], l3 = lam[3], l4 = lam[4];
+    for (long long x = threadIdx.x; x < n3; x += blockDim.x) {
+        const int i = (int)(x / (N * N)), j = (int)((x / N) % N), k = (int)(x % N);
+        const double prefact = wt(i, N) * wt(j, N) * wt(k, N) * dv * dv * dv * mass / 1;
+        const double t0 = prefact, t1 = prefact * v[i], t2 = prefact * v[j],
+                     t3 = prefact * v[k],
+                     t4 = prefact * 0.5 * (v[i] * v[i] + v[j] * v[j] + v[k] * v[k]);
+        Qb[x] -= (t0 * l0 + t1 * l1 + t2 * l2 + t3 * l3 + t4 * l4);
+    }
+}
+
+// Ns species (Ns <= 4), a single instance; Qp[n*Ns+m] are N^3 arrays.
+__global__ void __launch_bounds__(kThreads)
+conserve_species_kernel(double **__restrict__ Qp, const double *__restrict__ v,
+                        ConsParams cp)
+{
+    __shared__ double red[32 * 8];
+    __shared__ double lam[8];
+    const int N = cp.N, Ns = cp.Ns;
+    const long long n3 = (long long)N * N * N;
+    const double dv = cp.dv;
+    double m[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (long long x = threadIdx.x; x < n3; x += blockDim.x) {
+        const int i = (int)(x / (N * N)), j = (int)((x / N) % N), k = (int)(x % N);
+        for (int s = 0; s < Ns; s++) {
+            const double prefact = wt(i, N) * wt(j, N) * wt(k, N) * dv * dv * dv * cp.mass[s];
+            const double tm = prefact, tx = prefact * v[i], ty = prefact * v[j],
+                         tz = prefact * v[k],
+                         te = prefact * 0.5 * (v[i] * v[i] + v[j] * v[j] + v[k] * v[k]);
+            for (int n = 0; n < Ns; n++) {
+                const double q = Qp[n * Ns + s][x];
+                m[s] += q * tm;
+                m[Ns] += q * tx;
+                m[Ns + 1] += q * ty;
+                m[Ns + 2] += q * tz;
+                m[Ns + 3] += q * te;
+            }
+        }
+    }
+    block_sum<8>(m, red);
+    if (threadIdx.x == 0) {
+        double b[8];
+        for (int t = 0; t < 8; t++) b[t] = m[t];
+        solve_cct(cp, b);
+        for (int t = 0; t < 8; t++) lam[t] = b[t];
+    }
+    __syncthreads();
+    for (long long x = threadIdx.x; x < n3; x += blockDim.x) {
+        const int i = (int)(x / (N * N)), j = (int)((x / N) % N), k = (int)(x % N);
+        for (int s = 0; s < Ns; s++) {
+            const double prefact = wt(i, N) * wt(j, N) * wt(k, N) * dv * dv * dv * cp.mass[s] / Ns;
+            const double tm = prefact, tx = prefact * v[i], ty = prefact * v[j],
+                         tz = prefact * v[k],
+                         te = prefact * 0.5 * (v[i] * v[i] + v[j] * v[j] + v[k] * v[k]);
+            const double d = tm * lam[s] + tx * lam[Ns] + ty * lam[Ns + 1] +
+                             tz * lam[Ns + 2] + te * lam[Ns + 3];
+            for (int n = 0; n < Ns; n++) Qp[n * Ns + s][x] -= d;
+        }
+    }
+}
+
+// Moments (rho, u, T) of momentRoutines.c and the Maxwellian split of
+// find_maxwellians; one CTA per instance.
+__global__ void __launch_bounds__(kThreads)
+maxwellian_kernel(const double *__restrict__ f, double *__restrict__ M,
+                  double *__restrict__ g, const double *__restrict__ Mref,
+                  int N, const double *__restrict__ v, double mass, double KB,
+                  double *__restrict__ mom)
+{
+    __shared__ double red[32 * 4];
+    const long long n3 = (long long)N * N * N;
+    const long long off = (long long)blockIdx.x * n3;
+    const double dv = v[1] - v[0];
+    const double dv3 = dv * dv * dv;
+    // density and first moments (getDensity, getBulkVelocity)
+    double s[4] = {0, 0, 0, 0};
+    for (long long x = threadIdx.x; x < n3; x += blockDim.x) {
+        const int i = (int)(x / (N * N)), j = (int)((x / N) % N), k = (int)(x % N);
+        const double w = dv3 * wt(i, N) * wt(j, N) * wt(k, N);
+        const double fx = f[off + x];
+        s[0] += w * fx;
+        s[1] += v[i] * w * fx;
+        s[2] += v[j] * w * fx;
+        s[3] += v[k] * w * fx;
+    }
+    block_sum<4>(s, red);
+    const double rho = mass * s[0];
+    const double u0 = mass * (s[1] / rho), u1 = mass * (s[2] / rho),
+                 u2 = mass * (s[3] / rho);
+    // temperature (getTemperature)
+    double tt[1] = {0};
+    for (long long x = threadIdx.x; x < n3; x += blockDim.x) {
+        const int i = (int)(x / (N * N)), j = (int)((x / N) % N), k = (int)(x % N);
+        const double t = (v[i] - u0) * (v[i] - u0) + (v[j] - u1) * (v[j] - u1) +
+                         (v[k] - u2) * (v[k] - u2);
+        tt[0] += t * dv3 * wt(i, N) * wt(j, N) * wt(k, N) * f[off + x];
+    }
+    block_sum<1>(tt, red);
+    const double T = (mass * mass / KB) * (tt[0] / (3.0 * rho));
+    const double pre = rho * pow(0.5 / (M_PI * T), 1.5);
+    for (long long x = threadIdx.x; x < n3; x += blockDim.x) {
+        const int i = (int)(x / (N * N)), j = (int)((x / N) % N), k = (int)(x % N);
+        const double Mx = pre * exp(-(0.5 / T) * ((v[i] - u0) * (v[i] - u0) +
+                                                 (v[j] - u1) * (v[j] - u1) +
+                                                 (v[k] - u2) * (v[k] - u2)));
+        M[off + x] = Mx;
+        g[off + x] = f[off + x] - (Mref ? Mref[off + x] : Mx);
+    }
+    if (mom && threadIdx.x == 0) {
+        mom[5 * blockIdx.x + 0] = rho;
+        mom[5 * blockIdx.x + 1] = u0;
+        mom[5 * blockIdx.x + 2] = u1;
+        mom[5 * blockIdx.x + 3] = u2;
+        mom[5 * blockIdx.x + 4] = T;
+    }
+}
+
+__global__ void axpy_kernel(double *__restrict__ y, const double *__restrict__ x,
+                            const double *__restrict__ q, double a_y, double a_x,
+                            double a_q, long long n)
+{
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+         t += (long long)gridDim.x * blockDim.x) {
+        double r = a_y * y[t];
+        if (x) r += a_x * x[t];
+        if (q) r += a_q * q[t];
+        y[t] = r;
+    }
+}
+
+}  // namespace
+
+cudaError_t conserve_batch(double *Q, int B, const double *v,
+                           const ConsParams &cp, cudaStream_t st)
+{
+    if (B < 1) return cudaSuccess;
+    conserve_batch_kernel<<<B, kThreads, 0, st>>>(Q, v, cp);
+    return cudaGetLastError();
+}
+
+cudaError_t conserve_species(double **Qptrs_dev, const double *v,
+                             const ConsParams &cp, cudaStream_t st)
+{
+    conserve_species_kernel<<<1, kThreads, 0, st>>>(Qptrs_dev, v, cp);
+    return cudaGetLastError();
+}
+
+cudaError_t maxwellian_split(const double *f, double *M, double *g,
+                             const double *Mref, int B, int N, const double *v,
+                             double mass, double KB, double *moments_out,
+                             cudaStream_t st)
+{
+    if (B < 1) return cudaSuccess;
+    maxwellian_kernel<<<B, kThreads, 0, st>>>(f, M, g, Mref, N, v, mass, KB,
+                                              moments_out);
+    return cudaGetLastError();
+}
+
+cudaError_t axpy_update(double *y, const double *x, const double *q, double a_y,
+                        double a_x, double a_q, long long n, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    long long blocks = (n + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    axpy_kernel<<<(unsigned)blocks, 256, 0, st>>>(y, x, q, a_y, a_x, a_q, n);
+    return cudaGetLastError();
+}
+
+}  // namespace sbte

@@ -1,0 +1,121 @@
+// kernels.h -- launchers shared between the CUDA translation units of the
+// library.  All launchers are asynchronous on the given stream and return a
+// cudaError_t from the launch (not from execution).
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace sbte {
+
+// ---------------------------------------------------------------- DFT ---
+// The phase-shifted 3D transform of the reference's fft3D
+// (collisions.c:232-283), as three dense N x N axis matrices:
+//   out = prefactor * (D (x) D (x) D) in,
+//   D[k][n] = exp(i s L_end varr[k]) exp(i dir 2 pi (n k mod N)/N) wt[n]
+//             exp(i s n L_start delta).
+// Dt holds D transposed (Dt[n*N + k] = D[k][n]) in the compute precision.
+//
+// Batched layouts: element (b, pos) of an array with group width bg sits at
+//   (b / bg) * (N^3 * bg) + pos * bg + (b % bg)
+// bg = 1 is the plain instance-major layout [b][pos].
+
+enum class DftIn { kRealF64, kComplexF64, kComplexF32 };
+enum class DftOut { kComplexF64, kComplexF32, kRealF64, kRealF32 };
+
+// Forward or inverse 3D DFT of B instances, FP64 arithmetic.
+// in: real or complex FP64; tmp: B*N^3 double2 scratch; out: complex FP64
+// (kComplexF64) or its real part (kRealF64).
+cudaError_t dft3_f64(const void *in, DftIn in_kind, int in_bg, double2 *tmp,
+                     void *out, DftOut out_kind, int out_bg,
+                     const double2 *Dt, double prefactor, int N, int B,
+                     cudaStream_t st);
+
+// Same in FP32 arithmetic; in may be real FP64 (f from the caller) or
+// complex FP32; out complex FP32 or real FP64/FP32.
+cudaError_t dft3_f32(const void *in, DftIn in_kind, int in_bg, float2 *tmp,
+                     void *out, DftOut out_kind, int out_bg,
+                     const float2 *Dt, float prefactor, int N, int B,
+                     cudaStream_t st);
+
+// ------------------------------------------------------- convolution ---
+// qhat[b][zeta] = sum_xi W[zeta][xi] * P_b[xi] * R_b[idx(zeta, xi)]
+//               (+ S_b[xi] * T_b[idx(zeta, xi)] when S != nullptr),
+// idx per axis = (zeta_a + N/2 - xi_a) wrapped once into [0, N)
+// (collisions.c:141-160).  W is row-major [N^3][N^3] FP64.  All complex
+// arrays use the plain layout [b][pos].  qhat is written, not accumulated.
+cudaError_t conv_f64(const double *W, const double2 *P, const double2 *R,
+                     const double2 *S, const double2 *T, double2 *qhat,
+                     int N, int B, cudaStream_t st);
+
+// The FP32 batched convolution.  Wblk is FP32 in the tiled layout
+// [zrow][xrow][zz][xz] (zrow = zx*N+zy, xrow = xx*N+xy); P,R,S,T are
+// complex FP32 in the bg-interleaved layout; qacc is a FP64 accumulator in
+// the same interleaved layout [group][zeta][bg] (re, im); status receives
+// the bounded-wait flags.  Returns cudaErrorInvalidValue for unsupported
+// (N, bg).
+struct ConvF32Config {
+    int bg;         // instances per CTA (32, 64 or 128)
+    int stages;     // copy pipeline depth (2 or 3)
+    int flush;      // xi-rows between FP64 flushes of the FP32 partial sums
+};
+cudaError_t conv_f32_batched(const float *Wblk, const float2 *P,
+                             const float2 *R, const float2 *S,
+                             const float2 *T, double2 *qacc, int N, int B,
+                             ConvF32Config cfg, unsigned int *status,
+                             cudaStream_t st);
+size_t conv_f32_smem_bytes(int N, ConvF32Config cfg, bool two_pairs);
+bool conv_f32_supported(int N, ConvF32Config cfg, bool two_pairs);
+
+// Re-layout of FP64 row-major W into the FP32 tiled layout.
+cudaError_t weights_to_tiled_f32(const double *W, float *Wblk, int N,
+                                 cudaStream_t st);
+
+// --------------------------------------------- moments / conservation ---
+struct ConsParams {
+    int N, Ns;
+    double dv;
+    double mass[4];
+    double CCt[8][8];  // LU factors of CC^T (conserve.c:89-168)
+    int pivot[8];
+};
+// Conservation projection (conserve.c:207-264) for one species on B
+// independent instances Q[b][pos] (plain layout), in place, FP64.
+cudaError_t conserve_batch(double *Q, int B, const double *v,
+                           const ConsParams &cp, cudaStream_t st);
+// Multi-species form: Qptrs[n*Ns+m] point at N^3 arrays (one instance).
+cudaError_t conserve_species(double **Qptrs_dev, const double *v,
+                             const ConsParams &cp, cudaStream_t st);
+
+// Maxwellian split of find_maxwellians (collisions.c:91-106) for B
+// instances: M = Maxwellian with the (rho, u, T) of f, computed with the
+// momentRoutines.c formulas (mass, KB); g = f - Mref where Mref = M of the
+// instance's "first" argument (the reference always subtracts M_i).
+// When Mref == nullptr, g = f - M.
+cudaError_t maxwellian_split(const double *f, double *M, double *g,
+                             const double *Mref, int B, int N,
+                             const double *v, double mass, double KB,
+                             double *moments_out, cudaStream_t st);
+
+// Euler / RK2 combinations of boltz.c:206-241 on B*N^3 values.
+cudaError_t axpy_update(double *y, const double *x, const double *q,
+                        double a_y, double a_x, double a_q, long long n,
+                        cudaStream_t st);
+
+// ------------------------------------------------------------ weights ---
+struct WeightParams {
+    int N;
+    double L_v, lambda, mu, dfac, prefactor;
+    double zmax;  // max |zeta_a| over the grid
+};
+// Largest panel count the row kernel supports (16 nodes per panel).
+constexpr int kWeightMaxPanels = 160;
+// Panels needed for the gain integral of the worst row of this grid.
+int weights_panels_needed(const WeightParams &wp);
+// Isotropic weights (weights.c:265-281), FP64, rows [row0, row0+nrows),
+// row-major into W.  zeta is the device Fourier grid.
+cudaError_t weights_iso(double *W, int row0, int nrows, const double *zeta,
+                        const WeightParams &wp, const double *glx,
+                        const double *glw, double *loss_scratch,
+                        cudaStream_t st);
+
+}  // namespace sbte

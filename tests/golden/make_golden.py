@@ -39,7 +39,7 @@ _dp = C.POINTER(C.c_double)
 
 
 class Species(C.Structure):
-    """Layout of the reference's species struct (species.h:8-23)."""
+    """Layout of the reference's species struct (species.h:11-26)."""
     _fields_ = [("id", C.c_size_t), ("num_levels", C.c_size_t),
                 ("lev_id", C.c_void_p), ("Rgas", C.c_double),
                 ("mass", C.c_double), ("mm", C.c_double),
