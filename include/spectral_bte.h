@@ -157,8 +157,9 @@ int spectral_plan_set_conservation(spectral_plan *plan, double mass);
 
 /* Q for B instances.  f and Q are [B][N^3] FP64 in device memory; for
    flag SPECTRAL_FP32 the transforms and the convolution run in FP32 and
-   moments, Maxwellian split and conservation stay FP64.  stream may be
-   NULL (the plan's stream).  Asynchronous. */
+   moments, Maxwellian split and conservation stay FP64.  stream is a
+   cudaStream_t; NULL is the default stream, as in the CUDA runtime.
+   Asynchronous with respect to the host. */
 int spectral_computeQ_device(spectral_plan *plan, const double *f_dev,
                              double *Q_dev, int B, int flags, void *stream);
 /* Same with host arrays: copies in, computes, copies out, synchronises. */

@@ -287,7 +287,8 @@ def _ptr(x) -> int:
 
 def _stream(stream) -> Optional[int]:
     """The CUDA stream to launch on: the given handle, else torch's current
-    stream, so the library's work is ordered with the caller's torch ops."""
+    stream, so the library's work is ordered with the caller's torch ops.
+    None (NULL) is the CUDA default stream, which is torch's default."""
     if stream:
         return int(stream)
     try:

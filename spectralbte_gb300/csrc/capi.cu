@@ -788,7 +788,7 @@ int spectral_plan_set_conservation(spectral_plan *p, double mass)
 int spectral_computeQ_device(spectral_plan *p, const double *f_dev, double *Q_dev,
                              int B, int flags, void *stream)
 {
-    cudaStream_t st = stream ? (cudaStream_t)stream : (p ? p->stream : nullptr);
+    cudaStream_t st = (cudaStream_t)stream;  // NULL: the default stream
     return computeQ_dev(p, f_dev, Q_dev, B, flags, st);
 }
 
@@ -816,7 +816,7 @@ int spectral_computeQ_host(spectral_plan *p, const double *f_host, double *Q_hos
 int spectral_conserve_device(spectral_plan *p, double *Q_dev, int B, void *stream)
 {
     if (!p || !Q_dev || B < 1) return set_error(kErrArg, "bad arguments"), kErrArg;
-    cudaStream_t st = stream ? (cudaStream_t)stream : p->stream;
+    cudaStream_t st = (cudaStream_t)stream;  // NULL: the default stream
     SBTE_LAUNCH(conserve_batch(Q_dev, B, p->d_v, p->cons, st), 1);
     return kOk;
 }
@@ -826,7 +826,7 @@ int spectral_step_device(spectral_plan *p, double *f, int B, double dt, double K
 {
     if (!p || !f || B < 1 || (order != 1 && order != 2))
         return set_error(kErrArg, "step: bad arguments"), kErrArg;
-    cudaStream_t st = stream ? (cudaStream_t)stream : p->stream;
+    cudaStream_t st = (cudaStream_t)stream;  // NULL: the default stream
     SBTE_TRY(ensure_step(p, B));
     const long long n = (long long)B * p->n3;
     const int fl = flags | SPECTRAL_CONSERVE;
