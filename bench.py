@@ -43,6 +43,10 @@ N_DEF, LV_DEF, LAM_DEF = 32, 6.0, 1.0
 # Nominal FP32 CUDA-core peak of GB300: 152 SMs x 128 lanes x 2 flop/FMA
 # at the maximum SM clock.
 N_SM, FP32_LANES = 152, 128
+# DRAM bytes (read + write) of one conv_f32_kernel launch measured by ncu at
+# N=24, B=128, bg=64 (profiles/conv_f32_n24_b128_ncu.md).  W streams once per
+# instance group, so traffic scales with N^6 * B at fixed bg.
+NCU_TRAFFIC = {"bytes": 1.691575e9 + 66.592768e6, "N": 24, "B": 128, "bg": 64}
 
 
 def load_peaks():
@@ -334,7 +338,12 @@ def run_ours(args):
                             "tensor peak binds"),
             "algorithmic": f"10*N^6*B flop per launch = {flops:.3e}",
             "launch_ms": conv_avg_s * 1e3,
-            "traffic": None,
+            "traffic": (NCU_TRAFFIC["bytes"] * (float(n3) ** 2 * B) /
+                        (float(NCU_TRAFFIC["N"]) ** 6 * NCU_TRAFFIC["B"])
+                        if tuned[0] == NCU_TRAFFIC["bg"] else None),
+            "traffic_note": ("bytes per launch, scaled by N^6*B from the ncu capture at N=24, "
+                             "B=128, bg=64; W is re-read once per instance group, from HBM, "
+                             "far below the HBM peak"),
             "hbm": {"achieved": hbm_achieved, "peak": float(peaks["hbm_gbs"]), "unit": "GB/s",
                     "frac": hbm_achieved / float(peaks["hbm_gbs"]),
                     "algorithmic": f"W FP32 {w_bytes:.3e} B per launch"},
