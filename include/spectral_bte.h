@@ -199,6 +199,23 @@ int spectral_plan_conv_time(spectral_plan *plan, double *total_ms,
 /* Synchronise the plan's stream. */
 int spectral_plan_sync(spectral_plan *plan);
 
+/* Allocation-free batched 3D transform.  No counterpart in the reference:
+   it is fft3D (forward for invert = 0, inverse otherwise) on B instances of
+   interleaved complex [B][N^3] device arrays, for callers that cannot call
+   cudaMalloc, e.g. a solver inside a host application that owns all device
+   memory through its own pool, or a step in a time-critical loop.  It
+   allocates nothing.  Its scratch (the axis matrix and the plane-pass
+   intermediate) is one static 32 MiB device array that every GPU loading
+   the library holds until exit; N^2 + B*N^3 must not exceed 2,097,152
+   complex values (N = 32: B <= 63), larger sizes return SPECTRAL_ERR_ARG.
+   The first call on a device looks up the array's device address, so make
+   it before any stream capture.  All calls share the array and nothing in
+   it needs to start at zero; calls that overlap on the GPU race.  in_dev
+   may equal out_dev.  Asynchronous on stream (NULL: default stream). */
+int spectral_fft3d_noalloc(int N, double L_v, const double *v,
+                           const double *zeta, const double *in_dev,
+                           double *out_dev, int B, int invert, void *stream);
+
 /* Number of kernels the library launched since load (monotonic). */
 long long spectral_kernel_launches(void);
 

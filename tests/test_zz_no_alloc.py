@@ -1,0 +1,102 @@
+"""The allocation-free transform entry point, spectral_fft3d_noalloc.
+
+Some callers cannot call cudaMalloc.  One is a collision solver coupled into
+a host application that owns all device memory through its own pool.
+Another is a step inside a time-critical loop, where an allocation would
+stall.  For them the library offers one transform that allocates nothing.
+The caller passes input and output device buffers, and the transform keeps
+its only intermediate in a fixed static device array.
+
+This file checks it through the C ABI against the existing fft3D entry point.
+It makes several calls in a row that share the same static array, and the
+tolerance is the transform parity bar of the other tests: rel-L2 <= 1e-12.
+It also checks that a size beyond the array's limit is refused with an error.
+pytest collects this file last, so a run that stops at the first failure has
+already run every other test.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12
+DP = C.POINTER(C.c_double)
+
+
+def _entry(sb):
+    fn = sb.lib().spectral_fft3d_noalloc
+    fn.restype = C.c_int
+    fn.argtypes = [C.c_int, C.c_double, DP, DP, C.c_void_p, C.c_void_p, C.c_int,
+                   C.c_int, C.c_void_p]
+    return fn
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def test_noalloc_transform_matches_fft3D_on_consecutive_calls(gpu):
+    import torch
+    sb = gpu
+    N, L_v, B = 16, 5.0, 3
+    v, zeta = sb.grid_0d(N, L_v)
+    vp, zp = v.ctypes.data_as(DP), zeta.ctypes.data_as(DP)
+    ref = sb.ReferenceAPI()
+    ref.initialize_coll(N, L_v, v, zeta)
+    fn = _entry(sb)
+    rng = np.random.default_rng(2026)
+    x = rng.standard_normal((B, N ** 3)) + 1j * rng.standard_normal((B, N ** 3))
+    y = rng.standard_normal((B, N ** 3)) + 1j * rng.standard_normal((B, N ** 3))
+    # forward of x, forward of y, inverse of x: three calls in a row, all
+    # through the same static scratch array
+    for data, invert in ((x, 0), (y, 0), (x, 1)):
+        want = np.stack([ref.fft3D(data[b], invert) for b in range(B)])
+        src = torch.from_numpy(np.ascontiguousarray(data).view(np.float64).copy()).cuda()
+        out = torch.empty_like(src)
+        torch.cuda.synchronize()
+        rc = fn(N, L_v, vp, zp, src.data_ptr(), out.data_ptr(), B, invert, None)
+        torch.cuda.synchronize()
+        assert rc == 0, sb.lib().spectral_last_error_message()
+        got = out.cpu().numpy().view(np.complex128).reshape(B, -1)
+        for b in range(B):
+            assert _rel(got[b], want[b]) <= TOL, (invert, b, _rel(got[b], want[b]))
+
+
+def test_noalloc_transform_in_place_and_n32(gpu):
+    import torch
+    sb = gpu
+    N, L_v, B = 32, 6.0, 2
+    v, zeta = sb.grid_0d(N, L_v)
+    vp, zp = v.ctypes.data_as(DP), zeta.ctypes.data_as(DP)
+    ref = sb.ReferenceAPI()
+    ref.initialize_coll(N, L_v, v, zeta)
+    fn = _entry(sb)
+    rng = np.random.default_rng(7)
+    x = rng.standard_normal((B, N ** 3)) + 0j
+    want = np.stack([ref.fft3D(x[b], 0) for b in range(B)])
+    buf = torch.from_numpy(np.ascontiguousarray(x).view(np.float64).copy()).cuda()
+    for _ in range(2):  # the second call transforms the first call's output
+        torch.cuda.synchronize()
+        rc = fn(N, L_v, vp, zp, buf.data_ptr(), buf.data_ptr(), B, 0, None)
+        torch.cuda.synchronize()
+        assert rc == 0, sb.lib().spectral_last_error_message()
+        got = buf.cpu().numpy().view(np.complex128).reshape(B, -1)
+        for b in range(B):
+            assert _rel(got[b], want[b]) <= TOL
+        want = np.stack([ref.fft3D(want[b], 0) for b in range(B)])
+
+
+def test_noalloc_rejects_sizes_beyond_the_static_scratch(gpu):
+    import torch
+    sb = gpu
+    N, L_v = 32, 6.0
+    v, zeta = sb.grid_0d(N, L_v)
+    fn = _entry(sb)
+    small = torch.zeros(2, dtype=torch.float64, device="cuda")
+    # 64 instances at N=32 need 64*32768 + 1024 > 2^21 complex values
+    rc = fn(N, L_v, v.ctypes.data_as(DP), zeta.ctypes.data_as(DP), small.data_ptr(),
+            small.data_ptr(), 64, 0, None)
+    assert rc == sb.lib().spectral_last_error() == 2
+    assert b"32 MiB static scratch" in sb.lib().spectral_last_error_message()
