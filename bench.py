@@ -325,11 +325,13 @@ def run_ours(args):
             "N": N, "L_v": L_v, "lambda": lam, "batch_per_gpu": B,
             "parallelism": f"{world} independent GPU(s), instances sharded",
             "l2": "inputs larger than L2 (W FP32 4.3 GB, f 256 MB at B=1024)",
-            "tuning": {"bg": tuned[0], "stages": tuned[1], "flush": tuned[2]},
+            "tuning": {"variant": tuned[0], "bg": tuned[1], "zs": tuned[2],
+                       "stages": tuned[3], "flush": tuned[4]},
             "learned_operator": "not built",
         },
         "roofline": {
-            "bound": "fp32", "kernel": "conv_f32_kernel",
+            "bound": "fp32",
+            "kernel": "conv_ws_kernel" if tuned[0] == 2 else "conv_f32_kernel",
             "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
             "frac": achieved / fp32_peak,
             "peak_source": (f"nominal FP32 CUDA-core peak, {N_SM} SMs x {FP32_LANES} lanes x 2 "
@@ -340,7 +342,7 @@ def run_ours(args):
             "launch_ms": conv_avg_s * 1e3,
             "traffic": (NCU_TRAFFIC["bytes"] * (float(n3) ** 2 * B) /
                         (float(NCU_TRAFFIC["N"]) ** 6 * NCU_TRAFFIC["B"])
-                        if tuned[0] == NCU_TRAFFIC["bg"] else None),
+                        if tuned[1] == NCU_TRAFFIC["bg"] else None),
             "traffic_note": ("bytes per launch, scaled by N^6*B from the ncu capture at N=24, "
                              "B=128, bg=64; W is re-read once per instance group, from HBM, "
                              "far below the HBM peak"),

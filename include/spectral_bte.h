@@ -175,12 +175,15 @@ int spectral_step_device(spectral_plan *plan, double *f_dev, int B,
                          double dt, double Kn, int order, int flags,
                          void *stream);
 
-/* FP32 convolution tuning: bg = instances per CTA (32, 64, 128),
-   stages = copy pipeline depth, flush = xi-rows per FP64 flush.  The
-   autotuner times the supported shapes on B instances and keeps the
-   fastest; *chosen (optional, 3 ints) receives it. */
-int spectral_plan_set_tuning(spectral_plan *plan, int bg, int stages,
-                             int flush);
+/* FP32 convolution tuning.  variant 1 = block-barrier kernel, 2 = warp-
+   specialised kernel with packed FP32x2 math; bg = instances per CTA (32,
+   64, 128); zs = zeta_z values per thread (variant 2: 8 or 16); stages =
+   copy pipeline depth (variant 1: 2 or 3; variant 2 chooses its own);
+   flush = xi-rows per FP64 flush.  The autotuner times the supported
+   shapes on B instances and keeps the fastest; *chosen (optional, 5 ints:
+   variant, bg, zs, stages, flush) receives it. */
+int spectral_plan_set_tuning(spectral_plan *plan, int variant, int bg, int zs,
+                             int stages, int flush);
 int spectral_plan_autotune(spectral_plan *plan, int B, int flags,
                            int *chosen);
 

@@ -130,7 +130,7 @@ def lib() -> C.CDLL:
         "spectral_computeQ_host": (i, [v, _dp, _dp, i, i]),
         "spectral_conserve_device": (i, [v, v, i, v]),
         "spectral_step_device": (i, [v, v, i, d, d, i, i, v]),
-        "spectral_plan_set_tuning": (i, [v, i, i, i]),
+        "spectral_plan_set_tuning": (i, [v, i, i, i, i, i]),
         "spectral_plan_autotune": (i, [v, i, i, C.POINTER(C.c_int)]),
         "spectral_plan_status": (i, [v, C.POINTER(C.c_uint)]),
         "spectral_plan_sync": (i, [v]),
@@ -370,11 +370,14 @@ class Plan:
         _check(self.L.spectral_step_device(self.h, _ptr(f), B, float(dt), float(Kn), order,
                                            flags, _stream(stream)), "step_device")
 
-    def set_tuning(self, bg: int, stages: int, flush: int):
-        _check(self.L.spectral_plan_set_tuning(self.h, bg, stages, flush), "set_tuning")
+    def set_tuning(self, bg: int, stages: int = 0, flush: int = 16, variant: int = 1,
+                   zs: int = 0):
+        _check(self.L.spectral_plan_set_tuning(self.h, variant, bg, zs, stages, flush),
+               "set_tuning")
 
     def autotune(self, B: int, flags: int = FP32) -> tuple:
-        out = (C.c_int * 3)()
+        """(variant, bg, zs, stages, flush) of the fastest FP32 shape."""
+        out = (C.c_int * 5)()
         _check(self.L.spectral_plan_autotune(self.h, B, flags, out), "autotune")
         return tuple(out)
 

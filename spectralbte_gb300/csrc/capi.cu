@@ -633,7 +633,8 @@ static int q_fp32(spectral_plan_s *p, const double *fdev, double *Qdev, int B,
     if (!conv_f32_supported(N, cfg, maxpreserve)) {
         // the two-pair form stages twice the rows: fall back to a narrower
         // instance group that fits in shared memory
-        const ConvF32Config fallback[] = {{64, 2, cfg.flush}, {32, 2, cfg.flush}};
+        const ConvF32Config fallback[] = {{64, 2, cfg.flush, 3, 8}, {32, 3, cfg.flush, 3, 8},
+                                          {64, 2, cfg.flush}, {32, 2, cfg.flush}};
         bool found = false;
         for (const auto &c : fallback)
             if (!found && conv_f32_supported(N, c, maxpreserve)) {
@@ -652,7 +653,8 @@ static int q_fp32(spectral_plan_s *p, const double *fdev, double *Qdev, int B,
     if (!maxpreserve) {
         SBTE_LAUNCH(dft3_f32(fdev, DftIn::kRealF64, 1, p->tmp32, P, DftOut::kComplexF32, bg,
                              p->Dfwd32, pf_f, N, B, st), 2);
-        SBTE_CUDA(cudaMemsetAsync(p->qacc, 0, sizeof(double2) * (size_t)groups * bg * p->n3, st));
+        if (cfg.variant == 1)
+            SBTE_CUDA(cudaMemsetAsync(p->qacc, 0, sizeof(double2) * (size_t)groups * bg * p->n3, st));
         auto *ev = prof_slot(p);
         if (ev) cudaEventRecord(ev->first, st);
         SBTE_LAUNCH(conv_f32_batched(p->W.w32, P, P, nullptr, nullptr, p->qacc, N, B, cfg,
@@ -669,7 +671,8 @@ static int q_fp32(spectral_plan_s *p, const double *fdev, double *Qdev, int B,
                              p->Dfwd32, pf_f, N, B, st), 2);
         SBTE_LAUNCH(dft3_f32(M, DftIn::kRealF64, 1, p->tmp32, S, DftOut::kComplexF32, bg,
                              p->Dfwd32, pf_f, N, B, st), 2);
-        SBTE_CUDA(cudaMemsetAsync(p->qacc, 0, sizeof(double2) * (size_t)groups * bg * p->n3, st));
+        if (cfg.variant == 1)
+            SBTE_CUDA(cudaMemsetAsync(p->qacc, 0, sizeof(double2) * (size_t)groups * bg * p->n3, st));
         auto *ev = prof_slot(p);
         if (ev) cudaEventRecord(ev->first, st);
         SBTE_LAUNCH(conv_f32_batched(p->W.w32, P, R, S, P, p->qacc, N, B, cfg, p->d_status,
@@ -845,12 +848,15 @@ int spectral_step_device(spectral_plan *p, double *f, int B, double dt, double K
     return kOk;
 }
 
-int spectral_plan_set_tuning(spectral_plan *p, int bg, int stages, int flush)
+int spectral_plan_set_tuning(spectral_plan *p, int variant, int bg, int zs, int stages,
+                             int flush)
 {
     if (!p) return set_error(kErrArg, "null plan"), kErrArg;
-    ConvF32Config c{bg, stages, flush};
+    ConvF32Config c{bg, stages, flush, variant, zs};
     if (!conv_f32_supported(p->N, c, false))
-        return set_error(kErrUnsupported, "unsupported FP32 tuning bg=%d stages=%d", bg, stages),
+        return set_error(kErrUnsupported,
+                         "unsupported FP32 tuning variant=%d bg=%d zs=%d stages=%d", variant, bg,
+                         zs, stages),
                kErrUnsupported;
     p->tune = c;
     return kOk;
@@ -864,8 +870,10 @@ int spectral_plan_autotune(spectral_plan *p, int B, int flags, int *chosen)
     SBTE_TRY(ensure32(p, B));
     SBTE_TRY(ensure_w32(p->W, p->stream));
     const bool two = (flags & SPECTRAL_MAXPRESERVE) != 0;
-    const ConvF32Config cands[] = {{32, 2, 16}, {32, 3, 16}, {64, 2, 16},
-                                   {64, 3, 16}, {128, 2, 16}};
+    const ConvF32Config cands[] = {
+        {32, 2, 16},       {64, 2, 16},       {64, 3, 16},       {128, 2, 16},
+        {32, 2, 16, 2, 8}, {64, 2, 16, 2, 8}, {32, 3, 16, 3, 8}, {64, 2, 16, 3, 8},
+        {64, 3, 16, 3, 8}, {64, 2, 16, 3, 16}, {64, 3, 16, 3, 16}};
     cudaEvent_t e0, e1;
     SBTE_CUDA(cudaEventCreate(&e0));
     SBTE_CUDA(cudaEventCreate(&e1));
@@ -876,6 +884,10 @@ int spectral_plan_autotune(spectral_plan *p, int B, int flags, int *chosen)
         float2 *P = p->c32[0], *R = p->c32[1], *S = p->c32[2];
         float ms_total = 0.f;
         for (int rep = 0; rep < 3; rep++) {
+            if (c.variant == 1)
+                cudaMemsetAsync(p->qacc, 0,
+                                sizeof(double2) * (size_t)((B + c.bg - 1) / c.bg) * c.bg * p->n3,
+                                p->stream);
             cudaEventRecord(e0, p->stream);
             cudaError_t e = conv_f32_batched(p->W.w32, P, R, two ? S : nullptr,
                                              two ? P : nullptr, p->qacc, p->N, B, c,
@@ -902,9 +914,11 @@ int spectral_plan_autotune(spectral_plan *p, int B, int flags, int *chosen)
     cudaEventDestroy(e1);
     p->tune = bestc;
     if (chosen) {
-        chosen[0] = bestc.bg;
-        chosen[1] = bestc.stages;
-        chosen[2] = bestc.flush;
+        chosen[0] = bestc.variant;
+        chosen[1] = bestc.bg;
+        chosen[2] = bestc.zs;
+        chosen[3] = bestc.stages;
+        chosen[4] = bestc.flush;
     }
     return kOk;
 }

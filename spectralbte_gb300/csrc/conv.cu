@@ -21,6 +21,7 @@
 //    flush*N terms.
 #include "common.cuh"
 #include "kernels.h"
+#include "mbarrier.cuh"
 
 #include <cstdint>
 
@@ -88,61 +89,6 @@ conv_f64_kernel(const double *__restrict__ W, const double2 *__restrict__ P,
 }
 
 // ------------------------------------------------------------ FP32 ----
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p)
-{
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)),
-                 "r"(count)
-                 : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
-{
-    asm volatile(
-        "mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
-        "r"(bytes)
-        : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
-{
-    uint32_t done;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(done)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return done != 0;
-}
-
-// Bounded wait: gives up after ~2^31 clocks (about a second) and returns
-// false so the caller can record the failure and leave cleanly.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity)
-{
-    if (mbar_try_wait(bar, parity)) return true;
-    const long long t0 = clock64();
-    while (!mbar_try_wait(bar, parity)) {
-        if (clock64() - t0 > (1LL << 31)) return false;
-    }
-    return true;
-}
-
-__device__ __forceinline__ void bulk_g2s(void *dst, const void *src,
-                                         uint32_t bytes, uint64_t *bar)
-{
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
-        "[%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
-        "l"(src), "r"(bytes), "r"(smem_u32(bar))
-        : "memory");
-}
 
 template <int N, int BG, bool TWO>
 struct F32Layout {
@@ -404,6 +350,9 @@ cudaError_t conv_f64(const double *W, const double2 *P, const double2 *R,
 
 bool conv_f32_supported(int N, ConvF32Config cfg, bool two_pairs)
 {
+    if (cfg.variant == 2 || cfg.variant == 3)
+        return conv_ws_supported(N, cfg.bg, cfg.zs, cfg.variant == 2, cfg.stages, two_pairs);
+    if (cfg.variant != 1) return false;
     if (!(N == 8 || N == 16 || N == 24 || N == 32)) return false;
     const bool ok = (cfg.bg == 32 && (cfg.stages == 2 || cfg.stages == 3)) ||
                     (cfg.bg == 64 && (cfg.stages == 2 || cfg.stages == 3)) ||
@@ -425,6 +374,9 @@ cudaError_t conv_f32_batched(const float *Wblk, const float2 *P,
 {
     const bool two = (S != nullptr);
     if (!conv_f32_supported(N, cfg, two) || B < 1) return cudaErrorInvalidValue;
+    if (cfg.variant == 2 || cfg.variant == 3)
+        return conv_ws(Wblk, P, R, S, T, qacc, N, B, cfg.bg, cfg.zs, cfg.variant == 2,
+                       cfg.stages, cfg.flush, status, st);
     switch (N) {
     case 8:
         return two ? dispatch_bg<8, true>(Wblk, P, R, S, T, qacc, B, cfg, status, st)

@@ -54,9 +54,12 @@ cudaError_t conv_f64(const double *W, const double2 *P, const double2 *R,
 // the bounded-wait flags.  Returns cudaErrorInvalidValue for unsupported
 // (N, bg).
 struct ConvF32Config {
-    int bg;         // instances per CTA (32, 64 or 128)
-    int stages;     // copy pipeline depth (2 or 3)
-    int flush;      // xi-rows between FP64 flushes of the FP32 partial sums
+    int bg;           // instances per CTA (32, 64 or 128)
+    int stages;       // copy pipeline depth (variant 1: 2 or 3)
+    int flush;        // xi-rows between FP64 flushes of the FP32 partial sums
+    int variant = 1;  // 1: block-barrier kernel; 2: warp-specialised with
+                      // packed FP32x2 math; 3: warp-specialised, scalar math
+    int zs = 0;       // variants 2, 3: zeta_z values per thread (8 or 16)
 };
 cudaError_t conv_f32_batched(const float *Wblk, const float2 *P,
                              const float2 *R, const float2 *S,
@@ -65,6 +68,15 @@ cudaError_t conv_f32_batched(const float *Wblk, const float2 *P,
                              cudaStream_t st);
 size_t conv_f32_smem_bytes(int N, ConvF32Config cfg, bool two_pairs);
 bool conv_f32_supported(int N, ConvF32Config cfg, bool two_pairs);
+
+// The warp-specialised FP32x2 variant (conv_ws.cu); writes qacc on its
+// first flush, so it needs no zeroed accumulator.
+bool conv_ws_supported(int N, int bg, int zs, bool packed, int stages,
+                       bool two_pairs);
+cudaError_t conv_ws(const float *Wblk, const float2 *P, const float2 *R,
+                    const float2 *S, const float2 *T, double2 *qacc, int N, int B,
+                    int bg, int zs, bool packed, int stages, int flush,
+                    unsigned int *status, cudaStream_t st);
 
 // Re-layout of FP64 row-major W into the FP32 tiled layout.
 cudaError_t weights_to_tiled_f32(const double *W, float *Wblk, int N,
