@@ -175,6 +175,30 @@ int spectral_step_device(spectral_plan *plan, double *f_dev, int B,
                          double dt, double Kn, int order, int flags,
                          void *stream);
 
+/* 1D-3V solver on the device (boltz.c:264-394 for one species, one rank).
+   f holds nX + 2*order cells of N^3 values, interior cells order ..
+   nX+order-1; x and dx hold the cell centres and widths of all of them
+   (the reference's make_mesh layout).  ic is the reference's Init_field,
+   which selects the boundaries: 3 and 5 diffuse walls at T0 (left) and T1
+   (right), 1 a heated left wall at 2*TWall, 6 periodic, others outflow.
+   Transport is upwindOne (order 1) or the minmod advectTwo (order 2);
+   collisions run for all nX cells in one batched call with conservation,
+   then Euler (order 1) or RK2 (order 2), exactly as boltz.c orders them. */
+int spectral_1d_setup(spectral_plan *plan, int nX, int order, int ic, double dt,
+                      double Kn, const double *x, const double *dx, double T0,
+                      double T1, double TWall, double mass);
+int spectral_1d_step(spectral_plan *plan, double *f_dev, int flags, void *stream);
+/* The transport alone: fconv = advect(f) (also fills f's ghost cells). */
+int spectral_1d_advect(spectral_plan *plan, double *f_dev, double *fconv_dev,
+                       void *stream);
+
+/* CUDA graph of one time step: kind 0 = spectral_step_device(f, B, dt,
+   Kn, order, flags), kind 1 = spectral_1d_step(f, flags).  All scratch is
+   allocated before the capture; the graph replays on f_dev. */
+int spectral_graph_capture(spectral_plan *plan, int kind, double *f_dev, int B,
+                           double dt, double Kn, int order, int flags);
+int spectral_graph_launch(spectral_plan *plan, void *stream);
+
 /* FP32 convolution tuning.  variant 1 = block-barrier kernel, 2 = warp-
    specialised kernel with packed FP32x2 math; bg = instances per CTA (32,
    64, 128); zs = zeta_z values per thread (variant 2: 8 or 16); stages =

@@ -71,6 +71,11 @@ def lib() -> C.CDLL:
             "oracle_conserve_batch1": (None, [C.c_void_p, _dp, i]),
             "oracle_conservation_init": (i, [C.c_void_p, i, d, _dp, _dp, i]),
             "oracle_qhat_rows": (None, [i, _dp, i, i, _dp, _dp, _dp, i]),
+            "oracle_mesh_uniform": (None, [i, d, i, _dp, _dp]),
+            "oracle_init_1d": (None, [C.c_void_p, _dp, _dp]),
+            "oracle_advect": (None, [C.c_void_p, _dp, _dp, _dp, _dp]),
+            "oracle_run_1d": (None, [C.c_void_p, _dp, _dp, i, _dp, i]),
+            "oracle_diffuse_bc": (None, [i, _dp, _dp, _dp, d, i, d, d]),
         }
         for name, (res, args) in sigs.items():
             fn = getattr(L, name)
@@ -223,3 +228,47 @@ def run_0d(N, L_v, W, f0, dt, Kn, nT, order, maxpreserve=True,
                         _p(f), float(dt), float(Kn), nT, order,
                         1 if maxpreserve else 0, _p(rows), nthreads)
     return rows
+
+
+class _P1D(C.Structure):
+    _fields_ = [("N", C.c_int), ("nX", C.c_int), ("order", C.c_int), ("ic", C.c_int),
+                ("L_v", C.c_double), ("dt", C.c_double), ("Kn", C.c_double),
+                ("T0", C.c_double), ("T1", C.c_double), ("TWall", C.c_double),
+                ("mass", C.c_double), ("KB", C.c_double),
+                ("x", C.c_void_p), ("dx", C.c_void_p)]
+
+
+class Run1D:
+    """The 1D solver of boltz.c:254-394 on one rank: transport
+    (transportroutines.c), walls (boundaryConditions.c), initial data
+    (initializer.c:296-424), ComputeQ + conservation per cell."""
+
+    def __init__(self, N, L_v, nX, order, ic, dt, Kn, length=1.0, T0=1.0, T1=2.0,
+                 TWall=1.0, mass=1.0):
+        self.N, self.nX, self.order = N, nX, order
+        self.g = Grid(N, L_v, "1d")
+        nc = nX + 2 * order
+        self.x = np.zeros(nc)
+        self.dx = np.zeros(nc)
+        lib().oracle_mesh_uniform(nX, float(length), order, _p(self.x), _p(self.dx))
+        self.p = _P1D(N, nX, order, ic, float(L_v), float(dt), float(Kn), T0, T1, TWall,
+                      mass, 1.0 if mass == 1.0 else 1.380658e-23,
+                      self.x.ctypes.data, self.dx.ctypes.data)
+        self.n3 = N ** 3
+
+    def init(self) -> np.ndarray:
+        f = np.zeros((self.nX + 2 * self.order, self.n3))
+        lib().oracle_init_1d(C.byref(self.p), _p(self.g.v), _p(f))
+        return f
+
+    def advect(self, f: np.ndarray) -> np.ndarray:
+        fconv = np.zeros_like(f)
+        scratch = np.zeros((self.nX + 6, self.n3))
+        lib().oracle_advect(C.byref(self.p), _p(self.g.v), _p(f), _p(fconv), _p(scratch))
+        return fconv
+
+    def run(self, W, f, nT, nthreads=0) -> np.ndarray:
+        rows = np.zeros((nT + 1, self.nX, 6))
+        lib().oracle_run_1d(C.byref(self.p), _p(np.ascontiguousarray(W, dtype=np.float64)),
+                            _p(f), nT, _p(rows), nthreads)
+        return rows

@@ -695,3 +695,363 @@ void oracle_run_0d(int N, double L_v, const double *W, double *f, double dt,
     }
     free(v); free(zeta); free(Q); free(f1);
 }
+
+/* ------------------------------------------------------------ 1D driver */
+#define KB_JOULES 1.380658e-23 /* constants.h:6 */
+
+void oracle_mesh_uniform(int nX, double length, int order, double *x, double *dx)
+{
+    /* mesh_setup.c:59-160 for one zone on one rank: x = cell centres */
+    double dxz = length / (double)nX, x_edge = 0.0;
+    for (int j = 0; j < nX; j++) {
+        dx[order + j] = dxz;
+        x[order + j] = x_edge + 0.5 * dxz;
+        x_edge += dxz;
+    }
+    for (int g = order - 1; g >= 0; g--) {
+        dx[g] = dx[g + 1];
+        x[g] = x[g + 1] - dx[g + 1];
+    }
+    /* the reference leaves the right ghost cells unset on a single rank
+       (the rank-0 branch of make_mesh); extend the grid uniformly */
+    for (int g = nX + order; g < nX + 2 * order; g++) {
+        dx[g] = dx[g - 1];
+        x[g] = x[g - 1] + dx[g - 1];
+    }
+}
+
+void oracle_init_1d(const oracle_1d *p, const double *v, double *f)
+{
+    /* initializer.c:296-424 */
+    int N = p->N, nX = p->nX, order = p->order;
+    long n3 = (long)N * N * N;
+    double Ma = 1, TWall = 1.0;
+    double rho_l = 1.0, ux_l = 0.0, T_l = 1.0, rho_r = 1.0, ux_r = 0.0, T_r = 1.0;
+    double KB = p->KB, mass = p->mass;
+    switch (p->ic) {
+    case 0:
+        rho_l = 4.0 * Ma * Ma / (Ma * Ma + 3.0);
+        T_l = (5.0 * Ma * Ma - 1.0) * (Ma * Ma + 3.0) / (16.0 * Ma * Ma);
+        ux_l = -sqrt(5.0 / 3.0) * (Ma * Ma + 3.0) / (4.0 * Ma);
+        rho_r = 1.0; T_r = 1.0; ux_r = -Ma * sqrt(5.0 / 3.0);
+        break;
+    case 1: rho_r = 1.0; T_r = TWall; break;
+    case 2: rho_l = 1.0; T_r = 2.0; T_l = 1.0; ux_l = -1.0; ux_r = -1.0; break;
+    case 3: rho_r = 1.0; T_r = 1.5; break;
+    case 5: rho_l = 1.0; T_l = 1.0; break;
+    case 6: rho_l = 1.0; ux_l = 1.2972; T_l = 1.0; rho_r = 1.297; ux_r = 1.0; T_r = 1.195; break;
+    }
+    double maxTemp = T_r;
+    for (int l = order; l < nX + order; l++) {
+        double *fl = f + (long)l * n3;
+        for (int i = 0; i < N; i++)
+            for (int j = 0; j < N; j++)
+                for (int k = 0; k < N; k++) {
+                    long x = k + N * (j + (long)N * i);
+                    double val = 0.0;
+                    switch (p->ic) {
+                    case 0:
+                        if (l < nX / 2)
+                            val = rho_l * exp(-((v[i]) * (v[i]) + v[j] * v[j] + v[k] * v[k]) / T_l) /
+                                  ((T_l * M_PI) * sqrt(T_l * M_PI));
+                        else
+                            val = rho_r * exp(-((v[i]) * (v[i]) + v[j] * v[j] + v[k] * v[k]) / T_r) /
+                                  ((T_r * M_PI) * sqrt(T_r * M_PI));
+                        break;
+                    case 1:
+                        val = (rho_r / mass) * pow(0.5 * mass / (M_PI * KB * maxTemp), 1.5) *
+                              exp(-(0.5 * mass / (KB * maxTemp)) * ((v[i]) * (v[i]) + v[j] * v[j] + v[k] * v[k]));
+                        break;
+                    case 2:
+                        val = rho_l * exp(-((v[i] - ux_l) * (v[i] - ux_l) + v[j] * v[j] + v[k] * v[k]) / T_l) /
+                              ((T_l * M_PI) * sqrt(T_l * M_PI));
+                        break;
+                    case 3:
+                        val = rho_r * exp(-(v[i] * v[i] + v[j] * v[j] + v[k] * v[k]) / T_r) /
+                              ((T_r * M_PI) * sqrt(T_r * M_PI));
+                        break;
+                    case 5:
+                        val = rho_l * exp(-(v[i] * v[i] + v[j] * v[j] + v[k] * v[k]) / T_l) /
+                              ((T_l * M_PI) * sqrt(T_l * M_PI));
+                        break;
+                    case 6:
+                        if (l < nX / 2)
+                            val = rho_l * exp(-((v[i] - ux_l) * (v[i] - ux_l) + v[j] * v[j] + v[k] * v[k]) / T_l) /
+                                  ((T_l * M_PI) * sqrt(T_l * M_PI));
+                        else
+                            val = rho_r * exp(-((v[i] - ux_r) * (v[i] - ux_r) + v[j] * v[j] + v[k] * v[k]) / T_r) /
+                                  ((T_r * M_PI) * sqrt(T_r * M_PI));
+                        break;
+                    }
+                    fl[x] = val;
+                }
+    }
+    (void)ux_r;
+}
+
+void oracle_diffuse_bc(int N, const double *v, const double *in, double *out,
+                       double TW, int bdry, double mass, double KB)
+{
+    /* boundaryConditions.c:39-96 */
+    double wtN[4096];
+    trap_weights(N, wtN);
+    double h_v = v[1] - v[0], sigmaW = 0.0;
+    int ilo = bdry == 0 ? 0 : N / 2, ihi = bdry == 0 ? N / 2 : N;
+    for (int i = ilo; i < ihi; i++)
+        for (int j = 0; j < N; j++)
+            for (int k = 0; k < N; k++)
+                sigmaW += v[i] * wtN[i] * wtN[j] * wtN[k] * h_v * h_v * h_v * in[k + N * (j + N * i)];
+    if (bdry == 0) sigmaW *= -sqrt(2.0 * M_PI * mass / (KB * TW));
+    else sigmaW *= sqrt(2.0 * M_PI * mass / (KB * TW));
+    int olo = bdry == 0 ? N / 2 : 0, ohi = bdry == 0 ? N : N / 2;
+    for (int i = olo; i < ohi; i++)
+        for (int j = 0; j < N; j++)
+            for (int k = 0; k < N; k++)
+                out[k + N * (j + N * i)] = sigmaW * pow(0.5 * mass / (M_PI * KB * TW), 1.5) *
+                    exp(-0.5 * mass / (KB * TW) * (v[i] * v[i] + v[j] * v[j] + v[k] * v[k]));
+}
+
+static double mm_min(double a, double b) { return a > b ? b : a; }
+static double mm_max(double a, double b) { return a > b ? a : b; }
+static double minmod3(double a, double b, double c)
+{
+    /* transportroutines.c:80-90 */
+    if ((a > 0) && (b > 0) && (c > 0)) return mm_min(mm_min(a, b), c);
+    else if ((a < 0) && (b < 0) && (c < 0)) return mm_max(mm_max(a, b), c);
+    return 0;
+}
+
+static void upwind_one(const oracle_1d *p, const double *v, double *f, double *fc)
+{
+    /* transportroutines.c:94-238 on one rank */
+    int N = p->N, nX = p->nX, ic = p->ic;
+    long n3 = (long)N * N * N;
+    double *F0 = f, *F1 = f + n3, *Fn = f + (long)nX * n3, *Fn1 = f + (long)(nX + 1) * n3;
+    if (ic == 3 || ic == 5) oracle_diffuse_bc(N, v, F1, F0, p->T0, 0, p->mass, p->KB);
+    else if (ic == 1) oracle_diffuse_bc(N, v, F1, F0, 2.0 * p->TWall, 0, p->mass, p->KB);
+    else if (ic != 6) memcpy(F0, F1, sizeof(double) * n3);
+    if (ic == 3 || ic == 5) oracle_diffuse_bc(N, v, Fn, Fn1, p->T1, 1, p->mass, p->KB);
+    else if (ic != 6) memcpy(Fn1, Fn, sizeof(double) * n3);
+    if (ic == 6) {
+        memcpy(F0, Fn, sizeof(double) * n3);
+        memcpy(Fn1, F1, sizeof(double) * n3);
+    }
+    double Ma = 1.0;
+    for (int l = 1; l < nX + 1; l++) {
+        const double *fl = f + (long)l * n3, *fm = f + (long)(l - 1) * n3, *fp = f + (long)(l + 1) * n3;
+        double *out = fc + (long)l * n3;
+        for (int i = 0; i < N; i++)
+            for (int j = 0; j < N; j++) {
+                for (int k = 0; k < N; k++) {
+                    long x = k + N * (j + (long)N * i);
+                    double CFL_NUM = p->dt * v[i] / p->dx[l];
+                    if (i < N / 2) out[x] = (1.0 + CFL_NUM) * fl[x] - CFL_NUM * fp[x];
+                    else out[x] = (1.0 - CFL_NUM) * fl[x] + CFL_NUM * fm[x];
+                }
+                if (ic == 5) {
+                    for (int k = 0; k < N; k++) {
+                        long x = k + N * (j + (long)N * i);
+                        double c = Ma * p->dt / (2 * p->dx[l]);
+                        if (j == 0) out[x] = out[x] - c * fl[k + N * ((j + 1) + N * i)];
+                        else if (j == N - 1) out[x] = out[x] - c * fl[k + N * ((j - 1) + N * i)];
+                        else out[x] = out[x] - c * (fl[k + N * ((j + 1) + N * i)] - fl[k + N * ((j - 1) + N * i)]);
+                    }
+                }
+            }
+    }
+}
+
+static void upwind_two(const oracle_1d *p, const double *v, double *f, double *fc,
+                       double *f_l, double *f_r)
+{
+    /* transportroutines.c:241-470 on one rank */
+    int N = p->N, nX = p->nX, ic = p->ic;
+    long n3 = (long)N * N * N;
+    const double *x = p->x, *dx = p->dx;
+    double h_v = v[1] - v[0], Ma = 1.0;
+#define FL(l) (f + (long)(l) * n3)
+    for (long q = 0; q < n3; q++) {
+        FL(1)[q] = 2 * FL(2)[q] - FL(3)[q];
+        FL(nX + 2)[q] = 2 * FL(nX + 1)[q] - FL(nX)[q];
+        /* cells 0 and nX+3 are not filled by the reference on one rank;
+           their values only reach slopes that are never used */
+        FL(0)[q] = FL(1)[q];
+        FL(nX + 3)[q] = FL(nX + 2)[q];
+    }
+    for (int l = 2; l < nX + 2; l++) {
+        if (l == 2) {
+            for (int i = 0; i < N / 2; i++)
+                for (int j = 0; j < N; j++)
+                    for (int k = 0; k < N; k++) {
+                        long q = k + N * (j + (long)N * i);
+                        double s1 = minmod3((FL(2)[q] - FL(1)[q]) / (x[2] - x[1]),
+                                            (FL(3)[q] - FL(2)[q]) / (x[3] - x[2]),
+                                            (FL(3)[q] - FL(1)[q]) / (x[3] - x[1]));
+                        f_l[q] = FL(2)[q] - 0.5 * dx[2] * s1;
+                    }
+            if (ic == 3 || ic == 5) oracle_diffuse_bc(N, v, f_l, f_l, p->T0, 0, p->mass, p->KB);
+            else if (ic == 1) oracle_diffuse_bc(N, v, f_l, f_l, 2.0 * p->TWall, 0, p->mass, p->KB);
+            else {
+                for (int j = 0; j < N; j++)
+                    for (int k = 0; k < N; k++)
+                        for (int i = N / 2; i < N; i++) {
+                            long q = k + N * (j + (long)N * i);
+                            double s1 = minmod3((FL(2)[q] - FL(1)[q]) / (x[2] - x[1]),
+                                                (FL(3)[q] - FL(2)[q]) / (x[3] - x[2]),
+                                                (FL(3)[q] - FL(1)[q]) / (x[3] - x[1]));
+                            f_l[q] = FL(2)[q] + 0.5 * dx[2] * s1;
+                        }
+            }
+        }
+        if (l == nX + 1) {
+            for (int i = N / 2; i < N; i++)
+                for (int j = 0; j < N; j++)
+                    for (int k = 0; k < N; k++) {
+                        long q = k + N * (j + (long)N * i);
+                        double s1 = minmod3((FL(nX + 1)[q] - FL(nX)[q]) / (x[nX + 1] - x[nX]),
+                                            (FL(nX + 2)[q] - FL(nX + 1)[q]) / (x[nX + 2] - x[nX + 1]),
+                                            (FL(nX + 2)[q] - FL(nX)[q]) / (x[nX + 2] - x[nX]));
+                        f_r[q] = FL(nX + 1)[q] + 0.5 * dx[nX + 1] * s1;
+                    }
+            if (ic == 3 || ic == 5) oracle_diffuse_bc(N, v, f_r, f_r, p->T1, l, p->mass, p->KB);
+            else {
+                for (int i = 0; i < N / 2; i++)
+                    for (int j = 0; j < N; j++)
+                        for (int k = 0; k < N; k++) {
+                            long q = k + N * (j + (long)N * i);
+                            double s1 = minmod3((FL(nX + 1)[q] - FL(nX)[q]) / (x[nX + 1] - x[nX]),
+                                                (FL(nX + 2)[q] - FL(nX + 1)[q]) / (x[nX + 2] - x[nX + 1]),
+                                                (FL(nX + 2)[q] - FL(nX)[q]) / (x[nX + 2] - x[nX]));
+                            f_r[q] = FL(nX + 1)[q] - 0.5 * dx[nX + 1] * s1;
+                        }
+            }
+        }
+        double *out = fc + (long)l * n3;
+        for (int j = 0; j < N; j++)
+            for (int k = 0; k < N; k++) {
+                for (int i = N / 2; i < N; i++) {
+                    long q = k + N * (j + (long)N * i);
+                    double s1 = minmod3((FL(l)[q] - FL(l - 1)[q]) / (x[l] - x[l - 1]),
+                                        (FL(l + 1)[q] - FL(l)[q]) / (x[l + 1] - x[l]),
+                                        (FL(l + 1)[q] - FL(l - 1)[q]) / (x[l + 1] - x[l - 1]));
+                    double s0 = minmod3((FL(l - 1)[q] - FL(l - 2)[q]) / (x[l - 1] - x[l - 2]),
+                                        (FL(l)[q] - FL(l - 1)[q]) / (x[l] - x[l - 1]),
+                                        (FL(l)[q] - FL(l - 2)[q]) / (x[l] - x[l - 2]));
+                    double CFL_NUM = 0.5 * p->dt * v[i] / dx[l];
+                    if (l == 2)
+                        out[q] = FL(l)[q] - CFL_NUM * (FL(l)[q] + 0.5 * dx[l] * s1 - f_l[q]);
+                    else
+                        out[q] = FL(l)[q] - CFL_NUM * (FL(l)[q] + 0.5 * dx[l] * s1 -
+                                                      (FL(l - 1)[q] + 0.5 * dx[l - 1] * s0));
+                    if (ic == 5) {
+                        double c = Ma * 0.5 * p->dt / (2 * h_v);
+                        if (j == 0) out[q] = out[q] - c * FL(l)[k + N * ((j + 1) + N * i)];
+                        else if (j == N - 1) out[q] = out[q] - c * FL(l)[k + N * ((j - 1) + N * i)];
+                        else out[q] = out[q] - c * (FL(l)[k + N * ((j + 1) + N * i)] - FL(l)[k + N * ((j - 1) + N * i)]);
+                    }
+                }
+                for (int i = 0; i < N / 2; i++) {
+                    long q = k + N * (j + (long)N * i);
+                    double s2 = minmod3((FL(l + 1)[q] - FL(l)[q]) / (x[l + 1] - x[l]),
+                                        (FL(l + 2)[q] - FL(l + 1)[q]) / (x[l + 2] - x[l + 1]),
+                                        (FL(l + 2)[q] - FL(l)[q]) / (x[l + 2] - x[l]));
+                    double s1 = minmod3((FL(l)[q] - FL(l - 1)[q]) / (x[l] - x[l - 1]),
+                                        (FL(l + 1)[q] - FL(l)[q]) / (x[l + 1] - x[l]),
+                                        (FL(l + 1)[q] - FL(l - 1)[q]) / (x[l + 1] - x[l - 1]));
+                    double CFL_NUM = 0.5 * p->dt * v[i] / dx[l];
+                    if (l == nX + 1)
+                        out[q] = FL(l)[q] - CFL_NUM * (f_r[q] - (FL(l)[q] - 0.5 * dx[l] * s1));
+                    else
+                        out[q] = FL(l)[q] - CFL_NUM * (FL(l + 1)[q] - 0.5 * dx[l + 1] * s2 -
+                                                      (FL(l)[q] - 0.5 * dx[l] * s1));
+                    if (ic == 5) {
+                        double c = Ma * 0.5 * p->dt / (2 * h_v);
+                        if (j == 0) out[q] = out[q] - c * FL(l)[k + N * ((j + 1) + N * i)];
+                        else if (j == N - 1) out[q] = out[q] - c * FL(l)[k + N * ((j - 1) + N * i)];
+                        else out[q] = out[q] - c * (FL(l)[k + N * ((j + 1) + N * i)] - FL(l)[k + N * ((j - 1) + N * i)]);
+                    }
+                }
+            }
+    }
+#undef FL
+}
+
+void oracle_advect(const oracle_1d *p, const double *v, double *f, double *fconv,
+                   double *scratch)
+{
+    int N = p->N, nX = p->nX;
+    long n3 = (long)N * N * N;
+    if (p->order == 1) {
+        upwind_one(p, v, f, fconv);
+        return;
+    }
+    /* advectTwo, transportroutines.c:477-492; scratch = f_tmp + f_l + f_r */
+    double *ftmp = scratch, *f_l = scratch + (long)(nX + 4) * n3, *f_r = f_l + n3;
+    upwind_two(p, v, f, ftmp, f_l, f_r);
+    upwind_two(p, v, ftmp, fconv, f_l, f_r);
+    for (int l = 2; l < nX + 2; l++)
+        for (long q = 0; q < n3; q++)
+            fconv[(long)l * n3 + q] = 0.5 * (f[(long)l * n3 + q] + fconv[(long)l * n3 + q]);
+}
+
+static void stream_row_1d(const oracle_1d *p, const double *v, const double *f, double time,
+                          double *rows)
+{
+    /* write_streams_inhom, output.c:295-340 */
+    int N = p->N;
+    long n3 = (long)N * N * N;
+    for (int l = p->order; l < p->nX + p->order; l++) {
+        double bulkV[3];
+        const double *fl = f + (long)l * n3;
+        double density = oracle_density(N, v, fl, p->mass);
+        oracle_bulk_velocity(N, v, fl, density, p->mass, bulkV);
+        double kinTemp = oracle_temperature(N, v, fl, bulkV, density, p->mass, p->KB);
+        double *r = rows + (long)(l - p->order) * 6;
+        r[0] = time; r[1] = p->x[l]; r[2] = density; r[3] = bulkV[0];
+        r[4] = kinTemp; r[5] = density * kinTemp;
+    }
+}
+
+void oracle_run_1d(const oracle_1d *p, const double *W, double *f, int nT,
+                   double *rows, int nthreads)
+{
+    /* boltz.c:254-394 for one species on one rank */
+    int N = p->N, nX = p->nX, order = p->order;
+    long n3 = (long)N * N * N, ncell = nX + 2 * order;
+    double *v = (double *)malloc(sizeof(double) * N);
+    double *zeta = (double *)malloc(sizeof(double) * N);
+    oracle_grid_1d(N, p->L_v, v, zeta);
+    double *fconv = (double *)calloc((size_t)ncell * n3, sizeof(double));
+    double *f1 = (double *)calloc((size_t)ncell * n3, sizeof(double));
+    double *scratch = (double *)calloc((size_t)(nX + 6) * n3, sizeof(double));
+    double *Q = (double *)malloc(sizeof(double) * n3);
+    oracle_cons cons;
+    double mass = p->mass;
+    oracle_conservation_init(&cons, N, v[1] - v[0], v, &mass, 1);
+    stream_row_1d(p, v, f, 0.0, rows);
+    for (int t = 0; t < nT; t++) {
+        oracle_advect(p, v, f, fconv, scratch);
+        for (int l = order; l < nX + order; l++) {
+            double *fc = fconv + (long)l * n3;
+            oracle_computeQ(N, p->L_v, v, zeta, W, fc, fc, Q, nthreads);
+            oracle_conserve(&cons, &Q);
+            double *dst = (order == 1) ? f + (long)l * n3 : f1 + (long)l * n3;
+            for (long q = 0; q < n3; q++) {
+                dst[q] = fc[q];
+                dst[q] += p->dt * Q[q] / p->Kn;
+            }
+            if (order == 2) {
+                double *g1 = f1 + (long)l * n3;
+                oracle_computeQ(N, p->L_v, v, zeta, W, g1, g1, Q, nthreads);
+                oracle_conserve(&cons, &Q);
+                for (long q = 0; q < n3; q++) {
+                    fc[q] = 0.5 * fc[q] + 0.5 * g1[q];
+                    fc[q] += 0.5 * p->dt * Q[q] / p->Kn;
+                }
+            }
+        }
+        if (order == 2) oracle_advect(p, v, fconv, f, scratch);
+        stream_row_1d(p, v, f, p->dt * (t + 1), rows + (long)(t + 1) * nX * 6);
+    }
+    free(v); free(zeta); free(fconv); free(f1); free(scratch); free(Q);
+}

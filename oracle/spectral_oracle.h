@@ -133,6 +133,36 @@ void oracle_run_0d(int N, double L_v, const double *W, double *f, double dt,
 /* BKW initial data, initializer.c:123-135 (K from t0 = 5.5 unless K > 0). */
 void oracle_init_bkw(int N, const double *v, double K, double *f);
 
+/* ---- 1D driver (exec/boltz.c:254-394, transportroutines.c,
+        boundaryConditions.c, initializer.c:296-424, mesh_setup.c) ------- */
+typedef struct {
+    int N, nX, order, ic;      /* ic = the reference's Init_field value */
+    double L_v, dt, Kn;
+    double T0, T1, TWall;      /* wall temperatures (transportroutines.c:46-50) */
+    double mass, KB;
+    const double *x, *dx;      /* nX + 2*order entries incl. ghost cells */
+} oracle_1d;
+
+/* One zone of nX cells over [0, length], single rank (mesh_setup.c:59-160),
+   ghost cells by uniform extension on both sides. */
+void oracle_mesh_uniform(int nX, double length, int order, double *x, double *dx);
+/* Initial data of the interior cells, initializer.c:296-424. f holds
+   nX + 2*order cells of N^3. */
+void oracle_init_1d(const oracle_1d *p, const double *v, double *f);
+/* Diffuse reflection, boundaryConditions.c:39-96 (bdry 0 = left wall). */
+void oracle_diffuse_bc(int N, const double *v, const double *in, double *out,
+                       double TW, int bdry, double mass, double KB);
+/* upwindOne / advectTwo for a single rank (transportroutines.c:94-238,
+   241-470, 477-492).  f and fconv hold nX + 2*order cells.  scratch holds
+   nX + 2*order + 2 cells. */
+void oracle_advect(const oracle_1d *p, const double *v, double *f, double *fconv,
+                   double *scratch);
+/* nT steps of the 1D loop (boltz.c:264-394) with ComputeQ + conservation per
+   cell; rows receives (nT+1) dumps of nX lines (time, x, density, u_x,
+   temperature, pressure), as write_streams_inhom prints (output.c:295-340). */
+void oracle_run_1d(const oracle_1d *p, const double *W, double *f, int nT,
+                   double *rows, int nthreads);
+
 #ifdef __cplusplus
 }
 #endif

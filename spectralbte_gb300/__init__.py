@@ -135,6 +135,11 @@ def lib() -> C.CDLL:
         "spectral_plan_status": (i, [v, C.POINTER(C.c_uint)]),
         "spectral_plan_sync": (i, [v]),
         "spectral_plan_set_profiling": (i, [v, i]),
+        "spectral_1d_setup": (i, [v, i, i, i, d, d, _dp, _dp, d, d, d, d]),
+        "spectral_1d_step": (i, [v, v, i, v]),
+        "spectral_1d_advect": (i, [v, v, v, v]),
+        "spectral_graph_capture": (i, [v, i, v, i, d, d, i, i]),
+        "spectral_graph_launch": (i, [v, v]),
         "spectral_plan_conv_time": (i, [v, _dp, C.POINTER(C.c_int)]),
     }
     for name, (res, args) in sigs.items():
@@ -388,6 +393,31 @@ class Plan:
 
     def sync(self):
         _check(self.L.spectral_plan_sync(self.h), "sync")
+
+    def setup_1d(self, nX: int, order: int, ic: int, dt: float, Kn: float, x, dx,
+                 T0: float = 1.0, T1: float = 2.0, TWall: float = 1.0, mass: float = 1.0):
+        """1D-3V solver state: nX cells + 2*order ghosts (see spectral_1d_setup)."""
+        self._x = np.ascontiguousarray(x, dtype=np.float64)
+        self._dx = np.ascontiguousarray(dx, dtype=np.float64)
+        _check(self.L.spectral_1d_setup(self.h, nX, order, ic, float(dt), float(Kn),
+                                        _p(self._x), _p(self._dx), T0, T1, TWall, mass),
+               "spectral_1d_setup")
+
+    def step_1d(self, f, flags: int = FP64, stream: int = 0):
+        _check(self.L.spectral_1d_step(self.h, _ptr(f), flags, _stream(stream)), "spectral_1d_step")
+
+    def advect_1d(self, f, fconv, stream: int = 0):
+        _check(self.L.spectral_1d_advect(self.h, _ptr(f), _ptr(fconv), _stream(stream)),
+               "spectral_1d_advect")
+
+    def capture(self, kind: int, f, B: int = 0, dt: float = 0.0, Kn: float = 1.0,
+                order: int = 1, flags: int = FP64):
+        """Capture one time step (kind 0: 0D step, 1: 1D step) as a CUDA graph."""
+        _check(self.L.spectral_graph_capture(self.h, kind, _ptr(f), B, float(dt), float(Kn),
+                                             order, flags), "spectral_graph_capture")
+
+    def launch(self, stream: int = 0):
+        _check(self.L.spectral_graph_launch(self.h, _stream(stream)), "spectral_graph_launch")
 
     def set_profiling(self, on: bool):
         _check(self.L.spectral_plan_set_profiling(self.h, 1 if on else 0), "set_profiling")

@@ -17,8 +17,8 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libspectral_gb300.so")
 
-SOURCES = ["fft3d.cu", "conv.cu", "conv_ws.cu", "conserve.cu", "weights.cu", "capi.cu",
-           "noalloc.cu"]
+SOURCES = ["fft3d.cu", "conv.cu", "conv_ws.cu", "conserve.cu", "weights.cu", "transport.cu",
+           "capi.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
          "-Xcompiler", "-fvisibility=default"]

@@ -423,6 +423,15 @@ struct spectral_plan_s {
     bool profiling = false;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_events;
     size_t prof_used = 0;
+    // 1D-3V transport state (spectral_1d_setup)
+    bool t1d = false;
+    TransportParams tp{};
+    double Kn = 1.0;
+    double *d_x = nullptr, *d_dx = nullptr;
+    double *fconv = nullptr, *f1 = nullptr, *ftmp = nullptr, *f_l = nullptr, *f_r = nullptr;
+    // captured time step
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
     // host staging for spectral_computeQ_host
     int caphost = 0;
     double *d_fh = nullptr, *d_Qh = nullptr;
@@ -441,6 +450,9 @@ struct spectral_plan_s {
         dfree(qacc); dfree(tmp32);
         for (auto &p : r32) dfree(p);
         dfree(sQ); dfree(sf1); dfree(d_fh); dfree(d_Qh);
+        dfree(d_x); dfree(d_dx); dfree(fconv); dfree(f1); dfree(ftmp); dfree(f_l); dfree(f_r);
+        if (graph_exec) cudaGraphExecDestroy(graph_exec);
+        if (graph) cudaGraphDestroy(graph);
         for (auto &ev : prof_events) {
             cudaEventDestroy(ev.first);
             cudaEventDestroy(ev.second);
@@ -705,6 +717,54 @@ static int computeQ_dev(spectral_plan_s *p, const double *f, double *Q, int B,
     return kOk;
 }
 
+// Transport of the 1D solver: order 1 = upwindOne, order 2 = advectTwo
+// (two upwindTwo half-steps averaged, transportroutines.c:477-492).
+static int advect_1d(spectral_plan_s *p, double *f, double *fc, cudaStream_t st)
+{
+    const TransportParams &tp = p->tp;
+    const long long n3 = p->n3;
+    if (tp.order == 1) {
+        SBTE_LAUNCH(transport_ghosts1(f, p->d_v, tp, st), 1);
+        SBTE_LAUNCH(transport_upwind1(f, fc, p->d_v, p->d_dx, tp, st), 1);
+        return kOk;
+    }
+    SBTE_LAUNCH(transport_upwind2(f, p->ftmp, p->f_l, p->f_r, p->d_v, p->d_x, p->d_dx, tp, st), 4);
+    SBTE_LAUNCH(transport_upwind2(p->ftmp, fc, p->f_l, p->f_r, p->d_v, p->d_x, p->d_dx, tp, st), 4);
+    // f_conv = 0.5 (f + f_conv) on cells 2..nX+1
+    SBTE_LAUNCH(axpy_update(fc + 2 * n3, f + 2 * n3, nullptr, 0.5, 0.5, 0.0,
+                            (long long)tp.nX * n3, st), 1);
+    return kOk;
+}
+
+// One step of the 1D loop (boltz.c:270-353): transport, then ComputeQ +
+// conservation + Euler or RK2 for all nX cells in one batched call, then
+// the second transport half for order 2.
+static int step_1d(spectral_plan_s *p, double *f, int flags, cudaStream_t st)
+{
+    const TransportParams &tp = p->tp;
+    const long long n3 = p->n3;
+    const int nX = tp.nX, o = tp.order;
+    SBTE_TRY(ensure_step(p, nX));
+    const int fl = flags | SPECTRAL_CONSERVE;
+    double *fc_int = p->fconv + o * n3, *f_int = f + o * n3;
+    SBTE_TRY(advect_1d(p, f, p->fconv, st));
+    SBTE_TRY(computeQ_dev(p, fc_int, p->sQ, nX, fl, st));
+    const double a = tp.dt / p->Kn;
+    if (o == 1) {
+        // f = f_conv + dt Q / Kn  (boltz.c:302,315)
+        SBTE_LAUNCH(axpy_update(f_int, fc_int, p->sQ, 0.0, 1.0, a, (long long)nX * n3, st), 1);
+        return kOk;
+    }
+    // f_1 = f_conv + dt Q / Kn; Q = Q(f_1); f_conv = (f_conv + f_1)/2 + dt Q/(2 Kn)
+    // (boltz.c:307,317,327-342), then transport back into f
+    double *f1_int = p->f1 + o * n3;
+    SBTE_LAUNCH(axpy_update(f1_int, fc_int, p->sQ, 0.0, 1.0, a, (long long)nX * n3, st), 1);
+    SBTE_TRY(computeQ_dev(p, f1_int, p->sQ, nX, fl, st));
+    SBTE_LAUNCH(axpy_update(fc_int, f1_int, p->sQ, 0.5, 0.5, 0.5 * a, (long long)nX * n3, st), 1);
+    SBTE_TRY(advect_1d(p, p->fconv, f, st));
+    return kOk;
+}
+
 }  // namespace sbte
 
 // ====================================================== Part 2 (C API) ===
@@ -845,6 +905,112 @@ int spectral_step_device(spectral_plan *p, double *f, int B, double dt, double K
     SBTE_LAUNCH(axpy_update(p->sf1, nullptr, p->sQ, 1.0, 0.0, dt / Kn, n, st), 1);
     SBTE_TRY(computeQ_dev(p, p->sf1, p->sQ, B, fl, st));
     SBTE_LAUNCH(axpy_update(f, p->sf1, p->sQ, 0.5, 0.5, 0.5 * dt / Kn, n, st), 1);
+    return kOk;
+}
+
+int spectral_1d_setup(spectral_plan *p, int nX, int order, int ic, double dt, double Kn,
+                      const double *x, const double *dx, double T0, double T1, double TWall,
+                      double mass)
+{
+    if (!p || nX < 3 || (order != 1 && order != 2) || !x || !dx || Kn <= 0)
+        return set_error(kErrArg, "spectral_1d_setup: bad arguments"), kErrArg;
+    SBTE_CUDA(cudaSetDevice(p->device));
+    const int nc = nX + 2 * order;
+    TransportParams tp{p->N, nX, order, ic, dt, T0, T1, TWall, mass,
+                       mass == 1.0 ? 1.0 : 1.380658e-23};
+    dfree(p->d_x); dfree(p->d_dx); dfree(p->fconv); dfree(p->f1); dfree(p->ftmp);
+    dfree(p->f_l); dfree(p->f_r);
+    p->t1d = false;
+    const size_t cells = (size_t)nc * p->n3;
+    SBTE_TRY(dalloc(&p->d_x, nc));
+    SBTE_TRY(dalloc(&p->d_dx, nc));
+    SBTE_TRY(dalloc(&p->fconv, cells));
+    SBTE_TRY(dalloc(&p->f1, cells));
+    SBTE_TRY(dalloc(&p->ftmp, cells));
+    SBTE_TRY(dalloc(&p->f_l, (size_t)p->n3));
+    SBTE_TRY(dalloc(&p->f_r, (size_t)p->n3));
+    SBTE_CUDA(cudaMemcpy(p->d_x, x, sizeof(double) * nc, cudaMemcpyHostToDevice));
+    SBTE_CUDA(cudaMemcpy(p->d_dx, dx, sizeof(double) * nc, cudaMemcpyHostToDevice));
+    SBTE_CUDA(cudaMemset(p->fconv, 0, cells * sizeof(double)));
+    SBTE_CUDA(cudaMemset(p->f1, 0, cells * sizeof(double)));
+    SBTE_CUDA(cudaMemset(p->ftmp, 0, cells * sizeof(double)));
+    SBTE_TRY(ensure_step(p, nX));
+    p->tp = tp;
+    p->Kn = Kn;
+    p->t1d = true;
+    SBTE_TRY(spectral_plan_set_conservation(p, mass));
+    return kOk;
+}
+
+int spectral_1d_advect(spectral_plan *p, double *f_dev, double *fconv_dev, void *stream)
+{
+    if (!p || !p->t1d || !f_dev || !fconv_dev)
+        return set_error(kErrNotInit, "spectral_1d_advect: call spectral_1d_setup first"),
+               kErrNotInit;
+    return advect_1d(p, f_dev, fconv_dev, (cudaStream_t)stream);
+}
+
+int spectral_1d_step(spectral_plan *p, double *f_dev, int flags, void *stream)
+{
+    if (!p || !p->t1d || !f_dev)
+        return set_error(kErrNotInit, "spectral_1d_step: call spectral_1d_setup first"),
+               kErrNotInit;
+    if (!p->W.w64) return set_error(kErrWeights, "spectral_1d_step: no weights"), kErrWeights;
+    SBTE_CUDA(cudaSetDevice(p->device));
+    return step_1d(p, f_dev, flags, (cudaStream_t)stream);
+}
+
+int spectral_graph_capture(spectral_plan *p, int kind, double *f_dev, int B, double dt,
+                           double Kn, int order, int flags)
+{
+    if (!p || !f_dev || (kind != 0 && kind != 1))
+        return set_error(kErrArg, "spectral_graph_capture: bad arguments"), kErrArg;
+    SBTE_CUDA(cudaSetDevice(p->device));
+    // every allocation happens before the capture
+    const int nb = kind == 1 ? p->tp.nX : B;
+    if (kind == 1 && !p->t1d)
+        return set_error(kErrNotInit, "graph capture of a 1D step needs spectral_1d_setup"),
+               kErrNotInit;
+    SBTE_TRY(ensure_step(p, nb));
+    if (flags & SPECTRAL_FP32) {
+        SBTE_TRY(ensure32(p, nb));
+        SBTE_TRY(ensure_w32(p->W, p->stream));
+    } else {
+        SBTE_TRY(ensure64(p, nb));
+    }
+    if (p->graph_exec) {
+        cudaGraphExecDestroy(p->graph_exec);
+        p->graph_exec = nullptr;
+    }
+    if (p->graph) {
+        cudaGraphDestroy(p->graph);
+        p->graph = nullptr;
+    }
+    const bool prof = p->profiling;
+    p->profiling = false;
+    SBTE_CUDA(cudaStreamSynchronize(p->stream));
+    SBTE_CUDA(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeRelaxed));
+    int rc = kind == 1 ? step_1d(p, f_dev, flags, p->stream)
+                       : spectral_step_device(p, f_dev, B, dt, Kn, order, flags, p->stream);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(p->stream, &g);
+    p->profiling = prof;
+    if (rc != kOk) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess) return set_error(kErrCuda, "graph capture: %s", cudaGetErrorString(e)),
+                                 kErrCuda;
+    p->graph = g;
+    SBTE_CUDA(cudaGraphInstantiate(&p->graph_exec, g, 0));
+    return kOk;
+}
+
+int spectral_graph_launch(spectral_plan *p, void *stream)
+{
+    if (!p || !p->graph_exec)
+        return set_error(kErrNotInit, "spectral_graph_launch: nothing captured"), kErrNotInit;
+    SBTE_CUDA(cudaGraphLaunch(p->graph_exec, (cudaStream_t)stream));
     return kOk;
 }
 

@@ -215,7 +215,7 @@ __global__ void axpy_kernel(double *__restrict__ y, const double *__restrict__ x
 {
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
          t += (long long)gridDim.x * blockDim.x) {
-        double r = a_y * y[t];
+        double r = (a_y != 0.0) ? a_y * y[t] : 0.0;  // y is not read when a_y == 0
         if (x) r += a_x * x[t];
         if (q) r += a_q * q[t];
         y[t] = r;

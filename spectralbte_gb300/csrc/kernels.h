@@ -113,6 +113,25 @@ cudaError_t axpy_update(double *y, const double *x, const double *q,
                         double a_y, double a_x, double a_q, long long n,
                         cudaStream_t st);
 
+// ---------------------------------------------------------- transport ---
+// The 1D-3V transport of transportroutines.c on one device array of
+// nX + 2*order cells of N^3 values, for one rank.
+struct TransportParams {
+    int N, nX, order, ic;   // ic: the reference's Init_field (boundary kind)
+    double dt, T0, T1, TWall, mass, KB;
+};
+// Ghost cells of upwindOne (walls, outflow copy or periodic).
+cudaError_t transport_ghosts1(double *f, const double *v, const TransportParams &tp,
+                              cudaStream_t st);
+// upwindOne for cells 1..nX: fc from f (ghosts already set).
+cudaError_t transport_upwind1(const double *f, double *fc, const double *v,
+                              const double *dx, const TransportParams &tp,
+                              cudaStream_t st);
+// upwindTwo for cells 2..nX+1 (fills f's ghosts, wall values f_l, f_r).
+cudaError_t transport_upwind2(double *f, double *fc, double *f_l, double *f_r,
+                              const double *v, const double *x, const double *dx,
+                              const TransportParams &tp, cudaStream_t st);
+
 // ------------------------------------------------------------ weights ---
 struct WeightParams {
     int N;

@@ -111,3 +111,24 @@ def test_gauss_legendre(oracle):
     assert abs(w.sum() - 2) < 1e-14
     # exact for x^30
     assert abs((w * x ** 30).sum() - 2 / 31) < 1e-14
+
+
+def test_heat_transport_golden_moments(oracle):
+    """The heat_transport regression of the reference (1D, 250 cells, N=8,
+    L_v=9, lambda=1, Kn=3.2, first-order upwind between diffuse walls at
+    T=1 and T=2, dt=1e-4, 10 steps).  x, density, temperature and pressure
+    match to every printed digit.  u_x is round-off noise (~1e-15) in the
+    interior, where it depends on the last bits of W; the wall cells carry
+    a real velocity, which matches to the printed precision."""
+    r = oracle.Run1D(8, 9.0, 250, 1, 3, 1e-4, 3.2)
+    W = oracle.weights_iso(r.g, 1.0)
+    rows = r.run(W, r.init(), 10)
+    want = np.loadtxt(os.path.join(GOLDEN, "moments_heat_transport.txt")).reshape(11, 250, 6)
+    printed = np.vectorize(lambda x: float("%e" % x))(rows)
+    for c in (0, 1, 2, 4, 5):
+        assert np.array_equal(printed[..., c], want[..., c]), c
+    ux, wux = rows[..., 3], want[..., 3]
+    real = np.abs(wux) > 1e-10
+    assert real.sum() > 10
+    assert np.all(np.abs(ux[real] - wux[real]) <= 1e-6 * np.abs(wux[real]))
+    assert np.all(np.abs(ux[~real] - wux[~real]) < 1e-13)
