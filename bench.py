@@ -58,18 +58,26 @@ def load_peaks():
 
 
 def two_maxwellian_batch(v: np.ndarray, B: int, seed: int) -> np.ndarray:
-    """Discontinuous two-Maxwellian in v_x with +-5% jitter per parameter."""
-    rng = np.random.default_rng(seed)
-    N = v.size
-    vx, vy, vz = v[:, None, None], v[None, :, None], v[None, None, :]
-    out = np.empty((B, N ** 3))
-    for b in range(B):
-        j = rng.uniform(-0.05, 0.05, 5) + 1.0
-        r1, t1, r2, t2, u2 = 1.0 * j[0], 1.0 * j[1], 1.0 * j[2], 2.0 * j[3], 0.5 * j[4]
-        m1 = r1 * (2 * np.pi * t1) ** -1.5 * np.exp(-(vx ** 2 + vy ** 2 + vz ** 2) / (2 * t1))
-        m2 = r2 * (2 * np.pi * t2) ** -1.5 * np.exp(-((vx - u2) ** 2 + vy ** 2 + vz ** 2) / (2 * t2))
-        out[b] = np.where(vx < 0, m1, m2).reshape(-1)
-    return out
+    from spectralbte_gb300.workloads import two_maxwellian_batch as gen
+    return gen(v, B, seed)
+
+
+def max_over_ranks(value: float, dist) -> float:
+    """The max of a per-rank float over all ranks (the step time that
+    bounds the job), on whatever backend the process group uses."""
+    if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
+        return float(value)
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(value)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units_per_rank: int, steps: int, world: int, max_ms: float) -> float:
+    """Whole-job throughput: every rank evaluates its own instances (weak
+    scaling), and the slowest rank sets the time."""
+    return units_per_rank * steps * world / (max_ms / 1e3)
 
 
 class ClockSampler:
@@ -198,6 +206,55 @@ def run_reference(args):
     return 0
 
 
+def run_uneven(args):
+    """Config 4: one uneven batch of instances with N drawn from {16, 24, 32}
+    and lambda from {0, 1} (seeded), Maxwellian mixtures normalised to unit
+    mass.  Each (N, lambda) group has its own plan, and the groups run
+    together through spectral_group_computeQ."""
+    import torch
+    import spectralbte_gb300 as sb
+    from spectralbte_gb300.workloads import maxwellian_mixture_batch
+    torch.cuda.set_device(0)
+    rng = np.random.default_rng(args.seed)
+    Ns = rng.choice([16, 24, 32], size=args.batch)
+    lams = rng.choice([0.0, 1.0], size=args.batch)
+    plans, fs, Qs, groups = [], [], [], []
+    for N in (16, 24, 32):
+        for lam in (0.0, 1.0):
+            B = int(((Ns == N) & (lams == lam)).sum())
+            if B == 0:
+                continue
+            v, zeta = sb.grid_0d(N, LV_DEF)
+            p = sb.Plan(N, LV_DEF, v, zeta, B)
+            p.generate_weights_iso(lam)
+            f = torch.from_numpy(maxwellian_mixture_batch(v, B, args.seed + N + int(lam))).cuda()
+            p.autotune(B, sb.FP32)
+            plans.append(p)
+            fs.append(f)
+            Qs.append(torch.empty_like(f))
+            groups.append({"N": N, "lambda": lam, "instances": B})
+    flags = sb.FP32 | sb.CONSERVE
+    for _ in range(args.warmup):
+        sb.group_computeQ(plans, fs, Qs, flags)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        sb.group_computeQ(plans, fs, Qs, flags)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    line = {"metric": "Q evals/s, uneven batch N in {16,24,32} x lambda in {0,1}",
+            "value": args.batch / (ms / 1e3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "dtype": "fp32 (FP64 moments and conservation)", "data": "synthetic",
+            "config": {"workload": f"{args.batch} instances, Maxwellian mixtures, unit mass",
+                       "groups": groups}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_ours(args):
     import torch
     import spectralbte_gb300 as sb
@@ -246,12 +303,10 @@ def run_ours(args):
     conv_ms, conv_n = plan.conv_time()
     plan.set_profiling(False)
     clk = clocks.stop()
+    ms_total = max_over_ranks(ms_total, dist)
     if dist:
-        tt = torch.tensor([ms_total], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms_total = float(tt.item())
         dist.barrier()
-    value = B * args.steps * world / (ms_total / 1e3)
+    value = job_rate(B, args.steps, world, ms_total)
 
     # end to end through the C ABI with host buffers (pinned)
     f_pin = torch.from_numpy(f_host).pin_memory()
@@ -380,7 +435,10 @@ def main():
     ap.add_argument("--fp64-batch", type=int, default=8)
     ap.add_argument("--cpu-rows", type=int, default=2048)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="n32", choices=["n32", "uneven"])
     args = ap.parse_args()
+    if args.workload == "uneven" and args.impl != "reference":
+        return run_uneven(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -175,6 +175,14 @@ int spectral_step_device(spectral_plan *plan, double *f_dev, int B,
                          double dt, double Kn, int order, int flags,
                          void *stream);
 
+/* Uneven batches: Q for several plans at once (one plan per velocity grid
+   N and weight table, e.g. N in {16, 24, 32} x lambda in {0, 1}).  Plan i
+   evaluates B[i] instances f_dev[i] -> Q_dev[i] on its own stream, forked
+   from and joined back to `stream`, so the groups overlap on the device. */
+int spectral_group_computeQ(spectral_plan **plans, int nplans,
+                            const double *const *f_dev, double *const *Q_dev,
+                            const int *B, int flags, void *stream);
+
 /* 1D-3V solver on the device (boltz.c:264-394 for one species, one rank).
    f holds nX + 2*order cells of N^3 values, interior cells order ..
    nX+order-1; x and dx hold the cell centres and widths of all of them

@@ -140,6 +140,8 @@ def lib() -> C.CDLL:
         "spectral_1d_advect": (i, [v, v, v, v]),
         "spectral_graph_capture": (i, [v, i, v, i, d, d, i, i]),
         "spectral_graph_launch": (i, [v, v]),
+        "spectral_group_computeQ": (i, [C.POINTER(C.c_void_p), i, C.POINTER(C.c_void_p),
+                                        C.POINTER(C.c_void_p), C.POINTER(C.c_int), i, v]),
         "spectral_plan_conv_time": (i, [v, _dp, C.POINTER(C.c_int)]),
     }
     for name, (res, args) in sigs.items():
@@ -428,6 +430,18 @@ class Plan:
         n = C.c_int()
         _check(self.L.spectral_plan_conv_time(self.h, C.byref(ms), C.byref(n)), "conv_time")
         return ms.value, n.value
+
+
+def group_computeQ(plans, fs, Qs, flags: int = FP32 | CONSERVE, stream: int = 0):
+    """Q for several plans at once (spectral_group_computeQ); fs[i], Qs[i]
+    are [B_i][N_i^3] device tensors of plan i."""
+    n = len(plans)
+    ph = (C.c_void_p * n)(*[p.h.value for p in plans])
+    fp = (C.c_void_p * n)(*[_ptr(f) for f in fs])
+    qp = (C.c_void_p * n)(*[_ptr(q) for q in Qs])
+    bs = (C.c_int * n)(*[int(f.shape[0]) for f in fs])
+    _check(lib().spectral_group_computeQ(ph, n, fp, qp, bs, flags, _stream(stream)),
+           "spectral_group_computeQ")
 
 
 def kernel_launches() -> int:

@@ -1014,6 +1014,45 @@ int spectral_graph_launch(spectral_plan *p, void *stream)
     return kOk;
 }
 
+// Several plans (one per velocity grid and weight table) evaluated together:
+// each plan runs on its own stream, forked from and joined back to the
+// caller's stream, so batches of different N overlap on the device.
+int spectral_group_computeQ(spectral_plan **plans, int nplans, const double *const *f_dev,
+                            double *const *Q_dev, const int *B, int flags, void *stream)
+{
+    if (!plans || nplans < 1 || !f_dev || !Q_dev || !B)
+        return set_error(kErrArg, "spectral_group_computeQ: bad arguments"), kErrArg;
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaEvent_t fork;
+    SBTE_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+    SBTE_CUDA(cudaEventRecord(fork, st));
+    std::vector<cudaEvent_t> done;
+    int rc = kOk;
+    for (int i = 0; i < nplans && rc == kOk; i++) {
+        spectral_plan_s *p = plans[i];
+        if (!p || B[i] < 1) {
+            rc = kErrArg;
+            set_error(kErrArg, "spectral_group_computeQ: plan %d", i);
+            break;
+        }
+        if (cudaStreamWaitEvent(p->stream, fork, 0) != cudaSuccess) {
+            rc = kErrCuda;
+            break;
+        }
+        rc = computeQ_dev(p, f_dev[i], Q_dev[i], B[i], flags, p->stream);
+        cudaEvent_t ev;
+        if (rc == kOk && cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) == cudaSuccess) {
+            cudaEventRecord(ev, p->stream);
+            cudaStreamWaitEvent(st, ev, 0);
+            done.push_back(ev);
+        }
+    }
+    for (auto ev : done) cudaEventDestroy(ev);
+    cudaEventDestroy(fork);
+    if (rc == kErrCuda) set_error(kErrCuda, "spectral_group_computeQ: stream fork failed");
+    return rc;
+}
+
 int spectral_plan_set_tuning(spectral_plan *p, int variant, int bg, int zs, int stages,
                              int flush)
 {

@@ -1,0 +1,71 @@
+"""Synthetic initial data for the benchmark and test configurations.
+
+All families are seeded, and all are evaluated on the velocity grid v of
+the plan.  Index order is (i, j, k) -> k + N*(j + N*i), with i the x axis.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def _mesh(v: np.ndarray):
+    return v[:, None, None], v[None, :, None], v[None, None, :]
+
+
+def trapezoid_mass(v: np.ndarray, f: np.ndarray) -> float:
+    """Density with the trapezoid weights of getDensity
+    (momentRoutines.c:58-69), unit mass."""
+    N = v.size
+    wt = np.ones(N)
+    wt[0] = wt[-1] = 0.5
+    dv = v[1] - v[0]
+    w3 = wt[:, None, None] * wt[None, :, None] * wt[None, None, :] * dv ** 3
+    return float((w3 * f.reshape(N, N, N)).sum())
+
+
+def maxwellian(v, rho, u, T):
+    """rho (2 pi T)^(-3/2) exp(-|v-u|^2 / (2T))."""
+    vx, vy, vz = _mesh(v)
+    return rho * (2 * np.pi * T) ** -1.5 * np.exp(
+        -((vx - u[0]) ** 2 + (vy - u[1]) ** 2 + (vz - u[2]) ** 2) / (2 * T))
+
+
+def two_maxwellian_batch(v: np.ndarray, B: int, seed: int) -> np.ndarray:
+    """Discontinuous two-Maxwellian in v_x with +-5% seeded jitter on each
+    parameter: density 1, temperature 1 for v_x < 0; density 1,
+    temperature 2, drift 0.5 for v_x >= 0."""
+    rng = np.random.default_rng(seed)
+    N = v.size
+    vx = v[:, None, None]
+    out = np.empty((B, N ** 3))
+    for b in range(B):
+        j = rng.uniform(-0.05, 0.05, 5) + 1.0
+        m1 = maxwellian(v, 1.0 * j[0], (0, 0, 0), 1.0 * j[1])
+        m2 = maxwellian(v, 1.0 * j[2], (0.5 * j[4], 0, 0), 2.0 * j[3])
+        out[b] = np.where(vx < 0, m1, m2).reshape(-1)
+    return out
+
+
+def maxwellian_mixture_batch(v: np.ndarray, B: int, seed: int) -> np.ndarray:
+    """Mixtures of 2-3 Maxwellians with density U(0.2, 1), drift components
+    U(-1, 1) and temperature U(0.5, 2), normalised to unit mass."""
+    rng = np.random.default_rng(seed)
+    N = v.size
+    out = np.empty((B, N ** 3))
+    for b in range(B):
+        f = np.zeros((N, N, N))
+        for _ in range(int(rng.integers(2, 4))):
+            f += maxwellian(v, rng.uniform(0.2, 1.0), rng.uniform(-1, 1, 3),
+                            rng.uniform(0.5, 2.0))
+        out[b] = (f / trapezoid_mass(v, f)).reshape(-1)
+    return out
+
+
+def bkw(v: np.ndarray, K: float = 0.65) -> np.ndarray:
+    """BKW-type data exp(-|v|^2/(2K)) / (2 (2 pi K)^1.5) ((5K-3)/K +
+    (1-K)/K^2 |v|^2) (initializer.c:123-135 with Temp = 1)."""
+    vx, vy, vz = _mesh(v)
+    v2 = vx ** 2 + vy ** 2 + vz ** 2
+    f = np.exp(-v2 / (2 * K)) / (2.0 * (2 * np.pi * K) ** 1.5) * ((5 * K - 3) / K +
+                                                                (1 - K) * v2 / (K * K))
+    return f.reshape(-1)

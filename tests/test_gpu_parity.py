@@ -278,3 +278,28 @@ def test_bkw8_golden_through_reference_abi(gpu, oracle, ref_api, tmp_path, monke
         col = cols[c]
         assert abs(out[r, col] - want[r, col]) <= 1e-6 * abs(want[r, col]), (r, col)
     assert len(mism) <= 3, mism
+
+
+def test_group_computeQ_matches_per_plan_calls(gpu, oracle):
+    """Uneven batch (config 4 shape): plans of different N and lambda
+    evaluated together on forked streams equal the per-plan calls."""
+    import torch
+    from spectralbte_gb300.workloads import maxwellian_mixture_batch
+    specs = [(8, 5.0, 0.0, 5), (16, 5.0, 1.0, 7), (8, 5.0, 1.0, 3)]
+    plans, fs, Qs, Qr = [], [], [], []
+    for i, (N, L_v, lam, B) in enumerate(specs):
+        v, zeta = gpu.grid_0d(N, L_v)
+        p = gpu.Plan(N, L_v, v, zeta, B)
+        p.generate_weights_iso(lam)
+        f = torch.from_numpy(maxwellian_mixture_batch(v, B, 40 + i)).cuda()
+        plans.append(p)
+        fs.append(f)
+        Qs.append(torch.empty_like(f))
+        Qr.append(torch.empty_like(f))
+    flags = gpu.FP32 | gpu.CONSERVE
+    for p, f, q in zip(plans, fs, Qr):
+        p.computeQ_device(f, q, f.shape[0], flags)
+    gpu.group_computeQ(plans, fs, Qs, flags)
+    torch.cuda.synchronize()
+    for a, b in zip(Qs, Qr):
+        assert torch.equal(a, b)
