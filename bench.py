@@ -279,7 +279,12 @@ def run_ours(args):
     fd = torch.from_numpy(f_host).cuda()
     Qd = torch.empty_like(fd)
     flags = sb.FP32 | sb.CONSERVE
-    tuned = plan.autotune(B, sb.FP32)
+    if args.tuning:
+        variant, bg, zs, stages, flush = (int(x) for x in args.tuning.split(","))
+        plan.set_tuning(bg, stages, flush, variant=variant, zs=zs)
+        tuned = (variant, bg, zs, stages, flush)
+    else:
+        tuned = plan.autotune(B, sb.FP32)
 
     for _ in range(args.warmup):
         plan.computeQ_device(fd, Qd, B, flags)
@@ -344,6 +349,7 @@ def run_ours(args):
     b = Q64.cpu().numpy()
     rel = [float(np.linalg.norm(a[i] - b[i]) / np.linalg.norm(b[i])) for i in range(B64)]
     status = plan.status()
+    fma_rate = sb.fp32_fma_rate()  # measured on this GPU, after the timed region
 
     if rank != 0:
         return 0
@@ -352,7 +358,8 @@ def run_ours(args):
     flops = 10.0 * float(n3) ** 2 * B        # collisions.c:162-163, 10 flops/term
     achieved = flops / conv_avg_s / 1e12
     sm_max = float(peaks.get("sm_max_mhz", 2070.0))
-    fp32_peak = N_SM * FP32_LANES * 2 * sm_max * 1e6 / 1e12
+    fp32_nominal = N_SM * FP32_LANES * 2 * sm_max * 1e6 / 1e12
+    fp32_peak = fma_rate
     w_bytes = 4.0 * float(n3) ** 2           # one FP32 W pass per launch
     hbm_achieved = w_bytes / conv_avg_s / 1e9
 
@@ -389,10 +396,15 @@ def run_ours(args):
             "kernel": "conv_ws_kernel" if tuned[0] == 2 else "conv_f32_kernel",
             "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
             "frac": achieved / fp32_peak,
-            "peak_source": (f"nominal FP32 CUDA-core peak, {N_SM} SMs x {FP32_LANES} lanes x 2 "
-                            f"flop x {sm_max:.0f} MHz ({peak_src} sm_max_mhz); no dense GEMM "
-                            "exists in this operator, so neither the HBM copy nor the bf16 "
+            "peak_source": ("measured: sustained FP32 FMA rate of this GPU from the library's "
+                            "register-FMA probe (spectral_fp32_fma_rate), run in this process; "
+                            "MEASURED_PEAKS.json carries no FP32 figure, and no dense GEMM "
+                            "exists in this operator, so neither its HBM copy nor its bf16 "
                             "tensor peak binds"),
+            "nominal_peak": fp32_nominal,
+            "frac_of_nominal": achieved / fp32_nominal,
+            "nominal_source": (f"{N_SM} SMs x {FP32_LANES} lanes x 2 flop x {sm_max:.0f} MHz "
+                               f"({peak_src} sm_max_mhz)"),
             "algorithmic": f"10*N^6*B flop per launch = {flops:.3e}",
             "launch_ms": conv_avg_s * 1e3,
             "traffic": (NCU_TRAFFIC["bytes"] * (float(n3) ** 2 * B) /
@@ -436,6 +448,8 @@ def main():
     ap.add_argument("--cpu-rows", type=int, default=2048)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="n32", choices=["n32", "uneven"])
+    ap.add_argument("--tuning", default="",
+                    help="variant,bg,zs,stages,flush of the FP32 convolution (default: autotune)")
     args = ap.parse_args()
     if args.workload == "uneven" and args.impl != "reference":
         return run_uneven(args)

@@ -251,6 +251,11 @@ int spectral_fft3d_noalloc(int N, double L_v, const double *v,
                            const double *zeta, const double *in_dev,
                            double *out_dev, int B, int invert, void *stream);
 
+/* Roofline calibration: the FP32 FMA rate (TFLOP/s, FMA = 2 flop) that the
+   current GPU sustains on independent register FMA chains; the FP32
+   convolution's fraction of peak is reported against it. */
+int spectral_fp32_fma_rate(double *tflops, void *stream);
+
 /* Number of kernels the library launched since load (monotonic). */
 long long spectral_kernel_launches(void);
 

@@ -140,6 +140,7 @@ def lib() -> C.CDLL:
         "spectral_1d_advect": (i, [v, v, v, v]),
         "spectral_graph_capture": (i, [v, i, v, i, d, d, i, i]),
         "spectral_graph_launch": (i, [v, v]),
+        "spectral_fp32_fma_rate": (i, [_dp, v]),
         "spectral_group_computeQ": (i, [C.POINTER(C.c_void_p), i, C.POINTER(C.c_void_p),
                                         C.POINTER(C.c_void_p), C.POINTER(C.c_int), i, v]),
         "spectral_plan_conv_time": (i, [v, _dp, C.POINTER(C.c_int)]),
@@ -442,6 +443,13 @@ def group_computeQ(plans, fs, Qs, flags: int = FP32 | CONSERVE, stream: int = 0)
     bs = (C.c_int * n)(*[int(f.shape[0]) for f in fs])
     _check(lib().spectral_group_computeQ(ph, n, fp, qp, bs, flags, _stream(stream)),
            "spectral_group_computeQ")
+
+
+def fp32_fma_rate() -> float:
+    """Sustained FP32 FMA rate of the current GPU in TFLOP/s (probe kernel)."""
+    out = C.c_double()
+    _check(lib().spectral_fp32_fma_rate(C.byref(out), _stream(0)), "spectral_fp32_fma_rate")
+    return out.value
 
 
 def kernel_launches() -> int:

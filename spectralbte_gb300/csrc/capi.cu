@@ -255,12 +255,14 @@ static void solve_cct_host(const ConsParams &cp, double *b, int n)
 // ------------------------------------------------------------- weights ---
 struct WeightsDev {
     int N = 0;
-    double *w64 = nullptr;  // row-major [N^3][N^3]
-    float *w32 = nullptr;   // tiled FP32 (built on first FP32 use)
+    double *w64 = nullptr;   // row-major [N^3][N^3]
+    float *w32 = nullptr;    // tiled FP32 (built on first FP32 use)
+    float2 *w32x2 = nullptr; // tiled (w, w) pairs (built on first variant-4 use)
     void release()
     {
         dfree(w64);
         dfree(w32);
+        dfree(w32x2);
         N = 0;
     }
 };
@@ -276,6 +278,7 @@ static int upload_weights(WeightsDev &wd, int N, const double *flat,
         wd.N = N;
     }
     dfree(wd.w32);
+    dfree(wd.w32x2);
     if (flat) {
         SBTE_CUDA(cudaMemcpyAsync(wd.w64, flat, sizeof(double) * n3 * n3,
                                   flat_on_device ? cudaMemcpyDeviceToDevice
@@ -316,6 +319,16 @@ static int ensure_w32(WeightsDev &wd, cudaStream_t st)
     return kOk;
 }
 
+static int ensure_w32x2(WeightsDev &wd, cudaStream_t st)
+{
+    if (wd.w32x2) return kOk;
+    const long long n3 = (long long)wd.N * wd.N * wd.N;
+    SBTE_TRY(dalloc(&wd.w32x2, (size_t)(n3 * n3)));
+    SBTE_LAUNCH(weights_to_tiled_f32x2(wd.w64, wd.w32x2, wd.N, st), 1);
+    SBTE_CUDA(cudaStreamSynchronize(st));
+    return kOk;
+}
+
 struct IsoWeightSpec {
     int N = 0;
     double L_v = 0, lambda = 0, d_i = 2, d_j = 2, m_i = 1, m_j = 1;
@@ -334,6 +347,7 @@ static int generate_iso_device(WeightsDev &wd, const IsoWeightSpec &s,
         wd.N = N;
     }
     dfree(wd.w32);
+    dfree(wd.w32x2);
     WeightParams wp;
     wp.N = N;
     wp.L_v = s.L_v;
@@ -413,6 +427,8 @@ struct spectral_plan_s {
     // FP32 scratch: capacity cap32 instances (padded to 128)
     int cap32 = 0;
     float2 *c32[4] = {};   // P, R, S, T (bg-interleaved)
+    int cap32x4 = 0;
+    float4 *c32x4[4] = {}; // P, R, S, T in the expanded G4 / F4 forms
     double2 *qacc = nullptr;
     float2 *tmp32 = nullptr;
     double *r32[2] = {};   // M, g
@@ -447,6 +463,7 @@ struct spectral_plan_s {
         dfree(tmp64);
         for (auto &p : r64) dfree(p);
         for (auto &p : c32) dfree(p);
+        for (auto &p : c32x4) dfree(p);
         dfree(qacc); dfree(tmp32);
         for (auto &p : r32) dfree(p);
         dfree(sQ); dfree(sf1); dfree(d_fh); dfree(d_Qh);
@@ -538,6 +555,22 @@ static int ensure32(spectral_plan_s *p, int B)
     for (auto &q : p->r32) SBTE_TRY(dalloc(&q, (size_t)B * p->n3));
     SBTE_CUDA(cudaDeviceSynchronize());
     p->cap32 = padB;
+    return kOk;
+}
+
+static int ensure32x4(spectral_plan_s *p, int B)
+{
+    const int padB = (B + 127) / 128 * 128;
+    if (padB <= p->cap32x4) return kOk;
+    for (auto &q : p->c32x4) dfree(q);
+    p->cap32x4 = 0;
+    const size_t n = (size_t)padB * p->n3;
+    for (auto &q : p->c32x4) {
+        SBTE_TRY(dalloc(&q, n));
+        SBTE_CUDA(cudaMemset(q, 0, n * sizeof(float4)));
+    }
+    SBTE_CUDA(cudaDeviceSynchronize());
+    p->cap32x4 = padB;
     return kOk;
 }
 
@@ -662,6 +695,38 @@ static int q_fp32(spectral_plan_s *p, const double *fdev, double *Qdev, int B,
     const int groups = (B + bg - 1) / bg;
     const float pf_f = (float)p->pf_fwd, pf_i = (float)p->pf_inv;
     float2 *P = p->c32[0], *R = p->c32[1], *S = p->c32[2];
+    if (cfg.variant == 4) {
+        SBTE_TRY(ensure32x4(p, B));
+        SBTE_TRY(ensure_w32x2(p->W, st));
+        float4 *P4 = p->c32x4[0], *R4 = p->c32x4[1], *S4 = p->c32x4[2], *T4 = p->c32x4[3];
+        const double *gsrc = fdev;
+        if (maxpreserve) {
+            double *M = p->r32[0], *g = p->r32[1];
+            SBTE_LAUNCH(maxwellian_split(fdev, M, g, nullptr, B, N, p->d_v, p->mom_mass,
+                                         p->mom_KB, nullptr, st), 1);
+            SBTE_LAUNCH(dft3_f32(M, DftIn::kRealF64, 1, p->tmp32, S4, DftOut::kG4, bg,
+                                 p->Dfwd32, pf_f, N, B, st), 2);
+            gsrc = g;
+        }
+        // ghat in the G4 form (P) and, for the two-pair form, the F4 form (T);
+        // fhat in the F4 form (R)
+        SBTE_LAUNCH(dft3_f32(gsrc, DftIn::kRealF64, 1, p->tmp32, P4, DftOut::kG4, bg,
+                             p->Dfwd32, pf_f, N, B, st), 2);
+        SBTE_LAUNCH(dft3_f32(fdev, DftIn::kRealF64, 1, p->tmp32, R4, DftOut::kF4, bg,
+                             p->Dfwd32, pf_f, N, B, st), 2);
+        if (maxpreserve)
+            SBTE_LAUNCH(dft3_f32(gsrc, DftIn::kRealF64, 1, p->tmp32, T4, DftOut::kF4, bg,
+                                 p->Dfwd32, pf_f, N, B, st), 2);
+        auto *ev = prof_slot(p);
+        if (ev) cudaEventRecord(ev->first, st);
+        SBTE_LAUNCH(conv_x4(p->W.w32x2, P4, R4, maxpreserve ? S4 : nullptr,
+                            maxpreserve ? T4 : nullptr, p->qacc, N, B, cfg.bg, cfg.zs,
+                            cfg.stages, cfg.flush, p->d_status, st), 1);
+        if (ev) cudaEventRecord(ev->second, st);
+        SBTE_LAUNCH(dft3_f32(p->qacc, DftIn::kComplexF64, bg, p->tmp32, Qdev, DftOut::kRealF64,
+                             1, p->Dinv32, pf_i, N, B, st), 2);
+        return kOk;
+    }
     if (!maxpreserve) {
         SBTE_LAUNCH(dft3_f32(fdev, DftIn::kRealF64, 1, p->tmp32, P, DftOut::kComplexF32, bg,
                              p->Dfwd32, pf_f, N, B, st), 2);
@@ -975,6 +1040,10 @@ int spectral_graph_capture(spectral_plan *p, int kind, double *f_dev, int B, dou
     if (flags & SPECTRAL_FP32) {
         SBTE_TRY(ensure32(p, nb));
         SBTE_TRY(ensure_w32(p->W, p->stream));
+        if (p->tune.variant == 4) {
+            SBTE_TRY(ensure32x4(p, nb));
+            SBTE_TRY(ensure_w32x2(p->W, p->stream));
+        }
     } else {
         SBTE_TRY(ensure64(p, nb));
     }
@@ -1078,7 +1147,8 @@ int spectral_plan_autotune(spectral_plan *p, int B, int flags, int *chosen)
     const ConvF32Config cands[] = {
         {32, 2, 16},       {64, 2, 16},       {64, 3, 16},       {128, 2, 16},
         {32, 2, 16, 2, 8}, {64, 2, 16, 2, 8}, {32, 3, 16, 3, 8}, {64, 2, 16, 3, 8},
-        {64, 3, 16, 3, 8}, {64, 2, 16, 3, 16}, {64, 3, 16, 3, 16}};
+        {64, 3, 16, 3, 8}, {64, 2, 16, 3, 16}, {64, 3, 16, 3, 16},
+        {32, 2, 16, 4, 8}, {64, 2, 16, 4, 8}, {32, 3, 16, 4, 8}};
     cudaEvent_t e0, e1;
     SBTE_CUDA(cudaEventCreate(&e0));
     SBTE_CUDA(cudaEventCreate(&e1));
@@ -1093,10 +1163,18 @@ int spectral_plan_autotune(spectral_plan *p, int B, int flags, int *chosen)
                 cudaMemsetAsync(p->qacc, 0,
                                 sizeof(double2) * (size_t)((B + c.bg - 1) / c.bg) * c.bg * p->n3,
                                 p->stream);
+            if (c.variant == 4) {
+                SBTE_TRY(ensure32x4(p, B));
+                SBTE_TRY(ensure_w32x2(p->W, p->stream));
+            }
             cudaEventRecord(e0, p->stream);
-            cudaError_t e = conv_f32_batched(p->W.w32, P, R, two ? S : nullptr,
-                                             two ? P : nullptr, p->qacc, p->N, B, c,
-                                             p->d_status, p->stream);
+            cudaError_t e =
+                c.variant == 4
+                    ? conv_x4(p->W.w32x2, p->c32x4[0], p->c32x4[1], two ? p->c32x4[2] : nullptr,
+                              two ? p->c32x4[3] : nullptr, p->qacc, p->N, B, c.bg, c.zs,
+                              c.stages, c.flush, p->d_status, p->stream)
+                    : conv_f32_batched(p->W.w32, P, R, two ? S : nullptr, two ? P : nullptr,
+                                       p->qacc, p->N, B, c, p->d_status, p->stream);
             cudaEventRecord(e1, p->stream);
             if (e != cudaSuccess) {
                 cudaEventDestroy(e0);

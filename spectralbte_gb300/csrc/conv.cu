@@ -331,7 +331,30 @@ __global__ void tile_weights_kernel(const double *__restrict__ W,
     }
 }
 
+__global__ void tile_weights_x2_kernel(const double *__restrict__ W,
+                                       float2 *__restrict__ W2, int N)
+{
+    // W2[zrow][xrow][zz][xz] = ((float) w, (float) w)
+    const long long nn = (long long)N * N;
+    const long long n3 = nn * N;
+    const long long total = n3 * n3;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const long long row = t / n3, col = t % n3;
+        const long long zrow = row / N, zz = row % N;
+        const long long xrow = col / N, xz = col % N;
+        const float w = (float)W[t];
+        W2[((zrow * nn + xrow) * N + zz) * N + xz] = make_float2(w, w);
+    }
+}
+
 }  // namespace
+
+cudaError_t weights_to_tiled_f32x2(const double *W, float2 *W2blk, int N, cudaStream_t st)
+{
+    tile_weights_x2_kernel<<<152 * 8, 256, 0, st>>>(W, W2blk, N);
+    return cudaGetLastError();
+}
 
 cudaError_t conv_f64(const double *W, const double2 *P, const double2 *R,
                      const double2 *S, const double2 *T, double2 *qhat, int N,
@@ -352,6 +375,7 @@ bool conv_f32_supported(int N, ConvF32Config cfg, bool two_pairs)
 {
     if (cfg.variant == 2 || cfg.variant == 3)
         return conv_ws_supported(N, cfg.bg, cfg.zs, cfg.variant == 2, cfg.stages, two_pairs);
+    if (cfg.variant == 4) return conv_x4_supported(N, cfg.bg, cfg.zs, cfg.stages, two_pairs);
     if (cfg.variant != 1) return false;
     if (!(N == 8 || N == 16 || N == 24 || N == 32)) return false;
     const bool ok = (cfg.bg == 32 && (cfg.stages == 2 || cfg.stages == 3)) ||

@@ -145,13 +145,20 @@ conv_ws_kernel(const float *__restrict__ Wblk, const float2 *__restrict__ P,
     bool first_flush = true;
     int since = 0;
 
+    // The first flush stores; later ones add with fire-and-forget reductions
+    // (red.global.add.f64), so the consumer never waits on a global load.
+    // Each accumulator has a single writer, which adds in program order, so
+    // the sum is deterministic.
     auto do_flush = [&]() {
 #pragma unroll
         for (int i = 0; i < ZS; i++) {
-            double2 q = first_flush ? make_double2(0.0, 0.0) : qrow[(long long)i * BG];
-            q.x += (double)acc[i].x;
-            q.y += (double)acc[i].y;
-            qrow[(long long)i * BG] = q;
+            double2 *q = qrow + (long long)i * BG;
+            if (first_flush) {
+                *q = make_double2((double)acc[i].x, (double)acc[i].y);
+            } else {
+                atomicAdd(&q->x, (double)acc[i].x);
+                atomicAdd(&q->y, (double)acc[i].y);
+            }
             acc[i] = f2(0.f, 0.f);
         }
         first_flush = false;
@@ -331,6 +338,253 @@ cudaError_t conv_ws(const float *Wblk, const float2 *P, const float2 *R, const f
                                                                   flush, status, st);
     SBTE_WS_SHAPES(SBTE_WS_L)
 #undef SBTE_WS_L
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace sbte
+
+// ======================================================================
+// Variant 4: packed FP32x2 math with expanded operands.  The FFT writes
+// ghat as (g.x, g.x, -g.y, g.y) and fhat as (f.x, f.y, f.y, f.x), and W is
+// tiled as (w, w) pairs.  Every 128-bit shared load then hands the math two
+// ready-made 64-bit operand pairs, so one term costs three f32x2
+// instructions and no register moves.
+// ======================================================================
+namespace sbte {
+namespace {
+
+template <int N, int BG, int ZS, bool TWO, int ST>
+struct X4Layout {
+    static constexpr int kNeed = N + ZS + 6;          // window entries incl. wrap
+    static constexpr int kWBytes = N * N * 8;         // (w, w) pairs
+    static constexpr int kRowBytes = N * BG * 16;     // one G4 row
+    static constexpr int kWinBytes = kNeed * BG * 16; // F4 row + wrapped head
+    static constexpr int kStageBytes =
+        kWBytes + kRowBytes + kWinBytes + (TWO ? kRowBytes + kWinBytes : 0);
+    static constexpr int kConsumers = BG * (N / ZS);
+    static constexpr int kThreads = kConsumers + 32;
+};
+
+__device__ __forceinline__ float2 lo2(float4 q) { return make_float2(q.x, q.y); }
+__device__ __forceinline__ float2 hi2(float4 q) { return make_float2(q.z, q.w); }
+
+template <int N, int BG, int ZS, bool TWO, int ST>
+__global__ void __launch_bounds__(X4Layout<N, BG, ZS, TWO, ST>::kThreads)
+conv_x4_kernel(const float2 *__restrict__ W2blk, const float4 *__restrict__ P,
+               const float4 *__restrict__ R, const float4 *__restrict__ S,
+               const float4 *__restrict__ T, double2 *__restrict__ qacc, int flush,
+               unsigned int *__restrict__ status)
+{
+    using L = X4Layout<N, BG, ZS, TWO, ST>;
+    constexpr int NN = N * N;
+    constexpr int H = N / 2;
+    constexpr int NCW = L::kConsumers / 32;
+    constexpr long long N3 = (long long)NN * N;
+    static_assert(N % 8 == 0 && N % ZS == 0 && BG % 32 == 0, "shape");
+    static_assert(L::kNeed <= 3 * N, "window fits in three row copies");
+
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ uint64_t full[ST];
+    __shared__ uint64_t empty[ST];
+
+    const int tid = threadIdx.x;
+    const int warp = tid >> 5;
+    const int zrow = blockIdx.x;
+    const int zx = zrow / N, zy = zrow % N;
+    const long long grp = blockIdx.y;
+
+    if (tid == 0) {
+        for (int s = 0; s < ST; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], NCW);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+
+    if (warp == NCW) {
+        if ((tid & 31) != 0) return;
+        const float2 *Wbase = W2blk + (long long)zrow * NN * NN;
+        const float4 *Pg = P + grp * N3 * BG;
+        const float4 *Rg = R + grp * N3 * BG;
+        const float4 *Sg = TWO ? S + grp * N3 * BG : nullptr;
+        const float4 *Tg = TWO ? T + grp * N3 * BG : nullptr;
+        for (int it = 0; it < NN; it++) {
+            const int s = it % ST;
+            if (it >= ST) {
+                if (!mbar_wait_bounded(&empty[s], (uint32_t)(((it / ST) - 1) & 1))) {
+                    atomicOr(status, kStatusTimeout);
+                    return;
+                }
+            }
+            unsigned char *d = smem + s * L::kStageBytes;
+            const int xx = it / N, xy = it % N;
+            const int fx = (zx + H - xx < 0) ? zx + H - xx + N
+                           : (zx + H - xx > N - 1 ? zx + H - xx - N : zx + H - xx);
+            const int fy = (zy + H - xy < 0) ? zy + H - xy + N
+                           : (zy + H - xy > N - 1 ? zy + H - xy - N : zy + H - xy);
+            const long long prow = (long long)it * N * BG;
+            const long long rrow = ((long long)fx * N + fy) * N * BG;
+            mbar_expect_tx(&full[s], L::kStageBytes);
+            bulk_g2s(d, Wbase + (long long)it * NN, L::kWBytes, &full[s]);
+            d += L::kWBytes;
+            bulk_g2s(d, Pg + prow, L::kRowBytes, &full[s]);
+            d += L::kRowBytes;
+            for (int done = 0; done < L::kNeed; done += N) {
+                const int cnt = (L::kNeed - done < N) ? L::kNeed - done : N;
+                bulk_g2s(d + (size_t)done * BG * 16, Rg + rrow, cnt * BG * 16, &full[s]);
+            }
+            d += L::kWinBytes;
+            if (TWO) {
+                bulk_g2s(d, Sg + prow, L::kRowBytes, &full[s]);
+                d += L::kRowBytes;
+                for (int done = 0; done < L::kNeed; done += N) {
+                    const int cnt = (L::kNeed - done < N) ? L::kNeed - done : N;
+                    bulk_g2s(d + (size_t)done * BG * 16, Tg + rrow, cnt * BG * 16, &full[s]);
+                }
+            }
+        }
+        return;
+    }
+
+    const int b = tid % BG;
+    const int zq = tid / BG;
+    const int z0 = zq * ZS;
+    float2 acc[ZS];
+#pragma unroll
+    for (int i = 0; i < ZS; i++) acc[i] = make_float2(0.f, 0.f);
+    double2 *qrow = qacc + grp * N3 * BG + ((long long)zrow * N + z0) * BG + b;
+    bool first_flush = true;
+    int since = 0;
+    auto do_flush = [&]() {
+#pragma unroll
+        for (int i = 0; i < ZS; i++) {
+            double2 q = first_flush ? make_double2(0.0, 0.0) : qrow[(long long)i * BG];
+            q.x += (double)acc[i].x;
+            q.y += (double)acc[i].y;
+            qrow[(long long)i * BG] = q;
+            acc[i] = make_float2(0.f, 0.f);
+        }
+        first_flush = false;
+    };
+
+    for (int it = 0; it < NN; it++) {
+        const int s = it % ST;
+        if (!mbar_wait_bounded(&full[s], (uint32_t)((it / ST) & 1))) {
+            atomicOr(status, kStatusTimeout);
+            (void)mbar_wait_bounded(&full[s], (uint32_t)((it / ST) & 1));
+            return;
+        }
+        const unsigned char *base = smem + s * L::kStageBytes;
+        const float4 *W4 = reinterpret_cast<const float4 *>(base);
+        const float4 *G4 = reinterpret_cast<const float4 *>(base + L::kWBytes);
+        const float4 *F4 = reinterpret_cast<const float4 *>(base + L::kWBytes + L::kRowBytes);
+        const float4 *S4 = reinterpret_cast<const float4 *>(base + L::kWBytes + L::kRowBytes +
+                                                            L::kWinBytes);
+        const float4 *T4 = reinterpret_cast<const float4 *>(base + L::kWBytes +
+                                                            2 * L::kRowBytes + L::kWinBytes);
+#pragma unroll
+        for (int c = 0; c < N / 8; c++) {
+            float4 gq[8];
+            float4 sq[TWO ? 8 : 1];
+#pragma unroll
+            for (int e = 0; e < 8; e++) {
+                gq[e] = G4[(8 * c + e) * BG + b];
+                if (TWO) sq[e] = S4[(8 * c + e) * BG + b];
+            }
+            int start = z0 + H - 8 * c - 7;
+            start = start < 0 ? start + N : (start >= N ? start - N : start);
+            float4 fq[ZS + 7];
+            float4 tq[TWO ? ZS + 7 : 1];
+#pragma unroll
+            for (int d = 0; d < ZS + 7; d++) {
+                fq[d] = F4[(start + d) * BG + b];
+                if (TWO) tq[d] = T4[(start + d) * BG + b];
+            }
+#pragma unroll
+            for (int zl = 0; zl < ZS; zl++) {
+                // 8 (w, w) pairs of row z0+zl, columns 8c..8c+7
+                float4 wq[4];
+#pragma unroll
+                for (int m = 0; m < 4; m++) wq[m] = W4[((z0 + zl) * N + 8 * c) / 2 + m];
+#pragma unroll
+                for (int e = 0; e < 8; e++) {
+                    const float4 f = fq[zl - e + 7];
+                    float2 t = __fmul2_rn(lo2(gq[e]), lo2(f));
+                    t = __ffma2_rn(hi2(gq[e]), hi2(f), t);
+                    if (TWO) {
+                        const float4 tt = tq[zl - e + 7];
+                        t = __ffma2_rn(lo2(sq[e]), lo2(tt), t);
+                        t = __ffma2_rn(hi2(sq[e]), hi2(tt), t);
+                    }
+                    const float2 ww = (e & 1) ? hi2(wq[e >> 1]) : lo2(wq[e >> 1]);
+                    acc[zl] = __ffma2_rn(ww, t, acc[zl]);
+                }
+            }
+        }
+        __syncwarp();
+        if ((tid & 31) == 0) mbar_arrive(&empty[s]);
+        if (++since == flush) {
+            do_flush();
+            since = 0;
+        }
+    }
+    if (since || first_flush) do_flush();
+}
+
+template <int N, int BG, int ZS, bool TWO, int ST>
+cudaError_t launch_x4(const float2 *W2, const float4 *P, const float4 *R, const float4 *S,
+                      const float4 *T, double2 *qacc, int B, int flush, unsigned *status,
+                      cudaStream_t st)
+{
+    using L = X4Layout<N, BG, ZS, TWO, ST>;
+    const size_t smem = (size_t)ST * L::kStageBytes;
+    auto kern = conv_x4_kernel<N, BG, ZS, TWO, ST>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    dim3 grid(N * N, (B + BG - 1) / BG);
+    kern<<<grid, L::kThreads, smem, st>>>(W2, P, R, S, T, qacc, flush, status);
+    return cudaGetLastError();
+}
+
+template <int N, int BG, int ZS, bool TWO, int ST>
+size_t x4_smem()
+{
+    return (size_t)ST * X4Layout<N, BG, ZS, TWO, ST>::kStageBytes;
+}
+
+}  // namespace
+
+#define SBTE_X4_SHAPES(X)                                                     \
+    X(8, 32, 8, 2) X(16, 32, 8, 2) X(24, 32, 8, 2) X(32, 32, 8, 2)             \
+    X(32, 64, 8, 2) X(32, 32, 8, 3)
+
+bool conv_x4_supported(int N, int bg, int zs, int stages, bool two)
+{
+#define SBTE_X4_Q(NN, BGV, ZSV, STV)                                                  \
+    if (N == NN && bg == BGV && zs == ZSV && stages == STV)                           \
+        return (two ? x4_smem<NN, BGV, ZSV, true, STV>()                              \
+                    : x4_smem<NN, BGV, ZSV, false, STV>()) <= 227 * 1024;
+    SBTE_X4_SHAPES(SBTE_X4_Q)
+#undef SBTE_X4_Q
+    return false;
+}
+
+cudaError_t conv_x4(const float2 *W2blk, const float4 *P, const float4 *R, const float4 *S,
+                    const float4 *T, double2 *qacc, int N, int B, int bg, int zs, int stages,
+                    int flush, unsigned int *status, cudaStream_t st)
+{
+    const bool two = (S != nullptr);
+    if (!conv_x4_supported(N, bg, zs, stages, two) || B < 1) return cudaErrorInvalidValue;
+#define SBTE_X4_L(NN, BGV, ZSV, STV)                                                      \
+    if (N == NN && bg == BGV && zs == ZSV && stages == STV)                               \
+        return two ? launch_x4<NN, BGV, ZSV, true, STV>(W2blk, P, R, S, T, qacc, B, flush,  \
+                                                        status, st)                        \
+                   : launch_x4<NN, BGV, ZSV, false, STV>(W2blk, P, R, S, T, qacc, B, flush, \
+                                                         status, st);
+    SBTE_X4_SHAPES(SBTE_X4_L)
+#undef SBTE_X4_L
     return cudaErrorInvalidValue;
 }
 

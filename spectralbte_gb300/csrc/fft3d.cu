@@ -64,6 +64,13 @@ __device__ __forceinline__ void store_out(void *p, DftOut kind, long long i,
     case DftOut::kRealF32:
         static_cast<float *>(p)[i] = (float)v.x;
         break;
+    case DftOut::kF4:
+        static_cast<float4 *>(p)[i] = make_float4((float)v.x, (float)v.y, (float)v.y, (float)v.x);
+        break;
+    case DftOut::kG4:
+        static_cast<float4 *>(p)[i] =
+            make_float4((float)v.x, (float)v.x, -(float)v.y, (float)v.y);
+        break;
     }
 }
 

@@ -20,7 +20,10 @@ namespace sbte {
 // bg = 1 is the plain instance-major layout [b][pos].
 
 enum class DftIn { kRealF64, kComplexF64, kComplexF32 };
-enum class DftOut { kComplexF64, kComplexF32, kRealF64, kRealF32 };
+// kF4 / kG4: FP32 complex z written as the packed operand quadruples of
+// the expanded-operand convolution, (z.x, z.y, z.y, z.x) and
+// (z.x, z.x, -z.y, z.y).
+enum class DftOut { kComplexF64, kComplexF32, kRealF64, kRealF32, kF4, kG4 };
 
 // Forward or inverse 3D DFT of B instances, FP64 arithmetic.
 // in: real or complex FP64; tmp: B*N^3 double2 scratch; out: complex FP64
@@ -58,7 +61,8 @@ struct ConvF32Config {
     int stages;       // copy pipeline depth (variant 1: 2 or 3)
     int flush;        // xi-rows between FP64 flushes of the FP32 partial sums
     int variant = 1;  // 1: block-barrier kernel; 2: warp-specialised with
-                      // packed FP32x2 math; 3: warp-specialised, scalar math
+                      // packed FP32x2 math; 3: warp-specialised, scalar math;
+                      // 4: warp-specialised, FP32x2 on expanded operands
     int zs = 0;       // variants 2, 3: zeta_z values per thread (8 or 16)
 };
 cudaError_t conv_f32_batched(const float *Wblk, const float2 *P,
@@ -77,6 +81,17 @@ cudaError_t conv_ws(const float *Wblk, const float2 *P, const float2 *R,
                     const float2 *S, const float2 *T, double2 *qacc, int N, int B,
                     int bg, int zs, bool packed, int stages, int flush,
                     unsigned int *status, cudaStream_t st);
+
+// The expanded-operand FP32x2 convolution (variant 4): W tiled with every
+// value as a (w, w) pair; P, S in the G4 form and R, T in the F4 form
+// (DftOut), all bg-interleaved.
+bool conv_x4_supported(int N, int bg, int zs, int stages, bool two_pairs);
+cudaError_t conv_x4(const float2 *W2blk, const float4 *P, const float4 *R,
+                    const float4 *S, const float4 *T, double2 *qacc, int N, int B,
+                    int bg, int zs, int stages, int flush, unsigned int *status,
+                    cudaStream_t st);
+cudaError_t weights_to_tiled_f32x2(const double *W, float2 *W2blk, int N,
+                                   cudaStream_t st);
 
 // Re-layout of FP64 row-major W into the FP32 tiled layout.
 cudaError_t weights_to_tiled_f32(const double *W, float *Wblk, int N,

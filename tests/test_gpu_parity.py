@@ -181,9 +181,9 @@ def test_plan_fp32_matches_fp64(gpu, oracle, N, L_v, lam, B, mp):
     plan.computeQ_device(fd, Q64, B, gpu.FP64 | gpu.CONSERVE | extra)
     errs = []
     shapes = [(1, 32, 0, 2), (1, 64, 0, 3), (1, 128, 0, 2), (2, 32, 8, 2), (3, 32, 8, 3),
-              (3, 64, 8, 3)]
+              (3, 64, 8, 3), (4, 32, 8, 2)]
     if N == 32:
-        shapes += [(2, 64, 8, 2), (3, 64, 16, 2)]
+        shapes += [(2, 64, 8, 2), (3, 64, 16, 2), (4, 64, 8, 2)]
     for variant, bg, zs, stages in shapes:
         plan.set_tuning(bg, stages, 16, variant=variant, zs=zs)
         plan.computeQ_device(fd, Q32, B, gpu.FP32 | gpu.CONSERVE | extra)
