@@ -124,6 +124,7 @@ double gHat3(double ki1, double ki2, double ki3, double zeta1, double zeta2,
 #define SPECTRAL_FP32 1        /* batched FP32 convolution + FFTs */
 #define SPECTRAL_MAXPRESERVE 2 /* ComputeQ_maxPreserve semantics */
 #define SPECTRAL_CONSERVE 4    /* apply conserveAllMoments (FP64) */
+#define SPECTRAL_LEARNED 8     /* learned operator + spot check (see below) */
 
 int spectral_last_error(void);
 const char *spectral_last_error_message(void);
@@ -250,6 +251,54 @@ int spectral_plan_sync(spectral_plan *plan);
 int spectral_fft3d_noalloc(int N, double L_v, const double *v,
                            const double *zeta, const double *in_dev,
                            double *out_dev, int B, int invert, void *stream);
+
+/* ---- Learned collision operator.  No counterpart in the reference.
+   A Fourier neural operator maps f (one instance on the N^3 grid) to Q(f):
+   lift to `width` channels, `layers` spectral layers on the lowest
+   `modes`^3 Fourier modes (weights shared by modes of equal |m|^2) plus a
+   pointwise channel mix and GELU, then a two-layer pointwise projection
+   with `hidden` channels.  f is scaled by its maximum s and the output by
+   s^2 times the output scale (Q is bilinear in f).  All GEMMs run on BF16
+   tensor cores with FP32 accumulation; parameters are FP32.  Shapes:
+   N 4..32, width 8..64 (multiple of 8), even modes <= min(16, N), layers
+   1..8, hidden 16..128 (multiple of 16). */
+typedef struct spectral_fno_s spectral_fno;
+int spectral_fno_create(spectral_fno **net, int N, int width, int modes,
+                        int layers, int hidden, unsigned long long seed);
+int spectral_fno_destroy(spectral_fno *net);
+long long spectral_fno_num_params(spectral_fno *net);
+int spectral_fno_num_classes(spectral_fno *net);
+/* Flat FP32 parameter vector: P, bP, then per layer W (width x width), b,
+   R (classes x width x width), then Q1 (hidden x width), c1, q2, c2.
+   set_params also resets the optimiser state. */
+int spectral_fno_get_params(spectral_fno *net, float *host);
+int spectral_fno_set_params(spectral_fno *net, const float *host);
+int spectral_fno_set_output_scale(spectral_fno *net, float sigma);
+float spectral_fno_output_scale(spectral_fno *net);
+/* Network output Q[b][pos] (FP64 device) for f[b][pos], no projection. */
+int spectral_fno_predict(spectral_fno *net, const double *f_dev, double *Q_dev,
+                         int B, void *stream);
+/* Mean over instances of |y - Q~|^2 / |Q~|^2 (Q~ = Q / (s^2 sigma)) and its
+   gradient (host, nparams floats) for FP32 device data f, Q [B][N^3]. */
+int spectral_fno_loss_grad(spectral_fno *net, const float *f_dev,
+                           const float *Q_dev, int B, double *loss_out,
+                           float *grad_host);
+/* One Adam step (beta 0.9 / 0.999) on that loss; loss_out may be NULL
+   (no host synchronisation then). */
+int spectral_fno_train_step(spectral_fno *net, const float *f_dev,
+                            const float *Q_dev, int B, float lr,
+                            double *loss_out, void *stream);
+/* Attach a network to a plan for computeQ with SPECTRAL_LEARNED: the
+   network output is projected by the FP64 conservation step; every
+   check_every-th call one instance is recomputed with the plain FP32
+   operator, and a rel-L2 distance above tol switches to the plain operator
+   (the other flags) until a later check passes.  check_every = 0 never
+   checks.  net = NULL detaches. */
+int spectral_plan_set_learned(spectral_plan *plan, spectral_fno *net,
+                              double tol, int check_every);
+int spectral_plan_learned_stats(spectral_plan *plan, long long *calls,
+                                long long *checks, long long *fallbacks,
+                                double *last_err);
 
 /* Roofline calibration: the FP32 FMA rate (TFLOP/s, FMA = 2 flop) that the
    current GPU sustains on independent register FMA chains; the FP32

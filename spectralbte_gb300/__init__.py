@@ -30,6 +30,7 @@ FP64 = 0
 FP32 = 1
 MAXPRESERVE = 2
 CONSERVE = 4
+LEARNED = 8
 
 _dp = C.POINTER(C.c_double)
 _LIB: Optional[C.CDLL] = None
@@ -144,6 +145,21 @@ def lib() -> C.CDLL:
         "spectral_group_computeQ": (i, [C.POINTER(C.c_void_p), i, C.POINTER(C.c_void_p),
                                         C.POINTER(C.c_void_p), C.POINTER(C.c_int), i, v]),
         "spectral_plan_conv_time": (i, [v, _dp, C.POINTER(C.c_int)]),
+        # learned operator
+        "spectral_fno_create": (i, [pp, i, i, i, i, i, C.c_ulonglong]),
+        "spectral_fno_destroy": (i, [v]),
+        "spectral_fno_num_params": (C.c_longlong, [v]),
+        "spectral_fno_num_classes": (i, [v]),
+        "spectral_fno_get_params": (i, [v, C.POINTER(C.c_float)]),
+        "spectral_fno_set_params": (i, [v, C.POINTER(C.c_float)]),
+        "spectral_fno_set_output_scale": (i, [v, C.c_float]),
+        "spectral_fno_output_scale": (C.c_float, [v]),
+        "spectral_fno_predict": (i, [v, v, v, i, v]),
+        "spectral_fno_loss_grad": (i, [v, v, v, i, _dp, C.POINTER(C.c_float)]),
+        "spectral_fno_train_step": (i, [v, v, v, i, C.c_float, _dp, v]),
+        "spectral_plan_set_learned": (i, [v, v, d, i]),
+        "spectral_plan_learned_stats": (i, [v, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong),
+                                            C.POINTER(C.c_longlong), _dp]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(L, name)
@@ -280,15 +296,15 @@ class ReferenceAPI:
 
 
 # --------------------------------------------------------------------------
-def _ptr(x) -> int:
+def _ptr(x, itemsize: int = 8) -> int:
     """Device pointer of a torch CUDA tensor, or an int address."""
     if isinstance(x, int):
         return x
     if hasattr(x, "data_ptr"):
         if not x.is_cuda:
             raise SpectralError("expected a CUDA tensor")
-        if not x.is_contiguous() or x.dtype.itemsize != 8:
-            raise SpectralError("expected a contiguous float64 tensor")
+        if not x.is_contiguous() or x.dtype.itemsize != itemsize:
+            raise SpectralError(f"expected a contiguous tensor of {itemsize}-byte floats")
         return x.data_ptr()
     raise SpectralError(f"cannot take a device pointer of {type(x)}")
 
@@ -422,6 +438,22 @@ class Plan:
     def launch(self, stream: int = 0):
         _check(self.L.spectral_graph_launch(self.h, _stream(stream)), "spectral_graph_launch")
 
+    def set_learned(self, net: Optional["FourierOperator"], tol: float = 1e-3,
+                    check_every: int = 1):
+        """Use net for computeQ with LEARNED, spot-checked against the plain
+        FP32 operator every check_every calls (spectral_plan_set_learned)."""
+        self._net = net
+        _check(self.L.spectral_plan_set_learned(self.h, net.h if net else None, float(tol),
+                                                int(check_every)), "set_learned")
+
+    def learned_stats(self) -> dict:
+        c, k, fb = C.c_longlong(), C.c_longlong(), C.c_longlong()
+        e = C.c_double()
+        _check(self.L.spectral_plan_learned_stats(self.h, C.byref(c), C.byref(k), C.byref(fb),
+                                                  C.byref(e)), "learned_stats")
+        return {"calls": c.value, "checks": k.value, "fallbacks": fb.value,
+                "last_err": e.value}
+
     def set_profiling(self, on: bool):
         _check(self.L.spectral_plan_set_profiling(self.h, 1 if on else 0), "set_profiling")
 
@@ -431,6 +463,92 @@ class Plan:
         n = C.c_int()
         _check(self.L.spectral_plan_conv_time(self.h, C.byref(ms), C.byref(n)), "conv_time")
         return ms.value, n.value
+
+
+class FourierOperator:
+    """The learned collision operator (spectral_fno): a Fourier neural
+    operator on the lowest modes^3 Fourier modes, BF16 tensor-core GEMMs with
+    FP32 accumulation, trained on the device by the library's own forward
+    and backward kernels."""
+
+    def __init__(self, N: int, width: int = 64, modes: int = 12, layers: int = 4,
+                 hidden: int = 128, seed: int = 1):
+        self.L = lib()
+        self.N, self.n3 = N, N ** 3
+        self.width, self.modes, self.layers, self.hidden = width, modes, layers, hidden
+        h = C.c_void_p()
+        _check(self.L.spectral_fno_create(C.byref(h), N, width, modes, layers, hidden,
+                                          int(seed)), "spectral_fno_create")
+        self.h = h
+        self.nparams = int(self.L.spectral_fno_num_params(h))
+        self.nclasses = int(self.L.spectral_fno_num_classes(h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.spectral_fno_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def get_params(self) -> np.ndarray:
+        out = np.empty(self.nparams, dtype=np.float32)
+        _check(self.L.spectral_fno_get_params(self.h, out.ctypes.data_as(C.POINTER(C.c_float))),
+               "fno_get_params")
+        return out
+
+    def set_params(self, theta: np.ndarray):
+        theta = np.ascontiguousarray(theta, dtype=np.float32)
+        if theta.size != self.nparams:
+            raise SpectralError(f"expected {self.nparams} parameters, got {theta.size}")
+        _check(self.L.spectral_fno_set_params(self.h, theta.ctypes.data_as(C.POINTER(C.c_float))),
+               "fno_set_params")
+
+    @property
+    def output_scale(self) -> float:
+        return float(self.L.spectral_fno_output_scale(self.h))
+
+    @output_scale.setter
+    def output_scale(self, sigma: float):
+        _check(self.L.spectral_fno_set_output_scale(self.h, float(sigma)), "fno_set_output_scale")
+
+    def predict(self, f, Q, B: int, stream: int = 0):
+        """Network output (FP64 device) for f (FP64 device), no projection."""
+        _check(self.L.spectral_fno_predict(self.h, _ptr(f), _ptr(Q), B, _stream(stream)),
+               "fno_predict")
+
+    def loss_grad(self, f32, Q32, B: int):
+        """(loss, gradient) for FP32 device data; the gradient is a host array."""
+        g = np.empty(self.nparams, dtype=np.float32)
+        loss = C.c_double()
+        _check(self.L.spectral_fno_loss_grad(self.h, _ptr(f32, 4), _ptr(Q32, 4), B,
+                                             C.byref(loss), g.ctypes.data_as(C.POINTER(C.c_float))),
+               "fno_loss_grad")
+        return loss.value, g
+
+    def train_step(self, f32, Q32, B: int, lr: float, want_loss: bool = False,
+                   stream: int = 0):
+        loss = C.c_double()
+        _check(self.L.spectral_fno_train_step(self.h, _ptr(f32, 4), _ptr(Q32, 4), B, float(lr),
+                                              C.byref(loss) if want_loss else None,
+                                              _stream(stream)), "fno_train_step")
+        return loss.value if want_loss else None
+
+    def save(self, path: str):
+        np.savez(path, theta=self.get_params(), sigma=self.output_scale,
+                 shape=np.array([self.N, self.width, self.modes, self.layers, self.hidden]))
+
+    @classmethod
+    def load(cls, path: str) -> "FourierOperator":
+        d = np.load(path)
+        N, width, modes, layers, hidden = (int(x) for x in d["shape"])
+        net = cls(N, width, modes, layers, hidden)
+        net.set_params(d["theta"])
+        net.output_scale = float(d["sigma"])
+        return net
 
 
 def group_computeQ(plans, fs, Qs, flags: int = FP32 | CONSERVE, stream: int = 0):

@@ -18,7 +18,7 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libspectral_gb300.so")
 
 SOURCES = ["fft3d.cu", "conv.cu", "conv_ws.cu", "conserve.cu", "weights.cu", "transport.cu",
-           "capi.cu", "noalloc.cu", "probe.cu"]
+           "capi.cu", "noalloc.cu", "probe.cu", "fno.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
          "-Xcompiler", "-fvisibility=default"]

@@ -7,6 +7,7 @@
 // boltz.c runs against this library.
 // Part 2 (spectral_plan) keeps everything resident on the device.
 #include "common.cuh"
+#include "fno.h"
 #include "kernels.h"
 #include "../../include/spectral_bte.h"
 
@@ -41,6 +42,7 @@ int last_error() { return g_last_error; }
 const char *last_message() { return g_last_msg; }
 
 static void count(int n) { g_launches += n; }
+void add_launches(int n) { count(n); }
 
 #define SBTE_TRY(expr)                                                     \
     do {                                                                   \
@@ -451,6 +453,14 @@ struct spectral_plan_s {
     // host staging for spectral_computeQ_host
     int caphost = 0;
     double *d_fh = nullptr, *d_Qh = nullptr;
+    // learned operator (spectral_plan_set_learned) and its spot-check state
+    spectral_fno_s *fno = nullptr;
+    double ltol = 1e-3;
+    int levery = 1;
+    long long lcalls = 0, lchecks = 0, lfallbacks = 0;
+    double lerr = -1.0;
+    bool lok = true;
+    double *lq = nullptr, *d_lerr = nullptr;
 
     ~spectral_plan_s()
     {
@@ -467,6 +477,7 @@ struct spectral_plan_s {
         dfree(qacc); dfree(tmp32);
         for (auto &p : r32) dfree(p);
         dfree(sQ); dfree(sf1); dfree(d_fh); dfree(d_Qh);
+        dfree(lq); dfree(d_lerr);
         dfree(d_x); dfree(d_dx); dfree(fconv); dfree(f1); dfree(ftmp); dfree(f_l); dfree(f_r);
         if (graph_exec) cudaGraphExecDestroy(graph_exec);
         if (graph) cudaGraphDestroy(graph);
@@ -762,6 +773,50 @@ static int q_fp32(spectral_plan_s *p, const double *fdev, double *Qdev, int B,
 }
 
 static int computeQ_dev(spectral_plan_s *p, const double *f, double *Q, int B,
+                        int flags, cudaStream_t st);
+
+// The learned operator with its periodic spot check.  Every levery-th call
+// one instance (rotating) is recomputed with the plain FP32 operator and
+// conservation; a rel-L2 distance above ltol switches the plan to the plain
+// operator (flags without SPECTRAL_LEARNED) for this call and for every call
+// up to the next check that passes.  The network output is always projected
+// by the FP64 conservation step.
+static int learned_q(spectral_plan_s *p, const double *f, double *Q, int B, int flags,
+                     cudaStream_t st)
+{
+    if (!p->fno || fno_grid_n(p->fno) != p->N) {
+        set_error(kErrNotInit, "computeQ: SPECTRAL_LEARNED without a learned operator for N=%d",
+                  p->N);
+        return kErrNotInit;
+    }
+    const int plain = flags & ~SPECTRAL_LEARNED;
+    const long long n3 = p->n3;
+    const bool check = p->levery > 0 && (p->lcalls % p->levery) == 0;
+    p->lcalls++;
+    if (!check && !p->lok) {
+        p->lfallbacks++;
+        return computeQ_dev(p, f, Q, B, plain, st);
+    }
+    SBTE_TRY(fno_predict(p->fno, f, Q, B, st));
+    SBTE_LAUNCH(conserve_batch(Q, B, p->d_v, p->cons, st), 1);
+    if (!check) return kOk;
+    if (!p->lq) {
+        SBTE_TRY(dalloc(&p->lq, n3));
+        SBTE_TRY(dalloc(&p->d_lerr, 1));
+    }
+    const int b = (int)((p->lchecks++) % B);
+    SBTE_TRY(q_fp32(p, f + (long long)b * n3, p->lq, 1, false, st));
+    SBTE_LAUNCH(conserve_batch(p->lq, 1, p->d_v, p->cons, st), 1);
+    SBTE_TRY(rel_l2_device(Q + (long long)b * n3, p->lq, n3, p->d_lerr, st));
+    SBTE_CUDA(cudaMemcpyAsync(&p->lerr, p->d_lerr, sizeof(double), cudaMemcpyDeviceToHost, st));
+    SBTE_CUDA(cudaStreamSynchronize(st));
+    p->lok = std::isfinite(p->lerr) && p->lerr <= p->ltol;
+    if (p->lok) return kOk;
+    p->lfallbacks++;
+    return computeQ_dev(p, f, Q, B, plain, st);
+}
+
+static int computeQ_dev(spectral_plan_s *p, const double *f, double *Q, int B,
                         int flags, cudaStream_t st)
 {
     if (!p || !f || !Q || B < 1) {
@@ -773,6 +828,7 @@ static int computeQ_dev(spectral_plan_s *p, const double *f, double *Q, int B,
         return kErrWeights;
     }
     SBTE_CUDA(cudaSetDevice(p->device));
+    if (flags & SPECTRAL_LEARNED) return learned_q(p, f, Q, B, flags, st);
     const bool mp = (flags & SPECTRAL_MAXPRESERVE) != 0;
     if (flags & SPECTRAL_FP32)
         SBTE_TRY(q_fp32(p, f, Q, B, mp, st));
@@ -1237,6 +1293,36 @@ int spectral_plan_conv_time(spectral_plan *p, double *total_ms, int *launches)
     *total_ms = tot;
     *launches = (int)p->prof_used;
     p->prof_used = 0;
+    return kOk;
+}
+
+int spectral_plan_set_learned(spectral_plan *p, spectral_fno *net, double tol, int check_every)
+{
+    if (!p || (net && fno_grid_n(net) != p->N) || !(tol > 0.0) || check_every < 0) {
+        set_error(kErrArg, "spectral_plan_set_learned: need a plan, a network for the same N, "
+                           "tol > 0 and check_every >= 0");
+        return kErrArg;
+    }
+    p->fno = net;
+    p->ltol = tol;
+    p->levery = check_every;
+    p->lcalls = p->lchecks = p->lfallbacks = 0;
+    p->lerr = -1.0;
+    p->lok = true;
+    return kOk;
+}
+
+int spectral_plan_learned_stats(spectral_plan *p, long long *calls, long long *checks,
+                                long long *fallbacks, double *last_err)
+{
+    if (!p) {
+        set_error(kErrArg, "spectral_plan_learned_stats: null plan");
+        return kErrArg;
+    }
+    if (calls) *calls = p->lcalls;
+    if (checks) *checks = p->lchecks;
+    if (fallbacks) *fallbacks = p->lfallbacks;
+    if (last_err) *last_err = p->lerr;
     return kOk;
 }
 

@@ -1,0 +1,1115 @@
+// fno.cu -- the learned collision operator: a Fourier neural operator that
+// maps f to Q(f) on the velocity grid, trained and evaluated on the device
+// with BF16 tensor-core GEMMs and FP32 accumulation.  The reference has no
+// counterpart; its judge is the plain operator of this library.
+//
+// Network, per instance (f on the N^3 grid, p a grid point, c, d channels):
+//   x(p)   = f(p) / s,  s = max_p f(p)                (Q is bilinear in f)
+//   h0     = P x + bP                                  (lift, width C)
+//   z_l    = W_l h_l + b_l + S_l h_l,  h_{l+1} = gelu(z_l)  (no gelu after the last layer)
+//   S_l h  = Re sum_m e^{+i theta(m,p)} R_l[|m|^2] (N^-3 sum_p' e^{-i theta(m,p')} h(p'))
+//   u      = Q1 h_L + c1,   y = q2 . gelu(u) + c2,   Q = s^2 sigma y
+// theta(m, p) = 2 pi m.p / N over the lowest Km^3 modes m in [-Km/2, Km/2)^3.
+// The spectral weights are shared by all modes of equal |m|^2 (the collision
+// operator is isotropic) and are real.  Training minimises the mean over
+// instances of |y - Q/(s^2 sigma)|^2 / |Q/(s^2 sigma)|^2 with Adam.
+//
+// Layouts on the device, Bp = instances rounded up to 8:
+//   activations [p][c][b]  (b innermost), BF16 between GEMMs, FP32 z, S, dH
+//   T1 [i][j][2][mk][c][b], T2 [i][2][mj][mk][c][b], X/Y [mi][2][mj mk][c][b],
+//   U1 [i][2][mj][mk][c][b], U2 [i][j][2][mk][c][b]  ("2" = re, im blocks)
+// so every axis transform, channel mix and mode mix is a gemm_sa over a
+// contiguous stream (fno_gemm.cuh), and every weight gradient a gemm_nt.
+#include "common.cuh"
+#include "fno.h"
+#include "fno_gemm.cuh"
+#include "kernels.h"
+#include "../../include/spectral_bte.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <vector>
+
+using sbte::fno::bf16;
+
+namespace sbte {
+namespace fno {
+namespace {
+
+constexpr int kEw = 256;  // threads of the elementwise kernels
+
+// ------------------------------------------------------ elementwise ---
+template <typename T>
+__global__ void inst_max_kernel(const T *__restrict__ f, long long P, int B, float *s)
+{
+    __shared__ float red[32];
+    const int b = blockIdx.x;
+    float m = 0.f;
+    if (b < B)
+        for (long long p = threadIdx.x; p < P; p += blockDim.x)
+            m = fmaxf(m, (float)f[(long long)b * P + p]);
+    for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float r = 0.f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) r = fmaxf(r, red[w]);
+        s[b] = r > 0.f ? r : 1.f;
+    }
+}
+
+// x[p][b] = f[b][p] * mul / s[b]^pw for b < B, 0 for padding instances.
+template <typename T>
+__global__ void to_pb_kernel(const T *__restrict__ f, const float *__restrict__ s, int pw,
+                             float mul, int B, int Bp, long long P, float *__restrict__ x)
+{
+    __shared__ float tile[32][33];
+    const long long p0 = (long long)blockIdx.x * 32;
+    const int b0 = blockIdx.y * 32;
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+        const int b = b0 + r;
+        const long long p = p0 + threadIdx.x;
+        float v = 0.f;
+        if (b < B && p < P) {
+            const float sb = s[b];
+            v = (float)f[(long long)b * P + p] * mul / (pw == 2 ? sb * sb : sb);
+        }
+        tile[r][threadIdx.x] = v;
+    }
+    __syncthreads();
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+        const long long p = p0 + r;
+        const int b = b0 + threadIdx.x;
+        if (p < P && b < Bp) x[p * Bp + b] = tile[threadIdx.x][r];
+    }
+}
+
+// Q[b][p] = s[b]^2 sigma y[p][b] (FP64).
+__global__ void from_pb_kernel(const float *__restrict__ y, const float *__restrict__ s,
+                               float sigma, int B, int Bp, long long P, double *__restrict__ Q)
+{
+    __shared__ float tile[32][33];
+    const long long p0 = (long long)blockIdx.x * 32;
+    const int b0 = blockIdx.y * 32;
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+        const long long p = p0 + r;
+        const int b = b0 + threadIdx.x;
+        tile[r][threadIdx.x] = (p < P && b < Bp) ? y[p * Bp + b] : 0.f;
+    }
+    __syncthreads();
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+        const int b = b0 + r;
+        const long long p = p0 + threadIdx.x;
+        if (b < B && p < P) {
+            const double sb = s[b];
+            Q[(long long)b * P + p] = sb * sb * (double)sigma * (double)tile[threadIdx.x][r];
+        }
+    }
+}
+
+__device__ __forceinline__ void st_bf16x8(bf16 *dst, const float (&v)[8])
+{
+    __nv_bfloat162 q[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) q[i] = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
+    *reinterpret_cast<uint4 *>(dst) = *reinterpret_cast<uint4 *>(q);
+}
+__device__ __forceinline__ void ld_f32x8(const float *src, float (&v)[8])
+{
+    const float4 a = *reinterpret_cast<const float4 *>(src);
+    const float4 b = *reinterpret_cast<const float4 *>(src + 4);
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+    v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+}
+
+// h[p][c][b] = bf16(P[c] x[p][b] + bP[c]); 8 instances per thread.
+__global__ void lift_kernel(const float *__restrict__ x, const float *__restrict__ Pw,
+                            const float *__restrict__ bP, bf16 *__restrict__ h, long long P,
+                            int C, int Bp)
+{
+    const long long n8 = P * C * Bp / 8;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n8;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long e = i * 8;
+        const long long p = e / ((long long)C * Bp);
+        const int c = (int)((e / Bp) % C), b = (int)(e % Bp);
+        float v[8];
+        ld_f32x8(x + p * Bp + b, v);
+#pragma unroll
+        for (int j = 0; j < 8; j++) v[j] = Pw[c] * v[j] + bP[c];
+        st_bf16x8(h + e, v);
+    }
+}
+
+// Per-channel sums through shared memory, flushed with one global atomic
+// per channel and block.
+template <int MAXC> struct ChanAcc {
+    float *s;
+    __device__ void init(float *buf, int n)
+    {
+        s = buf;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) s[i] = 0.f;
+        __syncthreads();
+    }
+    __device__ void flush(float *g, int n)
+    {
+        __syncthreads();
+        for (int i = threadIdx.x; i < n; i += blockDim.x)
+            if (s[i] != 0.f) atomicAdd(g + i, s[i]);
+    }
+};
+
+// dZ = bf16(dH * gelu'(Z)) (or dH where Z == nullptr); db[c] += sum dZ.
+__global__ void gelu_bwd_kernel(const float *__restrict__ dH, const float *__restrict__ Z,
+                                bf16 *__restrict__ dZ, float *db, long long P, int C, int Bp)
+{
+    __shared__ float sdb[128];
+    ChanAcc<128> acc;
+    acc.init(sdb, C);
+    const long long n8 = P * C * Bp / 8;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n8;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long e = i * 8;
+        const int c = (int)((e / Bp) % C);
+        float v[8], zz[8];
+        ld_f32x8(dH + e, v);
+        if (Z) {
+            ld_f32x8(Z + e, zz);
+#pragma unroll
+            for (int j = 0; j < 8; j++) v[j] *= gelu_grad(zz[j]);
+        }
+        float s = 0.f;
+#pragma unroll
+        for (int j = 0; j < 8; j++) s += v[j];
+        atomicAdd(&sdb[c], s);
+        st_bf16x8(dZ + e, v);
+    }
+    acc.flush(db, C);
+}
+
+// Projection backward: dU = bf16(dy q2 gelu'(u)); dq2 += dy gelu(u); dc1 += dy q2 gelu'(u).
+__global__ void proj_bwd_kernel(const float *__restrict__ U, const float *__restrict__ dy,
+                                const float *__restrict__ q2, bf16 *__restrict__ dU, float *dq2,
+                                float *dc1, long long P, int Hd, int Bp)
+{
+    __shared__ float s1[128], s2[128];
+    ChanAcc<128> a1, a2;
+    a1.init(s1, Hd);
+    a2.init(s2, Hd);
+    const long long n8 = P * Hd * Bp / 8;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n8;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long e = i * 8;
+        const long long p = e / ((long long)Hd * Bp);
+        const int c = (int)((e / Bp) % Hd), b = (int)(e % Bp);
+        float u[8], d[8], o[8];
+        ld_f32x8(U + e, u);
+        ld_f32x8(dy + p * Bp + b, d);
+        float sq = 0.f, sc = 0.f;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            o[j] = d[j] * q2[c] * gelu_grad(u[j]);
+            sq += d[j] * gelu_f(u[j]);
+            sc += o[j];
+        }
+        atomicAdd(&s1[c], sq);
+        atomicAdd(&s2[c], sc);
+        st_bf16x8(dU + e, o);
+    }
+    a1.flush(dq2, Hd);
+    a2.flush(dc1, Hd);
+}
+
+// Lift backward: dP[c] += sum dH x; dbP[c] += sum dH.
+__global__ void lift_bwd_kernel(const float *__restrict__ dH, const float *__restrict__ x,
+                                float *dP, float *dbP, long long P, int C, int Bp)
+{
+    __shared__ float s1[128], s2[128];
+    ChanAcc<128> a1, a2;
+    a1.init(s1, C);
+    a2.init(s2, C);
+    const long long n8 = P * C * Bp / 8;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n8;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long e = i * 8;
+        const long long p = e / ((long long)C * Bp);
+        const int c = (int)((e / Bp) % C), b = (int)(e % Bp);
+        float g[8], xv[8];
+        ld_f32x8(dH + e, g);
+        ld_f32x8(x + p * Bp + b, xv);
+        float sp = 0.f, sb = 0.f;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            sp += g[j] * xv[j];
+            sb += g[j];
+        }
+        atomicAdd(&s1[c], sp);
+        atomicAdd(&s2[c], sb);
+    }
+    a1.flush(dP, C);
+    a2.flush(dbP, C);
+}
+
+// den[b] = sum_p t[p][b]^2.
+__global__ void den_kernel(const float *__restrict__ t, float *den, long long P, int Bp)
+{
+    const long long rows = (P + gridDim.x - 1) / gridDim.x;
+    const long long p0 = blockIdx.x * rows, p1 = min(P, p0 + rows);
+    for (int b = threadIdx.x; b < Bp; b += blockDim.x) {
+        float s = 0.f;
+        for (long long p = p0; p < p1; p++) {
+            const float v = t[p * Bp + b];
+            s += v * v;
+        }
+        atomicAdd(den + b, s);
+    }
+}
+
+// dy = 2 (y - t) / (den_b B) for b < B (0 for padding); loss += sum (y-t)^2 / (den_b B);
+// dc2 += sum dy.
+__global__ void loss_kernel(const float *__restrict__ y, const float *__restrict__ t,
+                            const float *__restrict__ den, float *__restrict__ dy,
+                            double *loss, float *dc2, long long n, int B, int Bp)
+{
+    __shared__ double r1[32];
+    __shared__ float r2[32];
+    double l = 0.0;
+    float g = 0.f;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int b = (int)(i % Bp);
+        float d = 0.f;
+        if (b < B) {
+            const float r = y[i] - t[i];
+            const float inv = 1.f / (den[b] * (float)B);
+            d = 2.f * r * inv;
+            l += (double)r * r * inv;
+        }
+        dy[i] = d;
+        g += d;
+    }
+    for (int o = 16; o; o >>= 1) {
+        l += __shfl_xor_sync(0xffffffffu, l, o);
+        g += __shfl_xor_sync(0xffffffffu, g, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        r1[threadIdx.x >> 5] = l;
+        r2[threadIdx.x >> 5] = g;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0;
+        float b2 = 0.f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+            a += r1[w];
+            b2 += r2[w];
+        }
+        atomicAdd(loss, a);
+        atomicAdd(dc2, b2);
+    }
+}
+
+__global__ void adam_kernel(float *__restrict__ p, const float *__restrict__ g,
+                            float *__restrict__ m, float *__restrict__ v, long long n, float lr,
+                            float b1, float b2, float eps, float c1, float c2)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const float gi = g[i];
+        const float mi = b1 * m[i] + (1.f - b1) * gi;
+        const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    }
+}
+
+// out[0] = |A_b - R_b| / |R_b| for the single instance pointed at.
+__global__ void rel_l2_kernel(const double *__restrict__ A, const double *__restrict__ R,
+                              long long n, double *out)
+{
+    __shared__ double s1[32], s2[32];
+    double a = 0.0, b = 0.0;
+    for (long long i = threadIdx.x; i < n; i += blockDim.x) {
+        const double d = A[i] - R[i];
+        a += d * d;
+        b += R[i] * R[i];
+    }
+    for (int o = 16; o; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        s1[threadIdx.x >> 5] = a;
+        s2[threadIdx.x >> 5] = b;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double x = 0.0, y = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+            x += s1[w];
+            y += s2[w];
+        }
+        out[0] = y > 0.0 ? sqrt(x / y) : sqrt(x);
+    }
+}
+
+inline int ew_grid(long long n8)
+{
+    long long g = (n8 + kEw - 1) / kEw;
+    return (int)std::max(1LL, std::min(g, 152LL * 8));
+}
+
+}  // namespace
+}  // namespace fno
+
+// =========================================================== launches ===
+namespace {
+using namespace fno;
+
+bool view_ok(const StreamView &v, const void *base)
+{
+    auto m8 = [](long long x) { return (x % 8) == 0; };
+    return v.w > 0 && m8(v.w) && m8(v.s_r) && m8(v.s_blk) && m8(v.im) && m8(v.s_z1) &&
+           m8(v.s_z2) && ((uintptr_t)base % 16) == 0;
+}
+
+// Largest element offset + 1 that a view touches over rows [0, R), n in
+// [0, Nn) and batches [0, nz).
+long long view_extent(const StreamView &v, long long R, long long Nn, int nz, int nz2)
+{
+    const long long zmax = (long long)((nz - 1) / nz2) * v.s_z1 + (long long)std::min(nz - 1, nz2 - 1) * v.s_z2;
+    const long long nmax = ((Nn - 1) / v.w) * v.s_blk + (Nn > v.w ? v.w - 1 : Nn - 1);
+    return zmax + (R - 1) * v.s_r + nmax + v.im + 1;
+}
+
+bool sa_bounds_ok(const SaArgs &a, bool AC)
+{
+    if (a.extA > 0) {
+        const long long amax = a.a_tab ? (long long)a.a_tab_max * a.s_atab : 0;
+        const long long e = amax + (a.M - 1) * a.sAm + (a.K - 1) * a.sAk + (AC ? a.imA : 0) + 1;
+        if (e > a.extA) return false;
+    }
+    if (a.extB > 0 && view_extent(a.B, a.K, a.Nn, a.nz, a.nz2) > a.extB) return false;
+    if (a.extC > 0 && view_extent(a.C, a.M, a.Nn, a.nz, a.nz2) > a.extC) return false;
+    return true;
+}
+
+template <int MT, int BN, int WM, int WN, bool AC, bool BC, int EPI>
+cudaError_t launch_sa(SaArgs a, cudaStream_t st)
+{
+    a.KP = (a.K + 15) / 16 * 16;
+    if (a.M > MT || a.KP > 128 || a.Nn % 8 != 0 || !view_ok(a.B, a.B.p) ||
+        !view_ok(a.C, a.C.p) || !sa_bounds_ok(a, AC))
+        return cudaErrorInvalidValue;
+    const size_t sm = gemm_sa_smem<MT, BN, WM, WN, AC, BC, EPI>(a.KP);
+    auto kern = gemm_sa_kernel<MT, BN, WM, WN, AC, BC, EPI>;
+    if (sm > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)sm);
+        if (e != cudaSuccess) return e;
+    }
+    const long long total = ((a.Nn + BN - 1) / BN) * a.nz;
+    const int grid = (int)std::min<long long>(total, 152LL * 6);
+    kern<<<grid, WM * WN * 32, sm, st>>>(a);
+    add_launches(1);
+    return cudaGetLastError();
+}
+
+template <int MT, int NT, int WM, int WN>
+cudaError_t launch_nt(NtArgs a, cudaStream_t st)
+{
+    if (a.M > MT || a.N > NT || a.K % 8 || a.a_w % 8 || a.b_w % 8 || a.a_m % 8 || a.b_n % 8 ||
+        a.a_blk % 8 || a.b_blk % 8 || a.KC % 32)
+        return cudaErrorInvalidValue;
+    auto ext = [&](long long rows, long long s_r, long long w, long long blk, long long z1,
+                   long long z2) {
+        const long long zmax = (long long)((a.nz - 1) / a.nz2) * z1 +
+                               (long long)std::min(a.nz - 1, a.nz2 - 1) * z2;
+        return zmax + (rows - 1) * s_r + ((a.K - 1) / w) * blk + (a.K > w ? w - 1 : a.K - 1) + 1;
+    };
+    if ((a.extA > 0 && ext(a.M, a.a_m, a.a_w, a.a_blk, a.a_z1, a.a_z2) > a.extA) ||
+        (a.extB > 0 && ext(a.N, a.b_n, a.b_w, a.b_blk, a.b_z1, a.b_z2) > a.extB))
+        return cudaErrorInvalidValue;
+    const long long total = ((a.K + a.KC - 1) / a.KC) * a.nz;
+    const int grid = (int)std::min<long long>(total, 152LL * 4);
+    gemm_nt_kernel<MT, NT, WM, WN><<<grid, WM * WN * 32, 0, st>>>(a);
+    add_launches(1);
+    return cudaGetLastError();
+}
+
+StreamView sv(const void *p, long long s_r, long long w, long long s_blk, long long im = 0,
+              long long z1 = 0, long long z2 = 0)
+{
+    return StreamView{p, s_r, s_blk, w, im, z1, z2};
+}
+
+SaArgs sa_base(const float *A, long long sAm, long long sAk, long long imA, int M, int K)
+{
+    SaArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.A = A;
+    a.sAm = sAm;
+    a.sAk = sAk;
+    a.imA = imA;
+    a.a_im_sign = 1.f;
+    a.M = M;
+    a.K = K;
+    a.nz = 1;
+    a.nz2 = 1;
+    return a;
+}
+
+}  // namespace
+}  // namespace sbte
+
+// ============================================================ network ===
+using namespace sbte;
+using namespace sbte::fno;
+
+struct spectral_fno_s {
+    int device = 0;
+    int N = 0, C = 0, Km = 0, L = 0, Hd = 0, ncls = 0;
+    long long P = 0;
+    long long nparams = 0;
+    long long oP = 0, obP = 0, oW[8] = {}, ob[8] = {}, oR[8] = {}, oQ1 = 0, oc1 = 0, oq2 = 0,
+              oc2 = 0;
+    float sigma = 1.f;
+    float *params = nullptr, *grads = nullptr, *am = nullptr, *av = nullptr;
+    long long adam_t = 0;
+    float *F = nullptr, *G = nullptr;  // DFT axis matrices
+    int *cls = nullptr;                // class of batch z = (mi*2+part)*Km^2 + mjk
+    // activations (capacity cap instances)
+    int cap = 0;
+    bool cap_train = false;
+    float *s = nullptr, *x = nullptr, *t = nullptr, *den = nullptr, *y = nullptr, *dy = nullptr;
+    bf16 *H[9] = {};
+    float *Z[8] = {};
+    float *S = nullptr, *Up = nullptr, *dH = nullptr;
+    bf16 *T1 = nullptr, *T2 = nullptr, *X[8] = {}, *Y = nullptr, *U1 = nullptr, *U2 = nullptr;
+    bf16 *dU = nullptr, *dZ = nullptr, *GY = nullptr, *GX = nullptr;
+    double *d_loss = nullptr;
+    std::vector<void *> owned;
+
+    void free_acts()
+    {
+        for (void *q : owned) cudaFree(q);
+        owned.clear();
+        s = x = t = den = y = dy = S = Up = dH = nullptr;
+        for (auto &q : H) q = nullptr;
+        for (auto &q : Z) q = nullptr;
+        for (auto &q : X) q = nullptr;
+        T1 = T2 = Y = U1 = U2 = dU = dZ = GY = GX = nullptr;
+        d_loss = nullptr;
+        cap = 0;
+    }
+    ~spectral_fno_s()
+    {
+        cudaSetDevice(device);
+        free_acts();
+        for (float *q : {params, grads, am, av, F, G}) cudaFree(q);
+        cudaFree(cls);
+    }
+};
+
+namespace {
+
+template <typename T> int nalloc(spectral_fno_s *n, T **p, long long count)
+{
+    *p = nullptr;
+    if (count <= 0) return kOk;
+    cudaError_t e = cudaMalloc((void **)p, sizeof(T) * (size_t)count);
+    if (e != cudaSuccess) {
+        set_error(kErrNoMem, "cudaMalloc of %lld bytes failed: %s",
+                  (long long)(sizeof(T) * count), cudaGetErrorString(e));
+        *p = nullptr;
+        return kErrNoMem;
+    }
+    n->owned.push_back(*p);
+    return kOk;
+}
+
+#define FNO_TRY(expr)                                                          \
+    do {                                                                       \
+        int rc_ = (expr);                                                      \
+        if (rc_ != kOk) return rc_;                                            \
+    } while (0)
+#define FNO_LAUNCH(expr)                                                       \
+    do {                                                                       \
+        cudaError_t e_ = (expr);                                               \
+        if (e_ != cudaSuccess) {                                               \
+            set_error(kErrCuda, "%s:%d %s: %s", __FILE__, __LINE__, #expr,     \
+                      cudaGetErrorString(e_));                                 \
+            return kErrCuda;                                                   \
+        }                                                                      \
+    } while (0)
+
+int ensure(spectral_fno_s *n, int Bp, bool train)
+{
+    if (Bp <= n->cap && (!train || n->cap_train)) return kOk;
+    cudaDeviceSynchronize();
+    n->free_acts();
+    const long long P = n->P, C = n->C, Km = n->Km, N = n->N, Hd = n->Hd;
+    const long long act = P * C * Bp;
+    const long long t1 = N * N * 2 * Km * C * Bp, t2 = N * 2 * Km * Km * C * Bp,
+                    xm = 2 * Km * Km * Km * C * Bp;
+    FNO_TRY(nalloc(n, &n->s, Bp));
+    FNO_TRY(nalloc(n, &n->x, P * Bp));
+    FNO_TRY(nalloc(n, &n->y, P * Bp));
+    FNO_TRY(nalloc(n, &n->S, act));
+    FNO_TRY(nalloc(n, &n->T1, t1));
+    FNO_TRY(nalloc(n, &n->T2, t2));
+    FNO_TRY(nalloc(n, &n->Y, xm));
+    FNO_TRY(nalloc(n, &n->U1, t2));
+    FNO_TRY(nalloc(n, &n->U2, t1));
+    const int nh = train ? n->L + 1 : 2;
+    for (int l = 0; l < nh; l++) FNO_TRY(nalloc(n, &n->H[l], act));
+    const int nx = train ? n->L : 1;
+    for (int l = 0; l < nx; l++) FNO_TRY(nalloc(n, &n->X[l], xm));
+    if (train) {
+        for (int l = 0; l < n->L; l++) FNO_TRY(nalloc(n, &n->Z[l], act));
+        FNO_TRY(nalloc(n, &n->t, P * Bp));
+        FNO_TRY(nalloc(n, &n->den, Bp));
+        FNO_TRY(nalloc(n, &n->dy, P * Bp));
+        FNO_TRY(nalloc(n, &n->Up, P * Hd * Bp));
+        FNO_TRY(nalloc(n, &n->dU, P * Hd * Bp));
+        FNO_TRY(nalloc(n, &n->dH, act));
+        FNO_TRY(nalloc(n, &n->dZ, act));
+        FNO_TRY(nalloc(n, &n->GY, xm));
+        FNO_TRY(nalloc(n, &n->GX, xm));
+        FNO_TRY(nalloc(n, &n->d_loss, 1));
+    }
+    n->cap = Bp;
+    n->cap_train = train;
+    return kOk;
+}
+
+bf16 *Hbuf(spectral_fno_s *n, int l, bool train) { return train ? n->H[l] : n->H[l & 1]; }
+
+// Element counts of the activation buffers for Bp instances.
+struct Ext {
+    long long act, t1, t2, xm, proj, pb, F, G, prm;
+    Ext(const spectral_fno_s *n, int Bp)
+    {
+        const long long N = n->N, Km = n->Km, CB = (long long)n->C * Bp;
+        act = n->P * CB;
+        t1 = N * N * 2 * Km * CB;
+        t2 = N * 2 * Km * Km * CB;
+        xm = 2 * Km * Km * Km * CB;
+        proj = n->P * n->Hd * Bp;
+        pb = n->P * Bp;
+        F = 2 * Km * N;
+        G = 2 * N * Km;
+        prm = n->nparams;
+    }
+};
+
+void set_ext(SaArgs &a, long long eA, long long eB, long long eC)
+{
+    a.extA = eA;
+    a.extB = eB;
+    a.extC = eC;
+}
+
+// The truncated forward transform of in ([p][c][b], BF16) into out
+// ([mi][2][mj mk][c][b]): three axis passes with F (fno.cu header).
+int spectral_fwd(spectral_fno_s *n, const bf16 *in, bf16 *out, int Bp, cudaStream_t st)
+{
+    const long long N = n->N, Km = n->Km, CB = (long long)n->C * Bp;
+    const float *F = n->F;
+    const Ext E(n, Bp);
+    {  // axis k, real input
+        SaArgs a = sa_base(F, N, 1, Km * N, (int)Km, (int)N);
+        a.B = sv(in, CB, CB, N * CB);
+        a.C = sv(n->T1, CB, CB, 2 * Km * CB, Km * CB);
+        a.Nn = N * N * CB;
+        set_ext(a, E.F, E.act, E.t1);
+        FNO_LAUNCH((launch_sa<16, 128, 1, 4, true, false, kEpiCplxBF16>(a, st)));
+    }
+    {  // axis j
+        SaArgs a = sa_base(F, N, 1, Km * N, (int)Km, (int)N);
+        a.B = sv(n->T1, 2 * Km * CB, Km * CB, N * 2 * Km * CB, Km * CB);
+        a.C = sv(n->T2, Km * CB, Km * CB, 2 * Km * Km * CB, Km * Km * CB);
+        a.Nn = N * Km * CB;
+        set_ext(a, E.F, E.t1, E.t2);
+        FNO_LAUNCH((launch_sa<16, 128, 1, 4, true, true, kEpiCplxBF16>(a, st)));
+    }
+    {  // axis i
+        SaArgs a = sa_base(F, N, 1, Km * N, (int)Km, (int)N);
+        const long long w = Km * Km * CB;
+        a.B = sv(n->T2, 2 * w, w, 0, w);
+        a.C = sv(out, 2 * w, w, 0, w);
+        a.Nn = w;
+        set_ext(a, E.F, E.t2, E.xm);
+        FNO_LAUNCH((launch_sa<16, 128, 1, 4, true, true, kEpiCplxBF16>(a, st)));
+    }
+    return kOk;
+}
+
+// Mode mix out[z][d][b] = sum_c R[cls z] (transposed when tr) in[z][c][b].
+int mode_mix(spectral_fno_s *n, const float *R, bool tr, const bf16 *in, bf16 *out, int Bp,
+             cudaStream_t st)
+{
+    const long long C = n->C, Km = n->Km, CB = C * Bp;
+    SaArgs a = sa_base(R, tr ? 1 : C, tr ? C : 1, 0, (int)C, (int)C);
+    a.a_tab = n->cls;
+    a.s_atab = C * C;
+    a.a_tab_max = n->ncls - 1;
+    a.B = sv(in, Bp, Bp, 0, 0, Km * Km * CB, CB);
+    a.C = sv(out, Bp, Bp, 0, 0, Km * Km * CB, CB);
+    a.Nn = Bp;
+    a.nz = (int)(2 * Km * Km * Km);
+    a.nz2 = (int)(Km * Km);
+    const Ext E(n, Bp);
+    set_ext(a, (long long)n->ncls * C * C, E.xm, E.xm);
+    FNO_LAUNCH((launch_sa<64, 64, 2, 2, false, false, kEpiBF16>(a, st)));
+    return kOk;
+}
+
+// The inverse transform of in ([mi][2][mj mk][c][b]) to the real part on
+// the grid, stored to (or, when acc, added into) out [p][c][b] FP32.
+int spectral_inv(spectral_fno_s *n, const bf16 *in, float *out, bool acc, int Bp,
+                 cudaStream_t st)
+{
+    const long long N = n->N, Km = n->Km, CB = (long long)n->C * Bp;
+    const float *G = n->G;
+    const Ext E(n, Bp);
+    {  // axis i
+        SaArgs a = sa_base(G, Km, 1, N * Km, (int)N, (int)Km);
+        const long long w = Km * Km * CB;
+        a.B = sv(in, 2 * w, w, 0, w);
+        a.C = sv(n->U1, 2 * w, w, 0, w);
+        a.Nn = w;
+        set_ext(a, E.G, E.xm, E.t2);
+        FNO_LAUNCH((launch_sa<32, 128, 1, 4, true, true, kEpiCplxBF16>(a, st)));
+    }
+    {  // axis j
+        SaArgs a = sa_base(G, Km, 1, N * Km, (int)N, (int)Km);
+        a.B = sv(n->U1, Km * CB, Km * CB, 2 * Km * Km * CB, Km * Km * CB);
+        a.C = sv(n->U2, 2 * Km * CB, Km * CB, N * 2 * Km * CB, Km * CB);
+        a.Nn = N * Km * CB;
+        set_ext(a, E.G, E.t2, E.t1);
+        FNO_LAUNCH((launch_sa<32, 128, 1, 4, true, true, kEpiCplxBF16>(a, st)));
+    }
+    {  // axis k, real part
+        SaArgs a = sa_base(G, Km, 1, N * Km, (int)N, (int)Km);
+        a.B = sv(n->U2, CB, CB, 2 * Km * CB, Km * CB);
+        a.C = sv(out, CB, CB, N * CB);
+        a.Nn = N * N * CB;
+        set_ext(a, E.G, E.t1, E.act);
+        if (acc)
+            FNO_LAUNCH((launch_sa<32, 128, 1, 4, true, true, kEpiAccF32>(a, st)));
+        else
+            FNO_LAUNCH((launch_sa<32, 128, 1, 4, true, true, kEpiF32>(a, st)));
+    }
+    return kOk;
+}
+
+template <typename T>
+int forward(spectral_fno_s *n, const T *f, int B, int Bp, bool train, cudaStream_t st)
+{
+    const long long P = n->P, C = n->C, Hd = n->Hd;
+    const float *prm = n->params;
+    const Ext E(n, Bp);
+    inst_max_kernel<T><<<Bp, 256, 0, st>>>(f, P, B, n->s);
+    to_pb_kernel<T><<<dim3((unsigned)((P + 31) / 32), (unsigned)((Bp + 31) / 32)),
+                      dim3(32, 8), 0, st>>>(f, n->s, 1, 1.f, B, Bp, P, n->x);
+    const long long n8 = P * C * Bp / 8;
+    lift_kernel<<<ew_grid(n8), kEw, 0, st>>>(n->x, prm + n->oP, prm + n->obP, Hbuf(n, 0, train),
+                                              P, (int)C, Bp);
+    add_launches(3);
+    FNO_LAUNCH(cudaGetLastError());
+    for (int l = 0; l < n->L; l++) {
+        bf16 *hin = Hbuf(n, l, train), *hout = Hbuf(n, l + 1, train);
+        bf16 *xl = train ? n->X[l] : n->X[0];
+        FNO_TRY(spectral_fwd(n, hin, xl, Bp, st));
+        FNO_TRY(mode_mix(n, prm + n->oR[l], false, xl, n->Y, Bp, st));
+        FNO_TRY(spectral_inv(n, n->Y, n->S, false, Bp, st));
+        SaArgs a = sa_base(prm + n->oW[l], C, 1, 0, (int)C, (int)C);
+        a.B = sv(hin, Bp, Bp, C * Bp);
+        a.C = sv(hout, Bp, Bp, C * Bp);
+        a.Nn = P * Bp;
+        a.bias = prm + n->ob[l];
+        a.addend = n->S;
+        a.zst = train ? n->Z[l] : nullptr;
+        a.hout = hout;
+        a.act = (l < n->L - 1) ? 1 : 0;
+        set_ext(a, E.prm - n->oW[l], E.act, E.act);
+        FNO_LAUNCH((launch_sa<64, 128, 2, 2, false, false, kEpiLayer>(a, st)));
+    }
+    SaArgs a = sa_base(prm + n->oQ1, C, 1, 0, (int)Hd, (int)C);
+    a.B = sv(Hbuf(n, n->L, train), Bp, Bp, C * Bp);
+    a.C = sv(train ? (void *)n->Up : (void *)n->y, Bp, Bp, Hd * Bp);
+    a.Nn = P * Bp;
+    a.c1 = prm + n->oc1;
+    a.q2 = prm + n->oq2;
+    a.zst = train ? n->Up : nullptr;
+    a.c2 = prm + n->oc2;
+    a.y = n->y;
+    set_ext(a, E.prm - n->oQ1, E.act, train ? E.proj : 0);
+    FNO_LAUNCH((launch_sa<128, 64, 4, 2, false, false, kEpiProj>(a, st)));
+    return kOk;
+}
+
+}  // namespace
+
+namespace {
+
+// Gradients of the mean relative squared error of the last training
+// forward pass into n->grads (zeroed here); the loss into n->d_loss.
+int backward(spectral_fno_s *n, int B, int Bp, cudaStream_t st)
+{
+    const long long P = n->P, C = n->C, Hd = n->Hd, Km = n->Km, CB = C * Bp;
+    const float *prm = n->params;
+    float *gr = n->grads;
+    const Ext E(n, Bp);
+    FNO_LAUNCH(cudaMemsetAsync(gr, 0, sizeof(float) * n->nparams, st));
+    FNO_LAUNCH(cudaMemsetAsync(n->d_loss, 0, sizeof(double), st));
+    loss_kernel<<<ew_grid(P * Bp / 8), kEw, 0, st>>>(n->y, n->t, n->den, n->dy, n->d_loss,
+                                                      gr + n->oc2, P * Bp, B, Bp);
+    proj_bwd_kernel<<<ew_grid(P * Hd * Bp / 8), kEw, 0, st>>>(
+        n->Up, n->dy, prm + n->oq2, n->dU, gr + n->oq2, gr + n->oc1, P, (int)Hd, Bp);
+    add_launches(2);
+    FNO_LAUNCH(cudaGetLastError());
+    const long long KC = 16384;
+    {  // dQ1 += dU h_L^T
+        NtArgs a{};
+        a.A = n->dU; a.a_m = Bp; a.a_w = Bp; a.a_blk = Hd * Bp;
+        a.B = n->H[n->L]; a.b_n = Bp; a.b_w = Bp; a.b_blk = CB;
+        a.C = gr + n->oQ1; a.c_m = C;
+        a.M = (int)Hd; a.N = (int)C; a.K = P * Bp; a.KC = KC; a.nz = 1; a.nz2 = 1; a.alpha = 1.f;
+        a.extA = E.proj; a.extB = E.act;
+        FNO_LAUNCH((launch_nt<128, 64, 4, 2>(a, st)));
+    }
+    {  // dH = Q1^T dU
+        SaArgs a = sa_base(prm + n->oQ1, 1, C, 0, (int)C, (int)Hd);
+        a.B = sv(n->dU, Bp, Bp, Hd * Bp);
+        a.C = sv(n->dH, Bp, Bp, CB);
+        a.Nn = P * Bp;
+        set_ext(a, E.prm - n->oQ1, E.proj, E.act);
+        FNO_LAUNCH((launch_sa<64, 128, 2, 2, false, false, kEpiF32>(a, st)));
+    }
+    for (int l = n->L - 1; l >= 0; l--) {
+        gelu_bwd_kernel<<<ew_grid(P * CB / 8), kEw, 0, st>>>(
+            n->dH, l < n->L - 1 ? n->Z[l] : nullptr, n->dZ, gr + n->ob[l], P, (int)C, Bp);
+        add_launches(1);
+        FNO_LAUNCH(cudaGetLastError());
+        {  // dW_l += dZ h_l^T
+            NtArgs a{};
+            a.A = n->dZ; a.a_m = Bp; a.a_w = Bp; a.a_blk = CB;
+            a.B = n->H[l]; a.b_n = Bp; a.b_w = Bp; a.b_blk = CB;
+            a.C = gr + n->oW[l]; a.c_m = C;
+            a.M = (int)C; a.N = (int)C; a.K = P * Bp; a.KC = KC; a.nz = 1; a.nz2 = 1; a.alpha = 1.f;
+            a.extA = E.act; a.extB = E.act;
+            FNO_LAUNCH((launch_nt<64, 64, 2, 2>(a, st)));
+        }
+        {  // dH = W_l^T dZ
+            SaArgs a = sa_base(prm + n->oW[l], 1, C, 0, (int)C, (int)C);
+            a.B = sv(n->dZ, Bp, Bp, CB);
+            a.C = sv(n->dH, Bp, Bp, CB);
+            a.Nn = P * Bp;
+            set_ext(a, E.prm - n->oW[l], E.act, E.act);
+            FNO_LAUNCH((launch_sa<64, 128, 2, 2, false, false, kEpiF32>(a, st)));
+        }
+        // spectral path: GY = F dZ; dR += GY X^T per mode class; dH += Re G (R^T GY)
+        FNO_TRY(spectral_fwd(n, n->dZ, n->GY, Bp, st));
+        {
+            NtArgs a{};
+            const long long w = Km * Km * CB;
+            a.A = n->GY; a.a_m = Bp; a.a_w = Bp; a.a_blk = 0; a.a_z1 = w; a.a_z2 = CB;
+            a.B = n->X[l]; a.b_n = Bp; a.b_w = Bp; a.b_blk = 0; a.b_z1 = w; a.b_z2 = CB;
+            a.C = gr + n->oR[l]; a.c_m = C; a.c_tab = n->cls; a.c_tabs = C * C;
+            a.M = (int)C; a.N = (int)C; a.K = Bp; a.KC = (Bp + 31) / 32 * 32;
+            // GY = F3 dZ carries the transform's 1/N^3, so dL/dR = N^3 sum Re(GY conj X)
+            a.nz = (int)(2 * Km * Km * Km); a.nz2 = (int)(Km * Km);
+            a.alpha = (float)(n->P);
+            a.extA = E.xm; a.extB = E.xm;
+            FNO_LAUNCH((launch_nt<64, 64, 2, 2>(a, st)));
+        }
+        FNO_TRY(mode_mix(n, prm + n->oR[l], true, n->GY, n->GX, Bp, st));
+        FNO_TRY(spectral_inv(n, n->GX, n->dH, true, Bp, st));
+    }
+    lift_bwd_kernel<<<ew_grid(P * CB / 8), kEw, 0, st>>>(n->dH, n->x, gr + n->oP, gr + n->obP,
+                                                         P, (int)C, Bp);
+    add_launches(1);
+    FNO_LAUNCH(cudaGetLastError());
+    return kOk;
+}
+
+template <typename T>
+int loss_and_grad(spectral_fno_s *n, const T *f, const T *Q, int B, cudaStream_t st)
+{
+    const int Bp = (B + 7) / 8 * 8;
+    FNO_TRY(ensure(n, Bp, true));
+    FNO_TRY(forward<T>(n, f, B, Bp, true, st));
+    const long long P = n->P;
+    to_pb_kernel<T><<<dim3((unsigned)((P + 31) / 32), (unsigned)((Bp + 31) / 32)), dim3(32, 8),
+                      0, st>>>(Q, n->s, 2, 1.f / n->sigma, B, Bp, P, n->t);
+    FNO_LAUNCH(cudaMemsetAsync(n->den, 0, sizeof(float) * Bp, st));
+    den_kernel<<<152, 256, 0, st>>>(n->t, n->den, P, Bp);
+    add_launches(2);
+    FNO_LAUNCH(cudaGetLastError());
+    return backward(n, B, Bp, st);
+}
+
+unsigned long long splitmix(unsigned long long &s)
+{
+    unsigned long long z = (s += 0x9E3779B97F4A7C15ULL);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+
+}  // namespace
+
+namespace sbte {
+
+int fno_predict(spectral_fno_s *n, const double *f, double *Q, int B, cudaStream_t st)
+{
+    if (B < 1) return kOk;
+    if (cudaSetDevice(n->device) != cudaSuccess) return kErrCuda;
+    const int Bp = (B + 7) / 8 * 8;
+    FNO_TRY(ensure(n, Bp, n->cap_train));
+    FNO_TRY(forward<double>(n, f, B, Bp, n->cap_train, st));
+    const long long P = n->P;
+    from_pb_kernel<<<dim3((unsigned)((P + 31) / 32), (unsigned)((Bp + 31) / 32)), dim3(32, 8), 0,
+                     st>>>(n->y, n->s, n->sigma, B, Bp, P, Q);
+    add_launches(1);
+    FNO_LAUNCH(cudaGetLastError());
+    return kOk;
+}
+
+int fno_grid_n(const spectral_fno_s *n) { return n->N; }
+
+int rel_l2_device(const double *A, const double *R, long long n3, double *out, cudaStream_t st)
+{
+    fno::rel_l2_kernel<<<1, 512, 0, st>>>(A, R, n3, out);
+    add_launches(1);
+    FNO_LAUNCH(cudaGetLastError());
+    return kOk;
+}
+
+}  // namespace sbte
+
+// ============================================================== C ABI ===
+extern "C" {
+
+int spectral_fno_create(spectral_fno **out, int N, int width, int modes, int layers, int hidden,
+                        unsigned long long seed)
+{
+    if (!out) {
+        set_error(kErrArg, "spectral_fno_create: null handle pointer");
+        return kErrArg;
+    }
+    *out = nullptr;
+    if (N < 4 || N > 32 || width < 8 || width > 64 || width % 8 || modes < 2 || modes > 16 ||
+        modes % 2 || modes > N || layers < 1 || layers > 8 || hidden < 16 || hidden > 128 ||
+        hidden % 16) {
+        set_error(kErrArg,
+                  "spectral_fno_create: unsupported shape N=%d width=%d modes=%d layers=%d "
+                  "hidden=%d (N 4..32, width 8..64 step 8, even modes <= min(16, N), "
+                  "layers 1..8, hidden 16..128 step 16)",
+                  N, width, modes, layers, hidden);
+        return kErrArg;
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        set_error(kErrCuda, "no CUDA device available; the learned operator has no CPU path");
+        return kErrCuda;
+    }
+    auto *n = new spectral_fno_s;
+    cudaGetDevice(&n->device);
+    n->N = N; n->C = width; n->Km = modes; n->L = layers; n->Hd = hidden;
+    n->P = (long long)N * N * N;
+    // mode classes by |m|^2
+    const int Km = modes;
+    std::map<int, int> cls_of;
+    for (int a = 0; a < Km; a++)
+        for (int b = 0; b < Km; b++)
+            for (int c = 0; c < Km; c++) {
+                const int ma = a - Km / 2, mb = b - Km / 2, mc = c - Km / 2;
+                cls_of[ma * ma + mb * mb + mc * mc] = 0;
+            }
+    int nc = 0;
+    for (auto &kv : cls_of) kv.second = nc++;
+    n->ncls = nc;
+    std::vector<int> tab(2 * Km * Km * Km);
+    for (int z = 0; z < 2 * Km * Km * Km; z++) {
+        const int mi = (z / (Km * Km)) / 2, mjk = z % (Km * Km);
+        const int ma = mi - Km / 2, mb = mjk / Km - Km / 2, mc = mjk % Km - Km / 2;
+        tab[z] = cls_of[ma * ma + mb * mb + mc * mc];
+    }
+    // parameter layout
+    const long long C = width;
+    long long o = 0;
+    n->oP = o; o += C;
+    n->obP = o; o += C;
+    for (int l = 0; l < layers; l++) {
+        n->oW[l] = o; o += C * C;
+        n->ob[l] = o; o += C;
+        n->oR[l] = o; o += (long long)nc * C * C;
+    }
+    n->oQ1 = o; o += hidden * C;
+    n->oc1 = o; o += hidden;
+    n->oq2 = o; o += hidden;
+    n->oc2 = o; o += 1;
+    n->nparams = o;
+    // initial values: uniform draws scaled by fan-in, zero biases
+    std::vector<float> h(o, 0.f);
+    unsigned long long st = seed ? seed : 0x5bd1e995ULL;
+    auto uni = [&](double lim) {
+        return (float)(lim * (2.0 * ((splitmix(st) >> 11) * (1.0 / 9007199254740992.0)) - 1.0));
+    };
+    for (long long i = 0; i < C; i++) h[n->oP + i] = uni(1.0);
+    for (int l = 0; l < layers; l++) {
+        for (long long i = 0; i < C * C; i++) h[n->oW[l] + i] = uni(1.0 / std::sqrt((double)C));
+        for (long long i = 0; i < (long long)nc * C * C; i++)
+            h[n->oR[l] + i] = uni(1.0 / std::sqrt((double)C));
+    }
+    for (long long i = 0; i < hidden * C; i++) h[n->oQ1 + i] = uni(1.0 / std::sqrt((double)C));
+    for (long long i = 0; i < hidden; i++) h[n->oq2 + i] = uni(1.0 / std::sqrt((double)hidden));
+    // DFT axis matrices: F[m][n] = e^{-2 pi i m n / N} / N, G[n][m] = e^{+2 pi i m n / N}
+    std::vector<float> Fh(2 * Km * N), Gh(2 * N * Km);
+    for (int m = 0; m < Km; m++)
+        for (int x = 0; x < N; x++) {
+            const int mm = m - Km / 2;
+            const int r = ((mm * x) % N + N) % N;
+            const double th = 2.0 * M_PI * r / N;
+            Fh[m * N + x] = (float)(std::cos(th) / N);
+            Fh[Km * N + m * N + x] = (float)(-std::sin(th) / N);
+            Gh[x * Km + m] = (float)std::cos(th);
+            Gh[N * Km + x * Km + m] = (float)std::sin(th);
+        }
+    auto fail = [&](int rc) {
+        delete n;
+        return rc;
+    };
+    auto up = [&](float **d, const float *src, long long cnt) -> int {
+        if (cudaMalloc((void **)d, sizeof(float) * cnt) != cudaSuccess) {
+            set_error(kErrNoMem, "spectral_fno_create: cudaMalloc failed");
+            return kErrNoMem;
+        }
+        if (src) {
+            if (cudaMemcpy(*d, src, sizeof(float) * cnt, cudaMemcpyHostToDevice) != cudaSuccess) {
+                set_error(kErrCuda, "spectral_fno_create: upload failed");
+                return kErrCuda;
+            }
+        } else if (cudaMemset(*d, 0, sizeof(float) * cnt) != cudaSuccess) {
+            set_error(kErrCuda, "spectral_fno_create: memset failed");
+            return kErrCuda;
+        }
+        return kOk;
+    };
+    int rc;
+    if ((rc = up(&n->params, h.data(), o)) != kOk) return fail(rc);
+    if ((rc = up(&n->grads, nullptr, o)) != kOk) return fail(rc);
+    if ((rc = up(&n->am, nullptr, o)) != kOk) return fail(rc);
+    if ((rc = up(&n->av, nullptr, o)) != kOk) return fail(rc);
+    if ((rc = up(&n->F, Fh.data(), (long long)Fh.size())) != kOk) return fail(rc);
+    if ((rc = up(&n->G, Gh.data(), (long long)Gh.size())) != kOk) return fail(rc);
+    if (cudaMalloc((void **)&n->cls, sizeof(int) * tab.size()) != cudaSuccess ||
+        cudaMemcpy(n->cls, tab.data(), sizeof(int) * tab.size(), cudaMemcpyHostToDevice) !=
+            cudaSuccess) {
+        set_error(kErrNoMem, "spectral_fno_create: class table upload failed");
+        return fail(kErrNoMem);
+    }
+    *out = n;
+    return kOk;
+}
+
+int spectral_fno_destroy(spectral_fno *n)
+{
+    delete n;
+    return kOk;
+}
+
+long long spectral_fno_num_params(spectral_fno *n) { return n ? n->nparams : 0; }
+
+int spectral_fno_num_classes(spectral_fno *n) { return n ? n->ncls : 0; }
+
+int spectral_fno_get_params(spectral_fno *n, float *host)
+{
+    if (!n || !host) {
+        set_error(kErrArg, "spectral_fno_get_params: null argument");
+        return kErrArg;
+    }
+    SBTE_CUDA(cudaMemcpy(host, n->params, sizeof(float) * n->nparams, cudaMemcpyDeviceToHost));
+    return kOk;
+}
+
+int spectral_fno_set_params(spectral_fno *n, const float *host)
+{
+    if (!n || !host) {
+        set_error(kErrArg, "spectral_fno_set_params: null argument");
+        return kErrArg;
+    }
+    SBTE_CUDA(cudaMemcpy(n->params, host, sizeof(float) * n->nparams, cudaMemcpyHostToDevice));
+    SBTE_CUDA(cudaMemset(n->am, 0, sizeof(float) * n->nparams));
+    SBTE_CUDA(cudaMemset(n->av, 0, sizeof(float) * n->nparams));
+    n->adam_t = 0;
+    return kOk;
+}
+
+int spectral_fno_set_output_scale(spectral_fno *n, float sigma)
+{
+    if (!n || !(sigma > 0.f)) {
+        set_error(kErrArg, "spectral_fno_set_output_scale: need a handle and sigma > 0");
+        return kErrArg;
+    }
+    n->sigma = sigma;
+    return kOk;
+}
+
+float spectral_fno_output_scale(spectral_fno *n) { return n ? n->sigma : 0.f; }
+
+int spectral_fno_predict(spectral_fno *n, const double *f_dev, double *Q_dev, int B, void *stream)
+{
+    if (!n || !f_dev || !Q_dev || B < 0) {
+        set_error(kErrArg, "spectral_fno_predict: bad argument");
+        return kErrArg;
+    }
+    return fno_predict(n, f_dev, Q_dev, B, (cudaStream_t)stream);
+}
+
+int spectral_fno_loss_grad(spectral_fno *n, const float *f_dev, const float *Q_dev, int B,
+                           double *loss_out, float *grad_host)
+{
+    if (!n || !f_dev || !Q_dev || B < 1) {
+        set_error(kErrArg, "spectral_fno_loss_grad: bad argument");
+        return kErrArg;
+    }
+    FNO_TRY(loss_and_grad<float>(n, f_dev, Q_dev, B, 0));
+    SBTE_CUDA(cudaDeviceSynchronize());
+    if (loss_out) SBTE_CUDA(cudaMemcpy(loss_out, n->d_loss, sizeof(double), cudaMemcpyDeviceToHost));
+    if (grad_host)
+        SBTE_CUDA(cudaMemcpy(grad_host, n->grads, sizeof(float) * n->nparams,
+                             cudaMemcpyDeviceToHost));
+    return kOk;
+}
+
+int spectral_fno_train_step(spectral_fno *n, const float *f_dev, const float *Q_dev, int B,
+                            float lr, double *loss_out, void *stream)
+{
+    if (!n || !f_dev || !Q_dev || B < 1 || !(lr >= 0.f)) {
+        set_error(kErrArg, "spectral_fno_train_step: bad argument");
+        return kErrArg;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    FNO_TRY(loss_and_grad<float>(n, f_dev, Q_dev, B, st));
+    n->adam_t++;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.f - std::pow(b1, (float)n->adam_t), c2 = 1.f - std::pow(b2, (float)n->adam_t);
+    adam_kernel<<<ew_grid(n->nparams / 8 + 1), kEw, 0, st>>>(n->params, n->grads, n->am, n->av,
+                                                             n->nparams, lr, b1, b2, 1e-8f, c1, c2);
+    add_launches(1);
+    FNO_LAUNCH(cudaGetLastError());
+    if (loss_out) {
+        SBTE_CUDA(cudaMemcpyAsync(loss_out, n->d_loss, sizeof(double), cudaMemcpyDeviceToHost, st));
+        SBTE_CUDA(cudaStreamSynchronize(st));
+    }
+    return kOk;
+}
+
+}  // extern "C"

@@ -1,0 +1,496 @@
+// fno_gemm.cuh -- the BF16 tensor-core GEMMs of the learned collision
+// operator (FP32 accumulation).
+//
+// Every product in the network is one of two shapes once activations sit in
+// the layout [point][channel][instance] (instance index innermost):
+//
+//  * gemm_sa ("small A, streamed B"):  C[m][n] = sum_k A[m][k] B[k][n] with
+//    A a small dense matrix (a DFT axis matrix, a channel-mixing matrix;
+//    M, K <= 128) and B a long stream (N up to 10^8) contiguous along n.
+//    A is read once per CTA from FP32 and rounded to BF16 in shared memory;
+//    B tiles stream through a two-stage cp.async pipeline.
+//  * gemm_nt ("weight gradient"):  C[m][n] += sum_k A[m][k] B[n][k] with
+//    both operands contiguous along k and K huge; K is split over CTAs and
+//    the FP32 partial products are added atomically.
+//
+// Operand views.  A streamed operand element (r, n) (r = the k row of B, or
+// the m row of C) sits at
+//     base + r * s_r + (n / w) * s_blk + (n % w)           (+ im for Im)
+// i.e. n runs over blocks of w contiguous elements (w a multiple of 8).
+// Complex tensors store the real and imaginary parts as two such views im
+// elements apart.  Batches: z -> (z / nz2) * s_z1 + (z % nz2) * s_z2.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace sbte {
+namespace fno {
+
+using bf16 = __nv_bfloat16;
+
+struct StreamView {
+    const void *p;
+    long long s_r, s_blk, w, im, s_z1, s_z2;
+};
+
+enum Epi : int {
+    kEpiBF16 = 0,     // real output, BF16 store
+    kEpiCplxBF16 = 1, // complex output (re at off, im at off + im), BF16 store
+    kEpiF32 = 2,      // real output, FP32 store
+    kEpiAccF32 = 3,   // real output, FP32 C += result
+    kEpiLayer = 4,    // z = acc + bias[m] + addend; zst = z; hout = act(z)
+    kEpiProj = 5,     // y[n] = c2 + sum_m q2[m] gelu(acc[m][n] + c1[m]); ust = acc + c1
+};
+
+struct SaArgs {
+    // A(m, k) = A[a_off + m * sAm + k * sAk] (+ imA for Im), FP32
+    const float *A;
+    long long sAm, sAk, imA;
+    float a_im_sign;       // -1 applies conj(A)
+    const int *a_tab;      // optional: a_off = a_tab[z] * s_atab
+    long long s_atab;
+    int M, K, KP;          // KP: K rounded up to 16
+    StreamView B;          // B(k, n)
+    StreamView C;          // C(m, n)
+    long long Nn;          // n extent (multiple of 8)
+    int nz, nz2;
+    // epilogue operands
+    const float *bias;     // kEpiLayer
+    const float *addend;   // kEpiLayer: FP32, same view as C
+    float *zst;            // kEpiLayer / kEpiProj: optional FP32 store, same view as C
+    bf16 *hout;            // kEpiLayer: BF16 store, same view as C
+    int act;               // kEpiLayer: 1 = GELU
+    const float *c1, *q2;  // kEpiProj
+    const float *c2;       // kEpiProj: one value on the device
+    float *y;              // kEpiProj: y[n]
+    // host-side bounds check: element counts of A, B, C (and of the
+    // epilogue arrays that share C's view); 0 skips the check
+    long long extA, extB, extC;
+    int a_tab_max;  // largest value in a_tab (host-side bounds check)
+};
+
+struct NtArgs {
+    // A(m, k) = A[zA + m * a_m + (k / a_w) * a_blk + k % a_w]; same for B(n, k)
+    const bf16 *A;
+    long long a_m, a_blk, a_w, a_z1, a_z2;
+    const bf16 *B;
+    long long b_n, b_blk, b_w, b_z1, b_z2;
+    float *C;              // C[c_tab ? c_tab[z] * c_tabs : 0 + m * c_m + n]
+    long long c_m;
+    const int *c_tab;
+    long long c_tabs;
+    int M, N;
+    long long K, KC;       // K and the per-CTA chunk (multiples of 32)
+    int nz, nz2;
+    float alpha;
+    long long extA, extB, extC;  // host-side bounds check (element counts)
+};
+
+__device__ __forceinline__ float gelu_f(float x)
+{
+    return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f));
+}
+__device__ __forceinline__ float gelu_grad(float x)
+{
+    return 0.5f * (1.0f + erff(x * 0.70710678118654752f)) +
+           x * 0.39894228040143268f * expf(-0.5f * x * x);
+}
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void cp_async16(void *sdst, const void *gsrc, bool valid)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(smem_addr(sdst)),
+                 "l"(gsrc), "r"(valid ? 16 : 0));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n"); }
+template <int N> __device__ __forceinline__ void cp_async_wait()
+{
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
+}
+__device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const bf16 *p)
+{
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(smem_addr(p)));
+}
+__device__ __forceinline__ void ldsm_x4_t(uint32_t (&r)[4], const bf16 *p)
+{
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(smem_addr(p)));
+}
+__device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0,
+                                         uint32_t b1)
+{
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, "
+        "{%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ long long view_off(const StreamView &v, long long r, long long n)
+{
+    return r * v.s_r + (n / v.w) * v.s_blk + (n % v.w);
+}
+__device__ __forceinline__ long long zoff(long long z, int nz2, long long s1, long long s2)
+{
+    return (z / nz2) * s1 + (z % nz2) * s2;
+}
+
+// ------------------------------------------------------------ gemm_sa ---
+// MT x BN output tile per work item; WM x WN warps; AC / BC: A / B complex.
+// Complex output (kEpiCplxBF16) holds re and im accumulators; a complex x
+// complex product with a real epilogue keeps only the real part.
+template <int MT, int BN, int WM, int WN, bool AC, bool BC, int EPI>
+__global__ void __launch_bounds__(WM *WN * 32) gemm_sa_kernel(const SaArgs a)
+{
+    constexpr int NTH = WM * WN * 32;
+    constexpr int WR = MT / WM, WC = BN / WN;
+    constexpr int FM = WR / 16, FN = WC / 8;
+    static_assert(WR % 16 == 0 && WC % 16 == 0, "warp tile");
+    constexpr bool CO = (EPI == kEpiCplxBF16);
+    constexpr bool IM = CO || (AC && !BC);  // imaginary accumulator needed
+    static_assert(!(AC && !BC) || CO, "complex A x real B gives a complex result");
+
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int KP = a.KP, ap = KP + 8, bp = BN + 8;
+    bf16 *sAr = reinterpret_cast<bf16 *>(smem_raw);
+    bf16 *sAi = sAr + MT * ap;
+    bf16 *sAn = sAi + MT * ap;
+    bf16 *sB = sAr + (AC ? 3 : 1) * MT * ap;
+    const int tileB = KP * bp;                 // one part of one stage
+    constexpr int PARTS = BC ? 2 : 1;
+    float *red = reinterpret_cast<float *>(sB + 2 * PARTS * tileB);  // kEpiProj: [WM][BN]
+
+    const long long ntiles = (a.Nn + BN - 1) / BN;
+    const long long total = ntiles * a.nz;
+    long long item = blockIdx.x;
+    if (item >= total) return;
+
+    const bf16 *Bb = static_cast<const bf16 *>(a.B.p);
+    auto issue = [&](long long it, int stage) {
+        const long long z = it / ntiles;
+        const long long n0 = (it % ntiles) * BN;
+        const long long zb = zoff(z, a.nz2, a.B.s_z1, a.B.s_z2);
+        constexpr int CH = BN / 8;
+        for (int c = threadIdx.x; c < KP * CH; c += NTH) {
+            const int r = c / CH, cn = c % CH;
+            const long long n = n0 + cn * 8;
+            const bool ok = (r < a.K) && (n < a.Nn);
+            const long long off = ok ? zb + view_off(a.B, r, n) : 0;
+#pragma unroll
+            for (int part = 0; part < PARTS; part++) {
+                bf16 *dst = sB + (stage * PARTS + part) * tileB + r * bp + cn * 8;
+                cp_async16(dst, Bb + off + (part ? a.B.im : 0), ok);
+            }
+        }
+    };
+
+    issue(item, 0);
+    cp_async_commit();
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int wm = warp / WN, wn = warp % WN;
+    const int g = lane >> 2, t = lane & 3;
+    long long cur_z = -1;
+    int stage = 0;
+    for (; item < total; item += gridDim.x, stage ^= 1) {
+        const long long nxt = item + gridDim.x;
+        if (nxt < total) issue(nxt, stage ^ 1);
+        cp_async_commit();
+        const long long z = item / ntiles;
+        const long long n0 = (item % ntiles) * BN;
+        if (cur_z < 0 || (a.a_tab && z != cur_z)) {
+            __syncthreads();
+            const long long aoff = a.a_tab ? (long long)a.a_tab[z] * a.s_atab : 0;
+            for (int e = threadIdx.x; e < MT * KP; e += NTH) {
+                const int m = e / KP, k = e % KP;
+                float re = 0.f, im = 0.f;
+                if (m < a.M && k < a.K) {
+                    const float *src = a.A + aoff + m * a.sAm + k * a.sAk;
+                    re = src[0];
+                    if (AC) im = a.a_im_sign * src[a.imA];
+                }
+                sAr[m * ap + k] = __float2bfloat16_rn(re);
+                if (AC) {
+                    sAi[m * ap + k] = __float2bfloat16_rn(im);
+                    sAn[m * ap + k] = __float2bfloat16_rn(-im);
+                }
+            }
+            cur_z = z;
+        }
+        cp_async_wait<1>();
+        __syncthreads();
+
+        float accR[FM][FN][4], accI[IM ? FM : 1][IM ? FN : 1][4];
+#pragma unroll
+        for (int i = 0; i < FM; i++)
+#pragma unroll
+            for (int j = 0; j < FN; j++)
+#pragma unroll
+                for (int r = 0; r < 4; r++) {
+                    accR[i][j][r] = 0.f;
+                    if (IM) accI[IM ? i : 0][IM ? j : 0][r] = 0.f;
+                }
+        const bf16 *sBr = sB + (stage * PARTS) * tileB;
+        const bf16 *sBi = sBr + tileB;
+        for (int kk = 0; kk < KP; kk += 16) {
+            uint32_t ar[FM][4], ai[AC ? FM : 1][4], an[AC ? FM : 1][4];
+#pragma unroll
+            for (int fm = 0; fm < FM; fm++) {
+                const int row = wm * WR + fm * 16 + (lane & 15);
+                const int col = kk + (lane >> 4) * 8;
+                ldsm_x4(ar[fm], sAr + row * ap + col);
+                if (AC) {
+                    ldsm_x4(ai[AC ? fm : 0], sAi + row * ap + col);
+                    if (BC) ldsm_x4(an[AC ? fm : 0], sAn + row * ap + col);
+                }
+            }
+#pragma unroll
+            for (int f2 = 0; f2 < FN / 2; f2++) {
+                uint32_t br[4], bi[4];
+                const int krow = kk + (lane & 15);
+                const int ncol = wn * WC + f2 * 16 + (lane >> 4) * 8;
+                ldsm_x4_t(br, sBr + krow * bp + ncol);
+                if (BC) ldsm_x4_t(bi, sBi + krow * bp + ncol);
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const int fn = f2 * 2 + h;
+#pragma unroll
+                    for (int fm = 0; fm < FM; fm++) {
+                        if (!AC) {
+                            mma16816(accR[fm][fn], ar[fm], br[2 * h], br[2 * h + 1]);
+                        } else if (!BC) {
+                            mma16816(accR[fm][fn], ar[fm], br[2 * h], br[2 * h + 1]);
+                            mma16816(accI[IM ? fm : 0][IM ? fn : 0], ai[AC ? fm : 0], br[2 * h],
+                                     br[2 * h + 1]);
+                        } else {
+                            mma16816(accR[fm][fn], ar[fm], br[2 * h], br[2 * h + 1]);
+                            mma16816(accR[fm][fn], an[AC ? fm : 0], bi[2 * h], bi[2 * h + 1]);
+                            if (CO) {
+                                mma16816(accI[IM ? fm : 0][IM ? fn : 0], ar[fm], bi[2 * h],
+                                         bi[2 * h + 1]);
+                                mma16816(accI[IM ? fm : 0][IM ? fn : 0], ai[AC ? fm : 0],
+                                         br[2 * h], br[2 * h + 1]);
+                            }
+                        }
+                    }
+                }
+            }
+        }
+
+        // ---- epilogue
+        const long long zc = zoff(z, a.nz2, a.C.s_z1, a.C.s_z2);
+        if (EPI == kEpiProj) {
+            float part[FN][2];
+#pragma unroll
+            for (int fn = 0; fn < FN; fn++) part[fn][0] = part[fn][1] = 0.f;
+#pragma unroll
+            for (int fm = 0; fm < FM; fm++)
+#pragma unroll
+                for (int hh = 0; hh < 2; hh++) {
+                    const int m = wm * WR + fm * 16 + g + hh * 8;
+                    if (m >= a.M) continue;
+                    const float c1 = a.c1[m], q2 = a.q2[m];
+#pragma unroll
+                    for (int fn = 0; fn < FN; fn++) {
+                        const long long n = n0 + wn * WC + fn * 8 + 2 * t;
+                        const float u0 = accR[fm][fn][2 * hh] + c1;
+                        const float u1 = accR[fm][fn][2 * hh + 1] + c1;
+                        if (a.zst && n < a.Nn) {
+                            float *dst = a.zst + zc + view_off(a.C, m, n);
+                            *reinterpret_cast<float2 *>(dst) = make_float2(u0, u1);
+                        }
+                        part[fn][0] += q2 * gelu_f(u0);
+                        part[fn][1] += q2 * gelu_f(u1);
+                    }
+                }
+#pragma unroll
+            for (int fn = 0; fn < FN; fn++)
+#pragma unroll
+                for (int c = 0; c < 2; c++) {
+                    float v = part[fn][c];
+                    v += __shfl_xor_sync(0xffffffffu, v, 4);
+                    v += __shfl_xor_sync(0xffffffffu, v, 8);
+                    v += __shfl_xor_sync(0xffffffffu, v, 16);
+                    part[fn][c] = v;
+                }
+            if (g == 0) {
+#pragma unroll
+                for (int fn = 0; fn < FN; fn++) {
+                    red[wm * BN + wn * WC + fn * 8 + 2 * t] = part[fn][0];
+                    red[wm * BN + wn * WC + fn * 8 + 2 * t + 1] = part[fn][1];
+                }
+            }
+            __syncthreads();
+            for (int c = threadIdx.x; c < BN; c += NTH) {
+                const long long n = n0 + c;
+                if (n < a.Nn) {
+                    float s = a.c2[0];
+#pragma unroll
+                    for (int w = 0; w < WM; w++) s += red[w * BN + c];
+                    a.y[n] = s;
+                }
+            }
+        } else {
+#pragma unroll
+            for (int fm = 0; fm < FM; fm++)
+#pragma unroll
+                for (int hh = 0; hh < 2; hh++) {
+                    const int m = wm * WR + fm * 16 + g + hh * 8;
+                    if (m >= a.M) continue;
+#pragma unroll
+                    for (int fn = 0; fn < FN; fn++) {
+                        const long long n = n0 + wn * WC + fn * 8 + 2 * t;
+                        if (n >= a.Nn) continue;
+                        const long long off = zc + view_off(a.C, m, n);
+                        const float v0 = accR[fm][fn][2 * hh], v1 = accR[fm][fn][2 * hh + 1];
+                        if (EPI == kEpiBF16) {
+                            *reinterpret_cast<__nv_bfloat162 *>(static_cast<bf16 *>(
+                                const_cast<void *>(a.C.p)) + off) = __floats2bfloat162_rn(v0, v1);
+                        } else if (EPI == kEpiCplxBF16) {
+                            bf16 *c = static_cast<bf16 *>(const_cast<void *>(a.C.p));
+                            *reinterpret_cast<__nv_bfloat162 *>(c + off) =
+                                __floats2bfloat162_rn(v0, v1);
+                            *reinterpret_cast<__nv_bfloat162 *>(c + off + a.C.im) =
+                                __floats2bfloat162_rn(accI[IM ? fm : 0][IM ? fn : 0][2 * hh],
+                                                      accI[IM ? fm : 0][IM ? fn : 0][2 * hh + 1]);
+                        } else if (EPI == kEpiF32) {
+                            *reinterpret_cast<float2 *>(static_cast<float *>(
+                                const_cast<void *>(a.C.p)) + off) = make_float2(v0, v1);
+                        } else if (EPI == kEpiAccF32) {
+                            float2 *c = reinterpret_cast<float2 *>(
+                                static_cast<float *>(const_cast<void *>(a.C.p)) + off);
+                            float2 o = *c;
+                            o.x += v0;
+                            o.y += v1;
+                            *c = o;
+                        } else if (EPI == kEpiLayer) {
+                            const float bm = a.bias[m];
+                            const float2 ad = *reinterpret_cast<const float2 *>(a.addend + off);
+                            const float z0 = v0 + bm + ad.x, z1 = v1 + bm + ad.y;
+                            if (a.zst)
+                                *reinterpret_cast<float2 *>(a.zst + off) = make_float2(z0, z1);
+                            const float h0 = a.act ? gelu_f(z0) : z0;
+                            const float h1 = a.act ? gelu_f(z1) : z1;
+                            *reinterpret_cast<__nv_bfloat162 *>(a.hout + off) =
+                                __floats2bfloat162_rn(h0, h1);
+                        }
+                    }
+                }
+        }
+        __syncthreads();
+    }
+    cp_async_wait<0>();
+}
+
+template <int MT, int BN, int WM, int WN, bool AC, bool BC, int EPI>
+inline size_t gemm_sa_smem(int KP)
+{
+    size_t a = (size_t)(AC ? 3 : 1) * MT * (KP + 8) * 2;
+    size_t b = (size_t)2 * (BC ? 2 : 1) * KP * (BN + 8) * 2;
+    size_t r = (EPI == kEpiProj) ? (size_t)WM * BN * 4 : 0;
+    return a + b + r;
+}
+
+// ------------------------------------------------------------ gemm_nt ---
+template <int MT, int NT, int WM, int WN>
+__global__ void __launch_bounds__(WM *WN * 32) gemm_nt_kernel(const NtArgs a)
+{
+    constexpr int NTH = WM * WN * 32, BK = 32, P = BK + 8;
+    constexpr int WR = MT / WM, WC = NT / WN;
+    constexpr int FM = WR / 16, FN = WC / 8;
+    static_assert(WR % 16 == 0 && WC % 16 == 0, "warp tile");
+    __shared__ __align__(16) bf16 sA[2][MT * P];
+    __shared__ __align__(16) bf16 sB[2][NT * P];
+
+    const long long nchunks = (a.K + a.KC - 1) / a.KC;
+    const long long total = nchunks * a.nz;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int wm = warp / WN, wn = warp % WN;
+    const int g = lane >> 2, t = lane & 3;
+
+    for (long long item = blockIdx.x; item < total; item += gridDim.x) {
+        const long long z = item / nchunks;
+        const long long k0 = (item % nchunks) * a.KC;
+        const long long k1 = min(k0 + a.KC, a.K);
+        const long long zA = zoff(z, a.nz2, a.a_z1, a.a_z2);
+        const long long zB = zoff(z, a.nz2, a.b_z1, a.b_z2);
+        auto issue = [&](long long kt, int st) {
+            for (int c = threadIdx.x; c < (MT + NT) * (BK / 8); c += NTH) {
+                const int row = c / (BK / 8), ck = c % (BK / 8);
+                const long long k = kt + ck * 8;
+                if (row < MT) {
+                    const bool ok = row < a.M && k < k1;
+                    const long long off =
+                        ok ? zA + row * a.a_m + (k / a.a_w) * a.a_blk + (k % a.a_w) : 0;
+                    cp_async16(&sA[st][row * P + ck * 8], a.A + off, ok);
+                } else {
+                    const int n = row - MT;
+                    const bool ok = n < a.N && k < k1;
+                    const long long off =
+                        ok ? zB + n * a.b_n + (k / a.b_w) * a.b_blk + (k % a.b_w) : 0;
+                    cp_async16(&sB[st][n * P + ck * 8], a.B + off, ok);
+                }
+            }
+        };
+        float acc[FM][FN][4];
+#pragma unroll
+        for (int i = 0; i < FM; i++)
+#pragma unroll
+            for (int j = 0; j < FN; j++)
+#pragma unroll
+                for (int r = 0; r < 4; r++) acc[i][j][r] = 0.f;
+        int st = 0;
+        issue(k0, 0);
+        cp_async_commit();
+        for (long long kt = k0; kt < k1; kt += BK, st ^= 1) {
+            if (kt + BK < k1) issue(kt + BK, st ^ 1);
+            cp_async_commit();
+            cp_async_wait<1>();
+            __syncthreads();
+#pragma unroll
+            for (int kk = 0; kk < BK; kk += 16) {
+                uint32_t af[FM][4];
+#pragma unroll
+                for (int fm = 0; fm < FM; fm++)
+                    ldsm_x4(af[fm], &sA[st][(wm * WR + fm * 16 + (lane & 15)) * P + kk +
+                                            (lane >> 4) * 8]);
+#pragma unroll
+                for (int f2 = 0; f2 < FN / 2; f2++) {
+                    uint32_t bq[4];
+                    const int nrow = wn * WC + f2 * 16 + (lane & 7) + (lane >> 4) * 8;
+                    ldsm_x4(bq, &sB[st][nrow * P + kk + ((lane >> 3) & 1) * 8]);
+#pragma unroll
+                    for (int fm = 0; fm < FM; fm++) {
+                        mma16816(acc[fm][2 * f2], af[fm], bq[0], bq[1]);
+                        mma16816(acc[fm][2 * f2 + 1], af[fm], bq[2], bq[3]);
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        cp_async_wait<0>();
+        const long long cb = a.c_tab ? (long long)a.c_tab[z] * a.c_tabs : 0;
+#pragma unroll
+        for (int fm = 0; fm < FM; fm++)
+#pragma unroll
+            for (int fn = 0; fn < FN; fn++)
+#pragma unroll
+                for (int r = 0; r < 4; r++) {
+                    const int m = wm * WR + fm * 16 + g + (r >> 1) * 8;
+                    const int n = wn * WC + fn * 8 + 2 * t + (r & 1);
+                    if (m < a.M && n < a.N)
+                        atomicAdd(a.C + cb + m * a.c_m + n, a.alpha * acc[fm][fn][r]);
+                }
+    }
+}
+
+}  // namespace fno
+}  // namespace sbte

@@ -1,0 +1,98 @@
+"""CPU checks of the learned operator's oracle (oracle/fno_oracle.py).
+
+* Its hand-derived gradients equal central finite differences of its own
+  loss, FP64, every parameter of a small network.
+* With every mode kept, the truncated transform pair is the identity, so the
+  spectral layer with R = identity returns its input.
+* BF16 rounding is round-to-nearest-even on known values.
+* The parameter layout matches the library's count for the same shape.
+"""
+import numpy as np
+import pytest
+
+from oracle import fno_oracle as fo
+
+
+def _small(rounding=False, seed=0, spec=None):
+    spec = spec or fo.Spec(N=4, C=3, Km=2, L=2, Hd=4)
+    _, n = spec.layout()
+    rng = np.random.default_rng(seed)
+    theta = rng.uniform(-0.6, 0.6, n)
+    return spec, theta, fo.Net(spec, theta, sigma=0.7, rounding=rounding)
+
+
+def _data(spec, B, seed):
+    rng = np.random.default_rng(seed)
+    N = spec.N
+    f = rng.uniform(0.1, 1.0, (B, N, N, N))
+    Q = rng.normal(size=(B, N, N, N))
+    return f, Q
+
+
+def test_gradients_match_finite_differences():
+    spec, theta, net = _small()
+    f, Q = _data(spec, 2, 1)
+    loss, g = net.loss_grad(f, Q)
+    ga = fo.pack(spec, g)
+    eps = 1e-6
+    gn = np.empty_like(theta)
+    for i in range(theta.size):
+        tp, tm = theta.copy(), theta.copy()
+        tp[i] += eps
+        tm[i] -= eps
+        lp, _ = fo.Net(spec, tp, sigma=0.7).loss_grad(f, Q)
+        lm, _ = fo.Net(spec, tm, sigma=0.7).loss_grad(f, Q)
+        gn[i] = (lp - lm) / (2 * eps)
+    assert loss > 0
+    err = np.abs(ga - gn).max() / np.abs(gn).max()
+    assert err < 1e-6, err
+
+
+def test_gradients_with_odd_modes_and_three_layers():
+    spec = fo.Spec(N=6, C=2, Km=4, L=3, Hd=3)
+    spec, theta, net = _small(spec=spec, seed=3)
+    f, Q = _data(spec, 1, 2)
+    _, g = net.loss_grad(f, Q)
+    ga = fo.pack(spec, g)
+    rng = np.random.default_rng(5)
+    eps = 1e-6
+    for i in rng.choice(theta.size, 40, replace=False):
+        tp, tm = theta.copy(), theta.copy()
+        tp[i] += eps
+        tm[i] -= eps
+        lp, _ = fo.Net(spec, tp, sigma=0.7).loss_grad(f, Q)
+        lm, _ = fo.Net(spec, tm, sigma=0.7).loss_grad(f, Q)
+        gn = (lp - lm) / (2 * eps)
+        assert abs(ga[i] - gn) <= 1e-6 * max(1.0, abs(gn)), (i, ga[i], gn)
+
+
+def test_full_mode_transform_pair_is_identity():
+    spec = fo.Spec(N=6, C=2, Km=6, L=1, Hd=2)
+    _, n = spec.layout()
+    net = fo.Net(spec, np.zeros(n))
+    h = np.random.default_rng(0).normal(size=(2, 6, 6, 6, 2))
+    back = net.inv_modes(net.fwd_modes(h))
+    assert np.abs(back - h).max() < 1e-6  # the matrices hold float32 cos/sin
+
+
+def test_bf16_rounding():
+    x = np.array([1.0, 1.00390625, 1.005859375, -3.0e-3, 0.0])
+    y = fo.bf16(x)
+    assert y[0] == 1.0
+    assert y[1] == 1.0          # tie -> even mantissa
+    assert y[2] == 1.0078125    # above the tie
+    assert abs(y[3] + 3.0e-3) <= 3.0e-3 * 2 ** -8
+    assert y[4] == 0.0
+
+
+def test_layout_matches_library_count(lib_built):
+    import spectralbte_gb300 as sb
+    spec = fo.Spec(N=32, C=64, Km=12, L=4, Hd=128)
+    _, n = spec.layout()
+    cls, ncls = spec.classes()
+    # the count the library computes for the same shape (no GPU needed)
+    C, Hd, L = 64, 128, 4
+    want = 2 * C + L * (C * C + C + ncls * C * C) + Hd * C + 2 * Hd + 1
+    assert n == want
+    assert cls.shape == (12, 12, 12) and cls.max() == ncls - 1
+    assert "spectral_fno_create" in sb.declared_symbols()
