@@ -257,19 +257,25 @@ int spectral_fft3d_noalloc(int N, double L_v, const double *v,
    lift to `width` channels, `layers` spectral layers on the lowest
    `modes`^3 Fourier modes (weights shared by modes of equal |m|^2) plus a
    pointwise channel mix and GELU, then a two-layer pointwise projection
-   with `hidden` channels.  f is scaled by its maximum s and the output by
-   s^2 times the output scale (Q is bilinear in f).  All GEMMs run on BF16
-   tensor cores with FP32 accumulation; parameters are FP32.  Shapes:
-   N 4..32, width 8..64 (multiple of 8), even modes <= min(16, N), layers
-   1..8, hidden 16..128 (multiple of 16). */
+   with `hidden` channels.  kind 0 applies GELU after every spectral layer
+   but the last and reads out y = q2 . gelu(u) + c2; kind 1 keeps the layers
+   linear and reads out the quadratic form y = c2 + sum_e q2[e] u_l(e) u_r(e)
+   over hidden/2 channel pairs (rows 16 (e/8) + e%8 and that + 8), the form
+   of a separable approximation of the collision kernel.  f is scaled by its
+   maximum s and the output by s^2 times the output scale (Q is bilinear in
+   f).  All GEMMs run on BF16 tensor cores with FP32 accumulation;
+   parameters are FP32.  Shapes: N 4..32, width 8..64 (multiple of 8), even
+   modes <= min(16, N), layers 1..8, hidden 16..128 (multiple of 16). */
 typedef struct spectral_fno_s spectral_fno;
 int spectral_fno_create(spectral_fno **net, int N, int width, int modes,
-                        int layers, int hidden, unsigned long long seed);
+                        int layers, int hidden, int kind,
+                        unsigned long long seed);
 int spectral_fno_destroy(spectral_fno *net);
 long long spectral_fno_num_params(spectral_fno *net);
 int spectral_fno_num_classes(spectral_fno *net);
 /* Flat FP32 parameter vector: P, bP, then per layer W (width x width), b,
-   R (classes x width x width), then Q1 (hidden x width), c1, q2, c2.
+   R (classes x width x width), then Q1 (hidden x width), c1, q2 (hidden, or
+   hidden/2 for kind 1), c2.
    set_params also resets the optimiser state. */
 int spectral_fno_get_params(spectral_fno *net, float *host);
 int spectral_fno_set_params(spectral_fno *net, const float *host);
@@ -278,8 +284,13 @@ float spectral_fno_output_scale(spectral_fno *net);
 /* Network output Q[b][pos] (FP64 device) for f[b][pos], no projection. */
 int spectral_fno_predict(spectral_fno *net, const double *f_dev, double *Q_dev,
                          int B, void *stream);
-/* Mean over instances of |y - Q~|^2 / |Q~|^2 (Q~ = Q / (s^2 sigma)) and its
-   gradient (host, nparams floats) for FP32 device data f, Q [B][N^3]. */
+/* Loss floor eps >= 0 (default 0): the training loss of each instance is
+   |y - Q~|^2 / (|Q~|^2 + eps * mean over the batch of |Q~|^2), so that
+   near-equilibrium instances with |Q~| -> 0 do not dominate. */
+int spectral_fno_set_loss_floor(spectral_fno *net, float eps);
+/* Mean over instances of |y - Q~|^2 / |Q~|^2 (Q~ = Q / (s^2 sigma), with the
+   loss floor above) and its gradient (host, nparams floats) for FP32 device
+   data f, Q [B][N^3]. */
 int spectral_fno_loss_grad(spectral_fno *net, const float *f_dev,
                            const float *Q_dev, int B, double *loss_out,
                            float *grad_host);

@@ -51,6 +51,13 @@ class Spec:
     Km: int
     L: int
     Hd: int
+    kind: int = 0  # 0: GELU layers and readout; 1: linear layers, bilinear readout
+
+    def pairs(self):
+        """Left and right rows of each readout pair (kind 1): 16 (e/8) + e%8 and +8."""
+        e = np.arange(self.Hd // 2)
+        left = 16 * (e // 8) + e % 8
+        return left, left + 8
 
     def classes(self):
         """Class index of each mode (a, b, c) by |m|^2, in increasing order."""
@@ -77,7 +84,7 @@ class Spec:
             put(f"R{l}", nc * C * C)
         put("Q1", Hd * C)
         put("c1", Hd)
-        put("q2", Hd)
+        put("q2", Hd // 2 if self.kind == 1 else Hd)
         put("c2", 1)
         return off, o
 
@@ -87,7 +94,8 @@ def unpack(spec: Spec, theta: np.ndarray) -> dict:
     assert theta.size == n, (theta.size, n)
     _, nc = spec.classes()
     C, Hd = spec.C, spec.Hd
-    shapes = {"P": (C,), "bP": (C,), "Q1": (Hd, C), "c1": (Hd,), "q2": (Hd,), "c2": (1,)}
+    nq = Hd // 2 if spec.kind == 1 else Hd
+    shapes = {"P": (C,), "bP": (C,), "Q1": (Hd, C), "c1": (Hd,), "q2": (nq,), "c2": (1,)}
     for l in range(spec.L):
         shapes[f"W{l}"] = (C, C)
         shapes[f"b{l}"] = (C,)
@@ -175,12 +183,16 @@ class Net:
             Y = self.mix(p[f"R{l}"], X)
             S = self.inv_modes(Y)
             z = np.einsum("dc,bijkc->bijkd", self.mat(p[f"W{l}"]), h) + p[f"b{l}"] + S
-            h = self.r(gelu(z) if l < sp.L - 1 else z)
+            h = self.r(gelu(z) if (sp.kind == 0 and l < sp.L - 1) else z)
             cache["X"].append(X)
             cache["z"].append(z)
             cache["h"].append(h)
         u = np.einsum("ec,bijkc->bijke", self.mat(p["Q1"]), h) + p["c1"]
-        y = gelu(u) @ p["q2"] + p["c2"][0]
+        if sp.kind == 1:
+            lft, rgt = sp.pairs()
+            y = (u[..., lft] * u[..., rgt]) @ p["q2"] + p["c2"][0]
+        else:
+            y = gelu(u) @ p["q2"] + p["c2"][0]
         cache["u"] = u
         return y, cache
 
@@ -188,23 +200,32 @@ class Net:
         y, c = self.forward(f)
         return y * (c["s"] ** 2 * self.sigma)[:, None, None, None]
 
-    def loss_grad(self, f, Q):
-        """Mean over instances of |y - t|^2/|t|^2, t = Q / (s^2 sigma), and
-        its gradient as a dict of arrays shaped like the parameters."""
+    def loss_grad(self, f, Q, floor: float = 0.0):
+        """Mean over instances of |y - t|^2/(|t|^2 + floor mean_b |t_b|^2),
+        t = Q / (s^2 sigma), and its gradient as a dict of arrays shaped like
+        the parameters."""
         p, sp = self.p, self.spec
         B = f.shape[0]
         y, c = self.forward(f)
         t = np.asarray(Q, dtype=np.float64).reshape(y.shape) / \
             (c["s"] ** 2 * self.sigma)[:, None, None, None]
         den = (t.reshape(B, -1) ** 2).sum(axis=1)
+        den = den + floor * den.mean()
         r = y - t
         loss = float(((r.reshape(B, -1) ** 2).sum(axis=1) / den).sum() / B)
         dy = 2.0 * r / (den * B)[:, None, None, None]
         g = {k: np.zeros_like(v) for k, v in p.items()}
         g["c2"][0] = dy.sum()
         u = c["u"]
-        g["q2"] = np.einsum("bijk,bijke->e", dy, gelu(u))
-        du = dy[..., None] * p["q2"] * gelu_grad(u)
+        if sp.kind == 1:
+            lft, rgt = sp.pairs()
+            g["q2"] = np.einsum("bijk,bijke->e", dy, u[..., lft] * u[..., rgt])
+            du = np.zeros_like(u)
+            du[..., lft] = dy[..., None] * p["q2"] * u[..., rgt]
+            du[..., rgt] = dy[..., None] * p["q2"] * u[..., lft]
+        else:
+            g["q2"] = np.einsum("bijk,bijke->e", dy, gelu(u))
+            du = dy[..., None] * p["q2"] * gelu_grad(u)
         g["c1"] = du.sum(axis=(0, 1, 2, 3))
         du = self.r(du)
         hL = c["h"][sp.L]
@@ -212,7 +233,7 @@ class Net:
         dh = np.einsum("ec,bijke->bijkc", self.mat(p["Q1"]), du)
         n3 = sp.N ** 3
         for l in range(sp.L - 1, -1, -1):
-            dz = dh * gelu_grad(c["z"][l]) if l < sp.L - 1 else dh
+            dz = dh * gelu_grad(c["z"][l]) if (sp.kind == 0 and l < sp.L - 1) else dh
             g[f"b{l}"] = dz.sum(axis=(0, 1, 2, 3))
             dz = self.r(dz)
             hl = c["h"][l]

@@ -146,7 +146,7 @@ def lib() -> C.CDLL:
                                         C.POINTER(C.c_void_p), C.POINTER(C.c_int), i, v]),
         "spectral_plan_conv_time": (i, [v, _dp, C.POINTER(C.c_int)]),
         # learned operator
-        "spectral_fno_create": (i, [pp, i, i, i, i, i, C.c_ulonglong]),
+        "spectral_fno_create": (i, [pp, i, i, i, i, i, i, C.c_ulonglong]),
         "spectral_fno_destroy": (i, [v]),
         "spectral_fno_num_params": (C.c_longlong, [v]),
         "spectral_fno_num_classes": (i, [v]),
@@ -154,6 +154,7 @@ def lib() -> C.CDLL:
         "spectral_fno_set_params": (i, [v, C.POINTER(C.c_float)]),
         "spectral_fno_set_output_scale": (i, [v, C.c_float]),
         "spectral_fno_output_scale": (C.c_float, [v]),
+        "spectral_fno_set_loss_floor": (i, [v, C.c_float]),
         "spectral_fno_predict": (i, [v, v, v, i, v]),
         "spectral_fno_loss_grad": (i, [v, v, v, i, _dp, C.POINTER(C.c_float)]),
         "spectral_fno_train_step": (i, [v, v, v, i, C.c_float, _dp, v]),
@@ -472,12 +473,13 @@ class FourierOperator:
     and backward kernels."""
 
     def __init__(self, N: int, width: int = 64, modes: int = 12, layers: int = 4,
-                 hidden: int = 128, seed: int = 1):
+                 hidden: int = 128, seed: int = 1, kind: int = 0):
         self.L = lib()
         self.N, self.n3 = N, N ** 3
         self.width, self.modes, self.layers, self.hidden = width, modes, layers, hidden
+        self.kind = kind
         h = C.c_void_p()
-        _check(self.L.spectral_fno_create(C.byref(h), N, width, modes, layers, hidden,
+        _check(self.L.spectral_fno_create(C.byref(h), N, width, modes, layers, hidden, kind,
                                           int(seed)), "spectral_fno_create")
         self.h = h
         self.nparams = int(self.L.spectral_fno_num_params(h))
@@ -515,6 +517,9 @@ class FourierOperator:
     def output_scale(self, sigma: float):
         _check(self.L.spectral_fno_set_output_scale(self.h, float(sigma)), "fno_set_output_scale")
 
+    def set_loss_floor(self, eps: float):
+        _check(self.L.spectral_fno_set_loss_floor(self.h, float(eps)), "fno_set_loss_floor")
+
     def predict(self, f, Q, B: int, stream: int = 0):
         """Network output (FP64 device) for f (FP64 device), no projection."""
         _check(self.L.spectral_fno_predict(self.h, _ptr(f), _ptr(Q), B, _stream(stream)),
@@ -539,13 +544,14 @@ class FourierOperator:
 
     def save(self, path: str):
         np.savez(path, theta=self.get_params(), sigma=self.output_scale,
-                 shape=np.array([self.N, self.width, self.modes, self.layers, self.hidden]))
+                 shape=np.array([self.N, self.width, self.modes, self.layers, self.hidden,
+                                 self.kind]))
 
     @classmethod
     def load(cls, path: str) -> "FourierOperator":
         d = np.load(path)
-        N, width, modes, layers, hidden = (int(x) for x in d["shape"])
-        net = cls(N, width, modes, layers, hidden)
+        N, width, modes, layers, hidden, kind = (int(x) for x in d["shape"])
+        net = cls(N, width, modes, layers, hidden, kind=kind)
         net.set_params(d["theta"])
         net.output_scale = float(d["sigma"])
         return net

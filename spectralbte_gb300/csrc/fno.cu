@@ -9,6 +9,11 @@
 //   z_l    = W_l h_l + b_l + S_l h_l,  h_{l+1} = gelu(z_l)  (no gelu after the last layer)
 //   S_l h  = Re sum_m e^{+i theta(m,p)} R_l[|m|^2] (N^-3 sum_p' e^{-i theta(m,p')} h(p'))
 //   u      = Q1 h_L + c1,   y = q2 . gelu(u) + c2,   Q = s^2 sigma y
+// The bilinear kind (kind 1) drops the GELU of the spectral layers and reads
+// out y = c2 + sum_e q2[e] u[l(e)] u[r(e)] over row pairs l(e) = 16 (e / 8)
+// + e % 8, r(e) = l(e) + 8: y is then a quadratic form in x, as Q is in f,
+// with the form sum_e (K_e * f)(v) (K'_e * f)(v) of a separable
+// approximation of the collision kernel in Fourier space.
 // theta(m, p) = 2 pi m.p / N over the lowest Km^3 modes m in [-Km/2, Km/2)^3.
 // The spectral weights are shared by all modes of equal |m|^2 (the collision
 // operator is isotropic) and are real.  Training minimises the mean over
@@ -222,6 +227,45 @@ __global__ void proj_bwd_kernel(const float *__restrict__ U, const float *__rest
     a2.flush(dc1, Hd);
 }
 
+// Bilinear readout backward: for row r with partner r ^ 8 and pair
+// e = 8 (r / 16) + r % 8, dU_r = dy q2[e] u_{r^8}; dc1[r] += dU_r;
+// dq2[e] += dy u_l u_r (counted on the left row).
+__global__ void proj_bwd_bil_kernel(const float *__restrict__ U, const float *__restrict__ dy,
+                                    const float *__restrict__ q2, bf16 *__restrict__ dU,
+                                    float *dq2, float *dc1, long long P, int Hd, int Bp)
+{
+    __shared__ float s1[64], s2[128];
+    ChanAcc<64> a1;
+    ChanAcc<128> a2;
+    a1.init(s1, Hd / 2);
+    a2.init(s2, Hd);
+    const long long n8 = P * Hd * Bp / 8;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n8;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long e = i * 8;
+        const long long p = e / ((long long)Hd * Bp);
+        const int r = (int)((e / Bp) % Hd), b = (int)(e % Bp);
+        const int pr = r ^ 8, pe = (r >> 4) * 8 + (r & 7);
+        float u[8], w[8], d[8], o[8];
+        ld_f32x8(U + e, u);
+        ld_f32x8(U + e + (long long)(pr - r) * Bp, w);
+        ld_f32x8(dy + p * Bp + b, d);
+        const float q = q2[pe];
+        float sq = 0.f, sc = 0.f;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            o[j] = d[j] * q * w[j];
+            sc += o[j];
+            sq += d[j] * u[j] * w[j];
+        }
+        if (!(r & 8)) atomicAdd(&s1[pe], sq);
+        atomicAdd(&s2[r], sc);
+        st_bf16x8(dU + e, o);
+    }
+    a1.flush(dq2, Hd / 2);
+    a2.flush(dc1, Hd);
+}
+
 // Lift backward: dP[c] += sum dH x; dbP[c] += sum dH.
 __global__ void lift_bwd_kernel(const float *__restrict__ dH, const float *__restrict__ x,
                                 float *dP, float *dbP, long long P, int C, int Bp)
@@ -250,6 +294,21 @@ __global__ void lift_bwd_kernel(const float *__restrict__ dH, const float *__res
     }
     a1.flush(dP, C);
     a2.flush(dbP, C);
+}
+
+// den[b] += eps * mean over the B real instances of den (the loss floor).
+__global__ void den_floor_kernel(float *den, int B, float eps)
+{
+    __shared__ float red[32];
+    float s = 0.f;
+    for (int b = threadIdx.x; b < B; b += blockDim.x) s += den[b];
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    float tot = 0.f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) tot += red[w];
+    __syncthreads();
+    for (int b = threadIdx.x; b < B; b += blockDim.x) den[b] += eps * tot / (float)B;
 }
 
 // den[b] = sum_p t[p][b]^2.
@@ -472,11 +531,13 @@ using namespace sbte::fno;
 struct spectral_fno_s {
     int device = 0;
     int N = 0, C = 0, Km = 0, L = 0, Hd = 0, ncls = 0;
+    int kind = 0;  // 0: GELU layers and readout; 1: linear layers, bilinear readout
     long long P = 0;
     long long nparams = 0;
     long long oP = 0, obP = 0, oW[8] = {}, ob[8] = {}, oR[8] = {}, oQ1 = 0, oc1 = 0, oq2 = 0,
               oc2 = 0;
     float sigma = 1.f;
+    float floor_eps = 0.f;  // loss: |y - t|^2 / (|t|^2 + floor_eps * mean_b |t_b|^2)
     float *params = nullptr, *grads = nullptr, *am = nullptr, *av = nullptr;
     long long adam_t = 0;
     float *F = nullptr, *G = nullptr;  // DFT axis matrices
@@ -569,7 +630,8 @@ int ensure(spectral_fno_s *n, int Bp, bool train)
     const int nx = train ? n->L : 1;
     for (int l = 0; l < nx; l++) FNO_TRY(nalloc(n, &n->X[l], xm));
     if (train) {
-        for (int l = 0; l < n->L; l++) FNO_TRY(nalloc(n, &n->Z[l], act));
+        if (n->kind == 0)
+            for (int l = 0; l < n->L - 1; l++) FNO_TRY(nalloc(n, &n->Z[l], act));
         FNO_TRY(nalloc(n, &n->t, P * Bp));
         FNO_TRY(nalloc(n, &n->den, Bp));
         FNO_TRY(nalloc(n, &n->dy, P * Bp));
@@ -733,9 +795,10 @@ int forward(spectral_fno_s *n, const T *f, int B, int Bp, bool train, cudaStream
         a.Nn = P * Bp;
         a.bias = prm + n->ob[l];
         a.addend = n->S;
-        a.zst = train ? n->Z[l] : nullptr;
+        const bool gelu = n->kind == 0 && l < n->L - 1;
+        a.zst = (train && gelu) ? n->Z[l] : nullptr;
         a.hout = hout;
-        a.act = (l < n->L - 1) ? 1 : 0;
+        a.act = gelu ? 1 : 0;
         set_ext(a, E.prm - n->oW[l], E.act, E.act);
         FNO_LAUNCH((launch_sa<64, 128, 2, 2, false, false, kEpiLayer>(a, st)));
     }
@@ -748,6 +811,7 @@ int forward(spectral_fno_s *n, const T *f, int B, int Bp, bool train, cudaStream
     a.zst = train ? n->Up : nullptr;
     a.c2 = prm + n->oc2;
     a.y = n->y;
+    a.bil = n->kind;
     set_ext(a, E.prm - n->oQ1, E.act, train ? E.proj : 0);
     FNO_LAUNCH((launch_sa<128, 64, 4, 2, false, false, kEpiProj>(a, st)));
     return kOk;
@@ -769,8 +833,12 @@ int backward(spectral_fno_s *n, int B, int Bp, cudaStream_t st)
     FNO_LAUNCH(cudaMemsetAsync(n->d_loss, 0, sizeof(double), st));
     loss_kernel<<<ew_grid(P * Bp / 8), kEw, 0, st>>>(n->y, n->t, n->den, n->dy, n->d_loss,
                                                       gr + n->oc2, P * Bp, B, Bp);
-    proj_bwd_kernel<<<ew_grid(P * Hd * Bp / 8), kEw, 0, st>>>(
-        n->Up, n->dy, prm + n->oq2, n->dU, gr + n->oq2, gr + n->oc1, P, (int)Hd, Bp);
+    if (n->kind == 1)
+        proj_bwd_bil_kernel<<<ew_grid(P * Hd * Bp / 8), kEw, 0, st>>>(
+            n->Up, n->dy, prm + n->oq2, n->dU, gr + n->oq2, gr + n->oc1, P, (int)Hd, Bp);
+    else
+        proj_bwd_kernel<<<ew_grid(P * Hd * Bp / 8), kEw, 0, st>>>(
+            n->Up, n->dy, prm + n->oq2, n->dU, gr + n->oq2, gr + n->oc1, P, (int)Hd, Bp);
     add_launches(2);
     FNO_LAUNCH(cudaGetLastError());
     const long long KC = 16384;
@@ -793,7 +861,8 @@ int backward(spectral_fno_s *n, int B, int Bp, cudaStream_t st)
     }
     for (int l = n->L - 1; l >= 0; l--) {
         gelu_bwd_kernel<<<ew_grid(P * CB / 8), kEw, 0, st>>>(
-            n->dH, l < n->L - 1 ? n->Z[l] : nullptr, n->dZ, gr + n->ob[l], P, (int)C, Bp);
+            n->dH, (n->kind == 0 && l < n->L - 1) ? n->Z[l] : nullptr, n->dZ, gr + n->ob[l], P,
+            (int)C, Bp);
         add_launches(1);
         FNO_LAUNCH(cudaGetLastError());
         {  // dW_l += dZ h_l^T
@@ -850,6 +919,10 @@ int loss_and_grad(spectral_fno_s *n, const T *f, const T *Q, int B, cudaStream_t
     FNO_LAUNCH(cudaMemsetAsync(n->den, 0, sizeof(float) * Bp, st));
     den_kernel<<<152, 256, 0, st>>>(n->t, n->den, P, Bp);
     add_launches(2);
+    if (n->floor_eps > 0.f) {
+        den_floor_kernel<<<1, 256, 0, st>>>(n->den, B, n->floor_eps);
+        add_launches(1);
+    }
     FNO_LAUNCH(cudaGetLastError());
     return backward(n, B, Bp, st);
 }
@@ -897,7 +970,7 @@ int rel_l2_device(const double *A, const double *R, long long n3, double *out, c
 extern "C" {
 
 int spectral_fno_create(spectral_fno **out, int N, int width, int modes, int layers, int hidden,
-                        unsigned long long seed)
+                        int kind, unsigned long long seed)
 {
     if (!out) {
         set_error(kErrArg, "spectral_fno_create: null handle pointer");
@@ -906,12 +979,12 @@ int spectral_fno_create(spectral_fno **out, int N, int width, int modes, int lay
     *out = nullptr;
     if (N < 4 || N > 32 || width < 8 || width > 64 || width % 8 || modes < 2 || modes > 16 ||
         modes % 2 || modes > N || layers < 1 || layers > 8 || hidden < 16 || hidden > 128 ||
-        hidden % 16) {
+        hidden % 16 || kind < 0 || kind > 1) {
         set_error(kErrArg,
                   "spectral_fno_create: unsupported shape N=%d width=%d modes=%d layers=%d "
-                  "hidden=%d (N 4..32, width 8..64 step 8, even modes <= min(16, N), "
-                  "layers 1..8, hidden 16..128 step 16)",
-                  N, width, modes, layers, hidden);
+                  "hidden=%d kind=%d (N 4..32, width 8..64 step 8, even modes <= min(16, N), "
+                  "layers 1..8, hidden 16..128 step 16, kind 0 or 1)",
+                  N, width, modes, layers, hidden, kind);
         return kErrArg;
     }
     int ndev = 0;
@@ -921,7 +994,7 @@ int spectral_fno_create(spectral_fno **out, int N, int width, int modes, int lay
     }
     auto *n = new spectral_fno_s;
     cudaGetDevice(&n->device);
-    n->N = N; n->C = width; n->Km = modes; n->L = layers; n->Hd = hidden;
+    n->N = N; n->C = width; n->Km = modes; n->L = layers; n->Hd = hidden; n->kind = kind;
     n->P = (long long)N * N * N;
     // mode classes by |m|^2
     const int Km = modes;
@@ -953,7 +1026,8 @@ int spectral_fno_create(spectral_fno **out, int N, int width, int modes, int lay
     }
     n->oQ1 = o; o += hidden * C;
     n->oc1 = o; o += hidden;
-    n->oq2 = o; o += hidden;
+    const int nq2 = kind == 1 ? hidden / 2 : hidden;
+    n->oq2 = o; o += nq2;
     n->oc2 = o; o += 1;
     n->nparams = o;
     // initial values: uniform draws scaled by fan-in, zero biases
@@ -969,7 +1043,7 @@ int spectral_fno_create(spectral_fno **out, int N, int width, int modes, int lay
             h[n->oR[l] + i] = uni(1.0 / std::sqrt((double)C));
     }
     for (long long i = 0; i < hidden * C; i++) h[n->oQ1 + i] = uni(1.0 / std::sqrt((double)C));
-    for (long long i = 0; i < hidden; i++) h[n->oq2 + i] = uni(1.0 / std::sqrt((double)hidden));
+    for (long long i = 0; i < nq2; i++) h[n->oq2 + i] = uni(1.0 / std::sqrt((double)nq2));
     // DFT axis matrices: F[m][n] = e^{-2 pi i m n / N} / N, G[n][m] = e^{+2 pi i m n / N}
     std::vector<float> Fh(2 * Km * N), Gh(2 * N * Km);
     for (int m = 0; m < Km; m++)
@@ -1063,6 +1137,16 @@ int spectral_fno_set_output_scale(spectral_fno *n, float sigma)
 }
 
 float spectral_fno_output_scale(spectral_fno *n) { return n ? n->sigma : 0.f; }
+
+int spectral_fno_set_loss_floor(spectral_fno *n, float eps)
+{
+    if (!n || !(eps >= 0.f)) {
+        set_error(kErrArg, "spectral_fno_set_loss_floor: need a handle and eps >= 0");
+        return kErrArg;
+    }
+    n->floor_eps = eps;
+    return kOk;
+}
 
 int spectral_fno_predict(spectral_fno *n, const double *f_dev, double *Q_dev, int B, void *stream)
 {

@@ -65,6 +65,7 @@ struct SaArgs {
     const float *c1, *q2;  // kEpiProj
     const float *c2;       // kEpiProj: one value on the device
     float *y;              // kEpiProj: y[n]
+    int bil;               // kEpiProj: bilinear readout over row pairs (m, m + 8)
     // host-side bounds check: element counts of A, B, C (and of the
     // epilogue arrays that share C's view); 0 skips the check
     long long extA, extB, extC;
@@ -292,25 +293,48 @@ __global__ void __launch_bounds__(WM *WN * 32) gemm_sa_kernel(const SaArgs a)
 #pragma unroll
             for (int fn = 0; fn < FN; fn++) part[fn][0] = part[fn][1] = 0.f;
 #pragma unroll
-            for (int fm = 0; fm < FM; fm++)
+            for (int fm = 0; fm < FM; fm++) {
+                const int m = wm * WR + fm * 16 + g;   // rows m and m + 8 of this thread
+                if (m >= a.M) continue;
+                if (a.bil) {
+                    // pair e = 8 (m / 16) + m % 8: left factor row m, right factor row m + 8
+                    const float cl = a.c1[m], cr = a.c1[m + 8];
+                    const float q = a.q2[(m >> 4) * 8 + (m & 7)];
+#pragma unroll
+                    for (int fn = 0; fn < FN; fn++) {
+                        const long long n = n0 + wn * WC + fn * 8 + 2 * t;
+                        const float l0 = accR[fm][fn][0] + cl, l1 = accR[fm][fn][1] + cl;
+                        const float r0 = accR[fm][fn][2] + cr, r1 = accR[fm][fn][3] + cr;
+                        if (a.zst && n < a.Nn) {
+                            *reinterpret_cast<float2 *>(a.zst + zc + view_off(a.C, m, n)) =
+                                make_float2(l0, l1);
+                            *reinterpret_cast<float2 *>(a.zst + zc + view_off(a.C, m + 8, n)) =
+                                make_float2(r0, r1);
+                        }
+                        part[fn][0] += q * l0 * r0;
+                        part[fn][1] += q * l1 * r1;
+                    }
+                    continue;
+                }
 #pragma unroll
                 for (int hh = 0; hh < 2; hh++) {
-                    const int m = wm * WR + fm * 16 + g + hh * 8;
-                    if (m >= a.M) continue;
-                    const float c1 = a.c1[m], q2 = a.q2[m];
+                    const int mh = m + hh * 8;
+                    if (mh >= a.M) continue;
+                    const float c1 = a.c1[mh], q2 = a.q2[mh];
 #pragma unroll
                     for (int fn = 0; fn < FN; fn++) {
                         const long long n = n0 + wn * WC + fn * 8 + 2 * t;
                         const float u0 = accR[fm][fn][2 * hh] + c1;
                         const float u1 = accR[fm][fn][2 * hh + 1] + c1;
                         if (a.zst && n < a.Nn) {
-                            float *dst = a.zst + zc + view_off(a.C, m, n);
+                            float *dst = a.zst + zc + view_off(a.C, mh, n);
                             *reinterpret_cast<float2 *>(dst) = make_float2(u0, u1);
                         }
                         part[fn][0] += q2 * gelu_f(u0);
                         part[fn][1] += q2 * gelu_f(u1);
                     }
                 }
+            }
 #pragma unroll
             for (int fn = 0; fn < FN; fn++)
 #pragma unroll

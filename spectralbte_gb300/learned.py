@@ -98,23 +98,30 @@ def sample_f(v: np.ndarray, family: str, B: int, seed: int, device="cuda"):
 def make_dataset(plan: Plan, n: int, seed: int, chunk: int = 512,
                  families=FAMILIES, out_dtype=None):
     """n pairs (f, Q) with Q = conserve(plain FP32 Q(f)), stored as float32 on
-    the device (out_dtype float64 keeps FP64).  Families rotate per chunk."""
+    the device (out_dtype float64 keeps FP64), and the family index of each
+    pair.  Instance i belongs to family i mod len(families)."""
     import torch
     out_dtype = out_dtype or torch.float32
     F = torch.empty(n, plan.n3, dtype=out_dtype, device="cuda")
     Q = torch.empty_like(F)
     Qc = torch.empty(chunk, plan.n3, dtype=torch.float64, device="cuda")
+    nf = len(families)
+    fam = torch.arange(n, device="cuda") % nf
     i, k = 0, 0
     while i < n:
         b = min(chunk, n - i)
-        f = sample_f(plan.v, families[k % len(families)], b, seed + 7919 * k)
+        f = torch.empty(b, plan.n3, dtype=torch.float64, device="cuda")
+        for j, name in enumerate(families):
+            idx = [r for r in range(b) if (i + r) % nf == j]
+            if idx:
+                f[idx] = sample_f(plan.v, name, len(idx), seed + 7919 * k + 104729 * j)
         plan.computeQ_device(f, Qc, b, FP32 | CONSERVE)
         F[i:i + b] = f.to(out_dtype)
         Q[i:i + b] = Qc[:b].to(out_dtype)
         i += b
         k += 1
     torch.cuda.synchronize()
-    return F, Q
+    return F, Q, fam
 
 
 def output_scale(F, Q) -> float:
@@ -168,6 +175,17 @@ def train(net: FourierOperator, F, Q, steps: int, batch: int = 32, lr: float = 2
     return log
 
 
+def family_stats(err, fam, families=FAMILIES) -> dict:
+    """Mean, median and max of per-instance errors by family."""
+    out = {}
+    for j, name in enumerate(families):
+        e = err[fam == j]
+        if e.numel():
+            out[name] = {"mean": e.mean().item(), "median": e.median().item(),
+                         "max": e.max().item()}
+    return out
+
+
 def rel_l2_per_instance(A, R):
     import torch
     d = (A.double() - R.double()).pow(2).sum(dim=1)
@@ -206,6 +224,8 @@ def main(argv=None):
     ap.add_argument("--modes", type=int, default=12)
     ap.add_argument("--layers", type=int, default=4)
     ap.add_argument("--hidden", type=int, default=128)
+    ap.add_argument("--kind", type=int, default=0, help="0: GELU network, 1: bilinear")
+    ap.add_argument("--floor", type=float, default=0.1)
     ap.add_argument("--pairs", type=int, default=200000)
     ap.add_argument("--heldout", type=int, default=512)
     ap.add_argument("--batch", type=int, default=32)
@@ -222,14 +242,16 @@ def main(argv=None):
     plan.generate_weights_iso(a.lam)
     plan.autotune(512, FP32)
     t0 = time.time()
-    F, Q = make_dataset(plan, a.pairs, seed=a.seed)
-    Fe, Qe = make_dataset(plan, a.heldout, seed=a.seed + 10 ** 6, out_dtype=torch.float64)
+    F, Q, _ = make_dataset(plan, a.pairs, seed=a.seed)
+    Fe, Qe, fam = make_dataset(plan, a.heldout, seed=a.seed + 10 ** 6, out_dtype=torch.float64)
     t_data = time.time() - t0
     if a.init:
         net = FourierOperator.load(a.init)
     else:
-        net = FourierOperator(a.n, a.width, a.modes, a.layers, a.hidden, seed=a.seed)
+        net = FourierOperator(a.n, a.width, a.modes, a.layers, a.hidden, seed=a.seed,
+                              kind=a.kind)
         net.output_scale = output_scale(F, Q)
+    net.set_loss_floor(a.floor)
     e0 = evaluate(net, plan, Fe, Qe)
     log = train(net, F, Q, a.steps, batch=a.batch, lr=a.lr, seed=a.seed,
                 time_limit=60.0 * a.minutes)
@@ -242,6 +264,7 @@ def main(argv=None):
         "heldout_rel_l2_untrained": {"mean": e0.mean().item(), "max": e0.max().item()},
         "heldout_rel_l2_trained": {"mean": e1.mean().item(), "median": e1.median().item(),
                                    "max": e1.max().item()},
+        "heldout_by_family": family_stats(e1, fam),
         "out": a.out}))
 
 

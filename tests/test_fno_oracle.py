@@ -66,6 +66,33 @@ def test_gradients_with_odd_modes_and_three_layers():
         assert abs(ga[i] - gn) <= 1e-6 * max(1.0, abs(gn)), (i, ga[i], gn)
 
 
+def test_bilinear_gradients_and_homogeneity():
+    spec = fo.Spec(N=4, C=3, Km=2, L=2, Hd=16, kind=1)
+    spec, theta, net = _small(spec=spec, seed=7)
+    f, Q = _data(spec, 2, 3)
+    _, g = net.loss_grad(f, Q, floor=0.2)
+    ga = fo.pack(spec, g)
+    eps = 1e-6
+    for i in range(theta.size):
+        tp, tm = theta.copy(), theta.copy()
+        tp[i] += eps
+        tm[i] -= eps
+        lp, _ = fo.Net(spec, tp, sigma=0.7).loss_grad(f, Q, floor=0.2)
+        lm, _ = fo.Net(spec, tm, sigma=0.7).loss_grad(f, Q, floor=0.2)
+        gn = (lp - lm) / (2 * eps)
+        assert abs(ga[i] - gn) <= 1e-6 * max(1.0, abs(gn)), (i, ga[i], gn)
+    # with zero biases the kind-1 network is a quadratic form in f
+    d = fo.unpack(spec, theta)
+    for k in d:
+        if k in ("bP", "c1", "c2") or k.startswith("b"):
+            d[k][:] = 0.0
+    q = fo.Net(spec, fo.pack(spec, d), sigma=0.7)
+    y1, c1 = q.forward(f)
+    y2, c2 = q.forward(3.0 * f)
+    assert np.allclose(y1, y2)  # the input is scaled by its maximum
+    assert np.allclose(q.predict(3.0 * f), 9.0 * q.predict(f))
+
+
 def test_full_mode_transform_pair_is_identity():
     spec = fo.Spec(N=6, C=2, Km=6, L=1, Hd=2)
     _, n = spec.layout()
@@ -94,5 +121,7 @@ def test_layout_matches_library_count(lib_built):
     C, Hd, L = 64, 128, 4
     want = 2 * C + L * (C * C + C + ncls * C * C) + Hd * C + 2 * Hd + 1
     assert n == want
+    _, n1 = fo.Spec(N=32, C=64, Km=12, L=4, Hd=128, kind=1).layout()
+    assert n1 == want - Hd // 2
     assert cls.shape == (12, 12, 12) and cls.max() == ncls - 1
     assert "spectral_fno_create" in sb.declared_symbols()

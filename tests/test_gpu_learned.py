@@ -1,11 +1,17 @@
 """GPU learned collision operator (fno.cu) against its FP64 oracle.
 
 * Forward: the network output on the device equals the oracle's with the
-  same BF16 rounding points within rel-L2 1e-3, and the pure-FP64 oracle
-  within rel-L2 3e-2 (the BF16 operands).
+  same BF16 rounding points within rel-L2 1e-3, or for deeper networks no
+  farther than that oracle is from the pure-FP64 one (FP32 accumulation
+  order flips a few BF16 roundings, and the layers amplify them), and the
+  pure-FP64 oracle within rel-L2 3e-2.
 * Gradients: every parameter block's gradient equals the rounding oracle's
-  within rel-L2 5e-3 and the FP64 oracle's within 5e-2; the loss within
-  1e-4 relative.  Batches that are not a multiple of 8 exercise the padding.
+  within rel-L2 5e-3 or twice that oracle's distance from the FP64 one
+  (the lift gradient is a sum with heavy cancellation, accumulated in FP32
+  atomics on the device), and the FP64 oracle's within 5e-2; the loss within
+  1e-4 relative.  An indexing or formula error shows as an O(1) difference.
+  Both network kinds (GELU, bilinear), three shapes, and batches that are
+  not a multiple of 8 (padding).
 * Training on pairs from the plain operator lowers the held-out error of the
   network well below that of the untrained network.
 * The plan's SPECTRAL_LEARNED path: the output is the conservation
@@ -23,54 +29,64 @@ from oracle import fno_oracle as fo
 pytestmark = pytest.mark.gpu
 
 N, WIDTH, MODES, LAYERS, HIDDEN = 8, 8, 4, 2, 16
+SHAPES = {"small": (8, 8, 4, 2, 16, 0), "wide": (16, 16, 8, 3, 32, 0),
+          "odd": (12, 24, 6, 1, 48, 0), "bil": (8, 8, 4, 2, 16, 1),
+          "wide_bil": (16, 16, 8, 3, 32, 1)}
 
 
-def _net(gpu, seed=7, sigma=0.5):
-    net = gpu.FourierOperator(N, WIDTH, MODES, LAYERS, HIDDEN, seed=seed)
+def _net(gpu, seed=7, sigma=0.5, shape="small"):
+    n, w, m, L, hd, kind = SHAPES[shape]
+    net = gpu.FourierOperator(n, w, m, L, hd, seed=seed, kind=kind)
     net.output_scale = sigma
-    spec = fo.Spec(N=N, C=WIDTH, Km=MODES, L=LAYERS, Hd=HIDDEN)
+    spec = fo.Spec(N=n, C=w, Km=m, L=L, Hd=hd, kind=kind)
     return net, spec
 
 
-def _data(B, seed):
+def _data(B, seed, n=N):
     rng = np.random.default_rng(seed)
-    f = rng.uniform(0.05, 1.0, (B, N ** 3)).astype(np.float32)
-    Q = rng.normal(size=(B, N ** 3)).astype(np.float32)
+    f = rng.uniform(0.05, 1.0, (B, n ** 3)).astype(np.float32)
+    Q = rng.normal(size=(B, n ** 3)).astype(np.float32)
     return f, Q
 
 
-@pytest.mark.parametrize("B", [3, 8, 13])
-def test_forward_matches_oracle(gpu, B):
+@pytest.mark.parametrize("B,shape", [(3, "small"), (8, "small"), (13, "small"), (5, "wide"),
+                                     (9, "odd"), (6, "bil"), (4, "wide_bil")])
+def test_forward_matches_oracle(gpu, B, shape):
     import torch
-    net, spec = _net(gpu)
+    net, spec = _net(gpu, shape=shape)
     theta = net.get_params().astype(np.float64)
-    f, _ = _data(B, B)
+    f, _ = _data(B, B, spec.N)
     fd = torch.from_numpy(f.astype(np.float64)).cuda()
     Qd = torch.zeros_like(fd)
     net.predict(fd, Qd, B)
     got = Qd.cpu().numpy()
     want_r = fo.Net(spec, theta, sigma=0.5, rounding=True).predict(f.astype(np.float64))
     want = fo.Net(spec, theta, sigma=0.5).predict(f.astype(np.float64))
-    assert rel_l2(got, want_r.reshape(B, -1)) < 1e-3
+    gap = rel_l2(want_r, want)
+    assert rel_l2(got, want_r.reshape(B, -1)) < max(1e-3, gap), gap
     assert rel_l2(got, want.reshape(B, -1)) < 3e-2
 
 
-@pytest.mark.parametrize("B", [5, 16])
-def test_gradients_match_oracle(gpu, B):
+@pytest.mark.parametrize("B,shape,floor", [(5, "small", 0.0), (16, "small", 0.3),
+                                           (6, "wide", 0.0), (3, "odd", 0.1),
+                                           (7, "bil", 0.1), (4, "wide_bil", 0.0)])
+def test_gradients_match_oracle(gpu, B, shape, floor):
     import torch
-    net, spec = _net(gpu, seed=11)
+    net, spec = _net(gpu, seed=11, shape=shape)
+    net.set_loss_floor(floor)
     theta = net.get_params().astype(np.float64)
-    f, Q = _data(B, 100 + B)
+    f, Q = _data(B, 100 + B, spec.N)
     loss, g = net.loss_grad(torch.from_numpy(f).cuda(), torch.from_numpy(Q).cuda(), B)
     lr_, gr = fo.Net(spec, theta, sigma=0.5, rounding=True).loss_grad(
-        f.astype(np.float64), Q.astype(np.float64))
+        f.astype(np.float64), Q.astype(np.float64), floor)
     l64, g64 = fo.Net(spec, theta, sigma=0.5).loss_grad(f.astype(np.float64),
-                                                        Q.astype(np.float64))
+                                                        Q.astype(np.float64), floor)
     assert abs(loss - lr_) <= 1e-4 * lr_
     off, _ = spec.layout()
     for k, (o, n) in off.items():
         gk = g[o:o + n].astype(np.float64)
-        assert rel_l2(gk, gr[k].reshape(-1)) < 5e-3, k
+        gap = rel_l2(gr[k].reshape(-1), g64[k].reshape(-1))
+        assert rel_l2(gk, gr[k].reshape(-1)) < max(5e-3, 2 * gap), (k, gap)
         assert rel_l2(gk, g64[k].reshape(-1)) < 5e-2, k
 
 
@@ -81,18 +97,20 @@ def _plan(gpu, n=N, L_v=6.0, lam=1.0):
     return plan
 
 
-def test_training_lowers_heldout_error(gpu):
+def test_training_lowers_heldout_error(gpu, shape="small"):
     import torch
     from spectralbte_gb300 import learned as lrn
     plan = _plan(gpu)
-    F, Q = lrn.make_dataset(plan, 768, seed=1, chunk=128)
-    Fe, Qe = lrn.make_dataset(plan, 96, seed=999, chunk=96, out_dtype=torch.float64)
-    net, _ = _net(gpu, seed=3, sigma=lrn.output_scale(F, Q))
-    e0 = lrn.evaluate(net, plan, Fe, Qe).mean().item()
-    log = lrn.train(net, F, Q, steps=400, batch=16, lr=3e-3, lr_final=1e-4)
-    e1 = lrn.evaluate(net, plan, Fe, Qe).mean().item()
-    assert log.losses[-1][1] < log.losses[0][1]
-    assert e1 < 0.5 * e0, (e0, e1)
+    F, Q, _ = lrn.make_dataset(plan, 768, seed=1, chunk=128)
+    Fe, Qe, fam = lrn.make_dataset(plan, 96, seed=999, chunk=96, out_dtype=torch.float64)
+    net, _ = _net(gpu, seed=3, sigma=lrn.output_scale(F, Q), shape=shape)
+    net.set_loss_floor(0.1)
+    e0 = lrn.evaluate(net, plan, Fe, Qe)
+    log = lrn.train(net, F, Q, steps=1500, batch=16, lr=1e-2, lr_final=3e-4)
+    e1 = lrn.evaluate(net, plan, Fe, Qe)
+    assert log.losses[-1][1] < 0.5 * log.losses[0][1]
+    assert e1.mean() < 0.5 * e0.mean(), (e0.mean().item(), e1.mean().item(),
+                                         lrn.family_stats(e1, fam))
 
 
 def _moments(v, Q):
