@@ -43,10 +43,27 @@ N_DEF, LV_DEF, LAM_DEF = 32, 6.0, 1.0
 # Nominal FP32 CUDA-core peak of GB300: 152 SMs x 128 lanes x 2 flop/FMA
 # at the maximum SM clock.
 N_SM, FP32_LANES = 152, 128
-# DRAM bytes (read + write) of one conv_f32_kernel launch measured by ncu at
-# N=24, B=128, bg=64 (profiles/conv_f32_n24_b128_ncu.md).  W streams once per
-# instance group, so traffic scales with N^6 * B at fixed bg.
-NCU_TRAFFIC = {"bytes": 1.691575e9 + 66.592768e6, "N": 24, "B": 128, "bg": 64}
+# DRAM bytes (read + write) of one convolution launch measured by ncu at
+# N=24, B=128, per kernel variant: the block-barrier kernel (variant 1, bg=64,
+# profiles/conv_f32_n24_b128_ncu.md) and the warp-specialised kernel
+# (variants 2-4, bg=32, profiles/conv_ws_n24_b128_ncu.md).  W streams once
+# per instance group, so traffic scales with N^6 times the number of groups.
+NCU_TRAFFIC = {
+    1: {"bytes": 1.691575e9 + 66.592768e6, "N": 24, "B": 128, "bg": 64,
+        "kernel": "conv_f32_kernel"},
+    3: {"bytes": 3.135992e9 + 75.185664e6, "N": 24, "B": 128, "bg": 32,
+        "kernel": "conv_ws_kernel"},
+}
+KERNEL_NAME = {1: "conv_f32_kernel", 2: "conv_ws_kernel", 3: "conv_ws_kernel",
+               4: "conv_x4_kernel"}
+
+
+def scaled_traffic(variant: int, N: int, B: int, bg: int):
+    """Per-launch DRAM bytes at (N, B, bg) from the capture of the same kernel."""
+    cap = NCU_TRAFFIC.get(1 if variant == 1 else 3)
+    groups = -(-B // bg)
+    cap_groups = -(-cap["B"] // cap["bg"])
+    return cap["bytes"] / cap_groups * groups * (N / cap["N"]) ** 6, cap
 
 
 def load_peaks():
@@ -255,6 +272,232 @@ def run_uneven(args):
     return 0
 
 
+def learned_work(N: int, C: int, Km: int, L: int, Hd: int) -> dict:
+    """Algorithmic flops and DRAM bytes of one learned-operator evaluation
+    (one instance): every GEMM's real multiply-adds, and every tensor the
+    kernel sequence writes once and reads once (BF16 between GEMMs, FP32 for
+    the spectral sum S, FP64 for f and Q and the conservation projection)."""
+    P = N ** 3
+    fl = (4 * Km * N ** 3 * C + 8 * Km ** 2 * N ** 2 * C + 8 * Km ** 3 * N * C   # forward axes
+          + 4 * C * C * Km ** 3                                                 # mode mix
+          + 8 * N * Km ** 3 * C + 8 * N ** 2 * Km ** 2 * C + 4 * N ** 3 * Km * C  # inverse axes
+          + 2 * C * C * P)                                                      # channel mix
+    flops = L * fl + 2 * Hd * C * P + 2 * Hd * P
+    act, s32 = 2 * P * C, 4 * P * C
+    t1, t2, xm = 2 * N * N * 2 * Km * C, 2 * N * 2 * Km * Km * C, 2 * 2 * Km ** 3 * C
+    per_layer = 2 * act + 2 * (t1 + t2 + xm) * 2 + 2 * s32 + act
+    bytes_ = 8 * P + 4 * P * 2 + act + L * per_layer + 4 * P + 8 * P + 4 * 8 * P
+    return {"flops": float(flops), "bytes": float(bytes_)}
+
+
+def run_learned(args, plan, fd, Qd, B, flags, peaks):
+    """Throughput and accuracy of the learned operator at the headline
+    workload, next to the plain FP32 operator's Q (already in Qd)."""
+    import torch
+    import spectralbte_gb300 as sb
+    path = args.learned or os.path.join(ROOT, "spectralbte_gb300", "models", "fno_n32.npz")
+    if not os.path.exists(path):
+        return {"status": f"no trained network at {os.path.relpath(path, ROOT)}"}
+    net = sb.FourierOperator.load(path)
+    if net.N != plan.N:
+        return {"status": f"network trained for N={net.N}, workload N={plan.N}"}
+    Ql = torch.empty_like(Qd)
+    lf = flags | sb.LEARNED
+    plan.set_learned(net, tol=1e-3, check_every=0)   # network + FP64 projection only
+    for _ in range(max(1, args.warmup)):
+        plan.computeQ_device(fd, Ql, B, lf)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    steps = max(2, args.steps)
+    k0 = sb.kernel_launches()
+    e0.record()
+    for _ in range(steps):
+        plan.computeQ_device(fd, Ql, B, lf)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    launches = (sb.kernel_launches() - k0) / steps
+    d = (Ql - Qd).pow(2).sum(dim=1) / Qd.pow(2).sum(dim=1)
+    rel = d.sqrt()
+    # the spot-checked path: one instance per call against the plain FP32 operator
+    plan.set_learned(net, tol=1e-3, check_every=1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        plan.computeQ_device(fd, Ql, B, lf)
+    torch.cuda.synchronize()
+    ms_checked = (time.perf_counter() - t0) * 1e3 / steps
+    st = plan.learned_stats()
+    plan.set_learned(None)
+    w = learned_work(net.N, net.width, net.modes, net.layers, net.hidden)
+    tflops = w["flops"] * B / (ms / 1e3) / 1e12
+    gbs = w["bytes"] * B / (ms / 1e3) / 1e9
+    return {
+        "network": {"N": net.N, "width": net.width, "modes": net.modes, "layers": net.layers,
+                    "hidden": net.hidden, "params": net.nparams,
+                    "checkpoint": os.path.relpath(path, ROOT)},
+        "value": B / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
+        "kernel_launches_per_step": launches,
+        "speedup_vs_fp32_plain": None,
+        "rel_l2_vs_plain_fp32": {"mean": float(rel.mean()), "median": float(rel.median()),
+                                 "max": float(rel.max())},
+        "tolerance": 1e-3,
+        "accepted": bool(float(rel.max()) <= 1e-3),
+        "spot_checked": {"value": B / (ms_checked / 1e3), "unit": UNIT,
+                         "calls": st["calls"], "fallbacks": st["fallbacks"],
+                         "last_check_rel_l2": st["last_err"]},
+        "roofline": {"bound": "hbm", "achieved": gbs, "peak": float(peaks["hbm_gbs"]),
+                     "unit": "GB/s", "frac": gbs / float(peaks["hbm_gbs"]),
+                     "algorithmic_bytes_per_eval": w["bytes"],
+                     "tensor": {"achieved": tflops, "peak": float(peaks["bf16_tflops"]),
+                                "unit": "TFLOP/s",
+                                "frac": tflops / float(peaks["bf16_tflops"]),
+                                "algorithmic_flops_per_eval": w["flops"]}},
+    }
+
+
+def run_learned_only(args):
+    """The learned operator alone at the headline workload (network + FP64
+    projection per step), for its launch list and profiles."""
+    import torch
+    import spectralbte_gb300 as sb
+    torch.cuda.set_device(0)
+    N, L_v, lam, B = args.n, LV_DEF, LAM_DEF, args.batch
+    v, zeta = sb.grid_0d(N, L_v)
+    plan = sb.Plan(N, L_v, v, zeta, B)
+    plan.generate_weights_iso(lam)
+    path = args.learned or os.path.join(ROOT, "spectralbte_gb300", "models", f"fno_n{N}.npz")
+    trained = os.path.exists(path)
+    net = sb.FourierOperator.load(path) if trained else sb.FourierOperator(N)
+    fd = torch.from_numpy(two_maxwellian_batch(v, B, args.seed)).cuda()
+    Qd = torch.empty_like(fd)
+    plan.set_learned(net, tol=1e-3, check_every=0)
+    flags = sb.FP32 | sb.CONSERVE | sb.LEARNED
+    for _ in range(args.warmup):
+        plan.computeQ_device(fd, Qd, B, flags)
+    torch.cuda.synchronize()
+    k0 = sb.kernel_launches()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        plan.computeQ_device(fd, Qd, B, flags)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    peaks, _ = load_peaks()
+    w = learned_work(N, net.width, net.modes, net.layers, net.hidden)
+    gbs = w["bytes"] * B / (ms / 1e3) / 1e9
+    print(json.dumps({
+        "metric": "learned-operator Q evals/s (network + FP64 projection)", "impl": "ours",
+        "value": B / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "steps": args.steps,
+        "warmup": args.warmup, "n_gpus": 1, "higher_is_better": True,
+        "config": {"workload": f"N={N}, {B} two-Maxwellian instances, "
+                               f"{'trained' if trained else 'untrained'} network"},
+        "gpu_launches": sb.kernel_launches() - k0,
+        "roofline": {"bound": "hbm", "achieved": gbs, "peak": float(peaks["hbm_gbs"]),
+                     "unit": "GB/s", "frac": gbs / float(peaks["hbm_gbs"]),
+                     "algorithmic_bytes_per_eval": w["bytes"]}}), flush=True)
+    return 0
+
+
+CFG_1D = {
+    # config 3: the reference's Mach-1.2 shock (Init_field 6), minmod transport
+    "shock": dict(N=24, L_v=6.0, lam=1.0, nX=128, order=2, ic=6, dt=0.001, Kn=0.1, steps=500,
+                  note="dt 0.001 instead of 0.002: with |v| <= 6 and dx = 1/128, dt = 0.002 "
+                       "is CFL 1.54 and the explicit upwind transport needs CFL <= 1"),
+    # config 5: heat transfer between diffuse walls at T = 1 and T = 2
+    "heat": dict(N=32, L_v=6.0, lam=1.0, nX=256, order=1, ic=3, dt=5e-4, Kn=0.05, steps=1000,
+                 note="dt 5e-4 (CFL 0.77 with |v| <= 6, dx = 1/256; the config names none)"),
+}
+
+
+def run_1d(args):
+    """A time-stepped 1D-3V run through spectral_1d_step, one CUDA graph per
+    step: config 3 (shock) or config 5 (heat transfer; plain FP32 operator
+    against the learned operator, unchecked and spot-checked)."""
+    import torch
+    import spectralbte_gb300 as sb
+    from spectralbte_gb300 import workloads as wl
+    torch.cuda.set_device(0)
+    c = CFG_1D[args.workload]
+    N, nX, order = c["N"], c["nX"], c["order"]
+    steps = args.nsteps or c["steps"]
+    v, zeta = sb.grid_1d(N, c["L_v"])
+    x, dx = wl.mesh_1d(nX, order)
+    f0 = wl.init_1d(v, nX, order, c["ic"])
+    plan = sb.Plan(N, c["L_v"], v, zeta, nX)
+    plan.generate_weights_iso(c["lam"])
+    plan.autotune(nX, sb.FP32)
+    plan.setup_1d(nX, order, c["ic"], c["dt"], c["Kn"], x, dx, T0=1.0, T1=2.0)
+
+    def run(flags, nsteps):
+        f = torch.from_numpy(f0).cuda()
+        plan.capture(1, f, flags=flags)
+        plan.launch()  # warm-up step
+        torch.cuda.synchronize()
+        k0 = sb.kernel_launches()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(nsteps - 1):
+            plan.launch()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / max(1, nsteps - 1)
+        mom = torch.empty((nX, 8), dtype=torch.float64, device="cuda")
+        plan.moments_device(f[order:order + nX], nX, mom)
+        return f, ms, mom.cpu().numpy(), sb.kernel_launches() - k0
+
+    f, ms, mom, launches = run(sb.FP32, steps)
+    rho = mom[:, 0]
+    mass0 = f0[order:order + nX].sum()
+    line = {
+        "metric": "1D-3V time steps/s", "impl": "ours", "value": 1e3 / ms,
+        "unit": "steps/s", "ms_per_step": ms, "steps": steps, "n_gpus": 1,
+        "higher_is_better": True, "dtype": "fp32 (FP64 moments and conservation)",
+        "data": "synthetic",
+        "config": {"workload": args.workload, **{k: c[k] for k in c if k not in ("steps",)}},
+        "cell_collisions_per_s": nX * (2 if order == 2 else 1) * 1e3 / ms,
+        "gpu_launches": launches,
+        "final": {"rho_min": float(rho.min()), "rho_max": float(rho.max()),
+                  "T_min": float(mom[:, 4].min()), "T_max": float(mom[:, 4].max()),
+                  "finite": bool(np.isfinite(mom).all())},
+    }
+    if args.workload == "heat":
+        path = args.learned or os.path.join(ROOT, "spectralbte_gb300", "models",
+                                            f"fno_n{N}.npz")
+        if os.path.exists(path):
+            net = sb.FourierOperator.load(path)
+            plan.set_learned(net, tol=1e-3, check_every=0)
+            fl, msl, moml, _ = run(sb.FP32 | sb.LEARNED, steps)
+            dev = {k: float(np.abs(moml[:, i] - mom[:, i]).max() / np.abs(mom[:, i]).max())
+                   for k, i in (("rho", 0), ("T", 4))}
+            dev["u_x_abs"] = float(np.abs(moml[:, 1] - mom[:, 1]).max())
+            # the spot-checked policy on a short run (a check reads back, so no graph)
+            plan.set_learned(net, tol=1e-3, check_every=1)
+            fc = torch.from_numpy(f0).cuda()
+            nchk = min(steps, 50)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(nchk):
+                plan.step_1d(fc, sb.FP32 | sb.LEARNED)
+            torch.cuda.synchronize()
+            msc = (time.perf_counter() - t0) * 1e3 / nchk
+            st = plan.learned_stats()
+            line["learned"] = {
+                "checkpoint": os.path.relpath(path, ROOT),
+                "unchecked": {"value": 1e3 / msl, "unit": "steps/s", "ms_per_step": msl,
+                              "speedup_vs_fp32": ms / msl,
+                              "final_moment_deviation_vs_fp32": dev},
+                "spot_checked_every_call": {"value": 1e3 / msc, "unit": "steps/s",
+                                            "steps": nchk, "calls": st["calls"],
+                                            "fallbacks": st["fallbacks"],
+                                            "last_check_rel_l2": st["last_err"],
+                                            "tolerance": 1e-3},
+            }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_ours(args):
     import torch
     import spectralbte_gb300 as sb
@@ -350,10 +593,16 @@ def run_ours(args):
     rel = [float(np.linalg.norm(a[i] - b[i]) / np.linalg.norm(b[i])) for i in range(B64)]
     status = plan.status()
     fma_rate = sb.fp32_fma_rate()  # measured on this GPU, after the timed region
+    peaks, peak_src = load_peaks()
+    learned = None
+    if not args.no_learned:
+        plan.computeQ_device(fd, Qd, B, flags)       # plain FP32 Q of every instance
+        learned = run_learned(args, plan, fd, Qd, B, flags, peaks)
+        if learned.get("value"):
+            learned["speedup_vs_fp32_plain"] = learned["value"] / (value / world)
 
     if rank != 0:
         return 0
-    peaks, peak_src = load_peaks()
     conv_avg_s = conv_ms / max(conv_n, 1) / 1e3
     flops = 10.0 * float(n3) ** 2 * B        # collisions.c:162-163, 10 flops/term
     achieved = flops / conv_avg_s / 1e12
@@ -361,6 +610,7 @@ def run_ours(args):
     fp32_nominal = N_SM * FP32_LANES * 2 * sm_max * 1e6 / 1e12
     fp32_peak = fma_rate
     w_bytes = 4.0 * float(n3) ** 2           # one FP32 W pass per launch
+    traffic, tcap = scaled_traffic(tuned[0], N, B, tuned[1])
     hbm_achieved = w_bytes / conv_avg_s / 1e9
 
     cpu = None
@@ -389,11 +639,11 @@ def run_ours(args):
             "l2": "inputs larger than L2 (W FP32 4.3 GB, f 256 MB at B=1024)",
             "tuning": {"variant": tuned[0], "bg": tuned[1], "zs": tuned[2],
                        "stages": tuned[3], "flush": tuned[4]},
-            "learned_operator": "not built",
+
         },
         "roofline": {
             "bound": "fp32",
-            "kernel": "conv_ws_kernel" if tuned[0] == 2 else "conv_f32_kernel",
+            "kernel": KERNEL_NAME[tuned[0]],
             "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
             "frac": achieved / fp32_peak,
             "peak_source": ("measured: sustained FP32 FMA rate of this GPU from the library's "
@@ -407,12 +657,11 @@ def run_ours(args):
                                f"({peak_src} sm_max_mhz)"),
             "algorithmic": f"10*N^6*B flop per launch = {flops:.3e}",
             "launch_ms": conv_avg_s * 1e3,
-            "traffic": (NCU_TRAFFIC["bytes"] * (float(n3) ** 2 * B) /
-                        (float(NCU_TRAFFIC["N"]) ** 6 * NCU_TRAFFIC["B"])
-                        if tuned[1] == NCU_TRAFFIC["bg"] else None),
-            "traffic_note": ("bytes per launch, scaled by N^6*B from the ncu capture at N=24, "
-                             "B=128, bg=64; W is re-read once per instance group, from HBM, "
-                             "far below the HBM peak"),
+            "traffic": traffic,
+            "traffic_note": (f"bytes per launch, scaled by N^6 x instance groups from the ncu "
+                             f"capture of {tcap['kernel']} at N=24, B=128, bg={tcap['bg']}; W is "
+                             f"re-read once per instance group of {tuned[1]}, from HBM, far "
+                             f"below the HBM peak"),
             "hbm": {"achieved": hbm_achieved, "peak": float(peaks["hbm_gbs"]), "unit": "GB/s",
                     "frac": hbm_achieved / float(peaks["hbm_gbs"]),
                     "algorithmic": f"W FP32 {w_bytes:.3e} B per launch"},
@@ -427,6 +676,8 @@ def run_ours(args):
         "weights_generation_s": t_weights,
         "device_status": status,
     }
+    if learned is not None:
+        line["learned"] = learned
     if cpu:
         line["cpu_baseline"] = cpu
     print(json.dumps(line), flush=True)
@@ -447,12 +698,22 @@ def main():
     ap.add_argument("--fp64-batch", type=int, default=8)
     ap.add_argument("--cpu-rows", type=int, default=2048)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="n32", choices=["n32", "uneven"])
+    ap.add_argument("--workload", default="n32",
+                    choices=["n32", "uneven", "learned", "shock", "heat"])
+    ap.add_argument("--nsteps", type=int, default=0,
+                    help="time steps of the shock / heat workloads (default: the config's)")
+    ap.add_argument("--learned", default="",
+                    help="trained network (.npz); default spectralbte_gb300/models/fno_n32.npz")
+    ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--tuning", default="",
                     help="variant,bg,zs,stages,flush of the FP32 convolution (default: autotune)")
     args = ap.parse_args()
     if args.workload == "uneven" and args.impl != "reference":
         return run_uneven(args)
+    if args.workload == "learned" and args.impl != "reference":
+        return run_learned_only(args)
+    if args.workload in CFG_1D and args.impl != "reference":
+        return run_1d(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -252,6 +252,14 @@ int spectral_fft3d_noalloc(int N, double L_v, const double *v,
                            const double *zeta, const double *in_dev,
                            double *out_dev, int B, int invert, void *stream);
 
+/* Output moments of B instances f_dev[B][N^3] (device) into out_dev[B][8]
+   (device): rho, u_x, u_y, u_z, T, rho T, and the positive and negative
+   parts of getEnergy -- everything write_streams / write_streams_inhom print
+   (output.c:156-213,295-404), so a dump reads 64 bytes per cell instead of
+   f.  Uses the plan's mass and KB.  Asynchronous on stream. */
+int spectral_moments_device(spectral_plan *plan, const double *f_dev, int B,
+                            double *out_dev, void *stream);
+
 /* ---- Learned collision operator.  No counterpart in the reference.
    A Fourier neural operator maps f (one instance on the N^3 grid) to Q(f):
    lift to `width` channels, `layers` spectral layers on the lowest
@@ -263,13 +271,17 @@ int spectral_fft3d_noalloc(int N, double L_v, const double *v,
    over hidden/2 channel pairs (rows 16 (e/8) + e%8 and that + 8), the form
    of a separable approximation of the collision kernel.  f is scaled by its
    maximum s and the output by s^2 times the output scale (Q is bilinear in
-   f).  All GEMMs run on BF16 tensor cores with FP32 accumulation;
-   parameters are FP32.  Shapes: N 4..32, width 8..64 (multiple of 8), even
-   modes <= min(16, N), layers 1..8, hidden 16..128 (multiple of 16). */
+   f).  All GEMMs run on 16-bit tensor cores with FP32 accumulation:
+   precision 0 stores activations and GEMM operands as BF16, precision 1 as
+   FP16 (same rate, 3 more mantissa bits; the backward pass then carries a
+   loss scale).  Parameters are FP32.  Shapes: N 4..32, width 8..64
+   (multiple of 8), even modes <= min(16, N), layers 1..8, hidden 16..128
+   (multiple of 16). */
 typedef struct spectral_fno_s spectral_fno;
 int spectral_fno_create(spectral_fno **net, int N, int width, int modes,
-                        int layers, int hidden, int kind,
+                        int layers, int hidden, int kind, int precision,
                         unsigned long long seed);
+int spectral_fno_precision(spectral_fno *net);
 int spectral_fno_destroy(spectral_fno *net);
 long long spectral_fno_num_params(spectral_fno *net);
 int spectral_fno_num_classes(spectral_fno *net);

@@ -36,6 +36,11 @@ def cbf16(z):
     return bf16(z.real) + 1j * bf16(z.imag)
 
 
+def fp16(x):
+    """Round to the nearest IEEE half (ties to even, subnormals kept); returns float64."""
+    return np.asarray(np.asarray(x, dtype=np.float32), dtype=np.float16).astype(np.float64)
+
+
 def gelu(x):
     return 0.5 * x * (1.0 + erf(x * SQRT_HALF))
 
@@ -112,17 +117,19 @@ def pack(spec: Spec, d: dict) -> np.ndarray:
     return out
 
 
-def dft_mats(N: int, Km: int):
-    """F[m][n] = e^{-2 pi i m n / N} / N and G[n][m] = e^{+2 pi i m n / N},
-    m = index - Km/2, with cos and sin rounded to float32 as the GPU holds them."""
+def dft_mats(N: int, Km: int, scaled: bool = True):
+    """F[m][n] = e^{-2 pi i m n / N} / N (without the 1/N when not scaled)
+    and G[n][m] = e^{+2 pi i m n / N}, m = index - Km/2, with cos and sin
+    rounded to float32 as the GPU holds them."""
     m = np.arange(Km) - Km // 2
     n = np.arange(N)
     r = np.mod(np.outer(m, n), N)
     th = 2.0 * np.pi * r / N
     c = np.float32(np.cos(th)).astype(np.float64)
     s = np.float32(np.sin(th)).astype(np.float64)
-    cN = np.float32(np.cos(th) / N).astype(np.float64)
-    sN = np.float32(np.sin(th) / N).astype(np.float64)
+    d = N if scaled else 1
+    cN = np.float32(np.cos(th) / d).astype(np.float64)
+    sN = np.float32(np.sin(th) / d).astype(np.float64)
     F = cN - 1j * sN
     G = (c + 1j * s).T
     return F, G
@@ -132,32 +139,37 @@ class Net:
     """The network of fno.cu with parameters theta (flat, FP64 copy)."""
 
     def __init__(self, spec: Spec, theta: np.ndarray, sigma: float = 1.0,
-                 rounding: bool = False):
+                 rounding: bool = False, precision: int = 0):
+        """precision 0: BF16 elements, 1: FP16 elements (the device's
+        spectral_fno_create precision); used when rounding is on."""
         self.spec, self.sigma, self.rnd = spec, float(sigma), rounding
+        self.q = fp16 if precision == 1 else bf16
         self.p = unpack(spec, theta)
         self.cls, self.ncls = spec.classes()
         F, G = dft_mats(spec.N, spec.Km)
-        self.F = cbf16(F) if rounding else F
-        self.G = cbf16(G) if rounding else G
+        Fu, _ = dft_mats(spec.N, spec.Km, scaled=False)
+        self.F, self.G, self.Fu = (self.rc(M) if rounding else M for M in (F, G, Fu))
 
     # rounding helpers
     def r(self, x):
-        return bf16(x) if self.rnd else x
+        return self.q(x) if self.rnd else x
 
     def rc(self, z):
-        return cbf16(z) if self.rnd else z
+        return (self.q(z.real) + 1j * self.q(z.imag)) if self.rnd else z
 
     def mat(self, a):
-        return bf16(a) if self.rnd else a
+        return self.q(a) if self.rnd else a
 
-    # truncated transforms, axis by axis in the GPU's order (k, j, i)
-    def fwd_modes(self, h):
-        F = self.F
+    # truncated transforms, axis by axis in the GPU's order (k, j, i).  The
+    # backward pass keeps the 1/N of the first axis only (N^2 F3 h).
+    def fwd_modes(self, h, bwd: bool = False):
+        F, F23 = self.F, (self.Fu if bwd else self.F)
         t1 = self.rc(np.einsum("ak,bijkc->bijac", F, h))
-        t2 = self.rc(np.einsum("aj,bijkc->biakc", F, t1))
-        return self.rc(np.einsum("ai,bijkc->bajkc", F, t2))
+        t2 = self.rc(np.einsum("aj,bijkc->biakc", F23, t1))
+        return self.rc(np.einsum("ai,bijkc->bajkc", F23, t2))
 
     def inv_modes(self, y):
+        """Real part of the inverse transform (FP64; the forward pass stores it as BF16)."""
         G = self.G
         u1 = self.rc(np.einsum("ia,bajkc->bijkc", G, y))
         u2 = self.rc(np.einsum("ja,biakc->bijkc", G, u1))
@@ -181,7 +193,7 @@ class Net:
         for l in range(sp.L):
             X = self.fwd_modes(h)
             Y = self.mix(p[f"R{l}"], X)
-            S = self.inv_modes(Y)
+            S = self.r(self.inv_modes(Y))   # stored as BF16 on the device
             z = np.einsum("dc,bijkc->bijkd", self.mat(p[f"W{l}"]), h) + p[f"b{l}"] + S
             h = self.r(gelu(z) if (sp.kind == 0 and l < sp.L - 1) else z)
             cache["X"].append(X)
@@ -213,7 +225,9 @@ class Net:
         den = den + floor * den.mean()
         r = y - t
         loss = float(((r.reshape(B, -1) ** 2).sum(axis=1) / den).sum() / B)
-        dy = 2.0 * r / (den * B)[:, None, None, None]
+        # the device carries gradients times the loss scale gs = B mean(den) / 2
+        gs = 0.5 * den.sum()
+        dy = 2.0 * r / (den * B)[:, None, None, None] * gs
         g = {k: np.zeros_like(v) for k, v in p.items()}
         g["c2"][0] = dy.sum()
         u = c["u"]
@@ -231,7 +245,6 @@ class Net:
         hL = c["h"][sp.L]
         g["Q1"] = np.einsum("bijke,bijkc->ec", du, hL)
         dh = np.einsum("ec,bijke->bijkc", self.mat(p["Q1"]), du)
-        n3 = sp.N ** 3
         for l in range(sp.L - 1, -1, -1):
             dz = dh * gelu_grad(c["z"][l]) if (sp.kind == 0 and l < sp.L - 1) else dh
             g[f"b{l}"] = dz.sum(axis=(0, 1, 2, 3))
@@ -239,18 +252,19 @@ class Net:
             hl = c["h"][l]
             g[f"W{l}"] = np.einsum("bijkd,bijkc->dc", dz, hl)
             dh = np.einsum("dc,bijkd->bijkc", self.mat(p[f"W{l}"]), dz)
-            # spectral path: with GY = F3 dz (F carries 1/N per axis), the
-            # complex gradient of Y is N^3 GY, so dR = N^3 sum Re(GY conj X)
-            GY = self.fwd_modes(dz)
+            # spectral path: GY = N^2 F3 dz (the backward transform keeps
+            # one 1/N); the complex gradient of Y is N^3 F3 dz, so
+            # dR = N sum Re(GY conj X), and dh += Re(G3 R^T GY) / N^2
+            GY = self.fwd_modes(dz, bwd=True)
             X = c["X"][l]
             per_mode = np.einsum("bxyzd,bxyzc->xyzdc", GY.real, X.real) + \
                 np.einsum("bxyzd,bxyzc->xyzdc", GY.imag, X.imag)
             dR = np.zeros_like(p[f"R{l}"])
             np.add.at(dR, self.cls, per_mode)
-            g[f"R{l}"] = n3 * dR
+            g[f"R{l}"] = sp.N * dR
             GX = self.mix(p[f"R{l}"], GY, transpose=True)
-            dh = dh + self.inv_modes(GX)
+            dh = dh + self.inv_modes(GX) / (sp.N * sp.N)
         x = c["x"]
         g["P"] = np.einsum("bijkc,bijk->c", dh, x)
         g["bP"] = dh.sum(axis=(0, 1, 2, 3))
-        return loss, g
+        return loss, {k: val / gs for k, val in g.items()}

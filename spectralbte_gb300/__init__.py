@@ -146,7 +146,8 @@ def lib() -> C.CDLL:
                                         C.POINTER(C.c_void_p), C.POINTER(C.c_int), i, v]),
         "spectral_plan_conv_time": (i, [v, _dp, C.POINTER(C.c_int)]),
         # learned operator
-        "spectral_fno_create": (i, [pp, i, i, i, i, i, i, C.c_ulonglong]),
+        "spectral_fno_create": (i, [pp, i, i, i, i, i, i, i, C.c_ulonglong]),
+        "spectral_fno_precision": (i, [v]),
         "spectral_fno_destroy": (i, [v]),
         "spectral_fno_num_params": (C.c_longlong, [v]),
         "spectral_fno_num_classes": (i, [v]),
@@ -159,6 +160,7 @@ def lib() -> C.CDLL:
         "spectral_fno_loss_grad": (i, [v, v, v, i, _dp, C.POINTER(C.c_float)]),
         "spectral_fno_train_step": (i, [v, v, v, i, C.c_float, _dp, v]),
         "spectral_plan_set_learned": (i, [v, v, d, i]),
+        "spectral_moments_device": (i, [v, v, i, v, v]),
         "spectral_plan_learned_stats": (i, [v, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong),
                                             C.POINTER(C.c_longlong), _dp]),
     }
@@ -439,6 +441,11 @@ class Plan:
     def launch(self, stream: int = 0):
         _check(self.L.spectral_graph_launch(self.h, _stream(stream)), "spectral_graph_launch")
 
+    def moments_device(self, f, B: int, out, stream: int = 0):
+        """out[B][8] = rho, u_x, u_y, u_z, T, rho T, E+, E- of each instance."""
+        _check(self.L.spectral_moments_device(self.h, _ptr(f), B, _ptr(out), _stream(stream)),
+               "moments_device")
+
     def set_learned(self, net: Optional["FourierOperator"], tol: float = 1e-3,
                     check_every: int = 1):
         """Use net for computeQ with LEARNED, spot-checked against the plain
@@ -473,14 +480,14 @@ class FourierOperator:
     and backward kernels."""
 
     def __init__(self, N: int, width: int = 64, modes: int = 12, layers: int = 4,
-                 hidden: int = 128, seed: int = 1, kind: int = 0):
+                 hidden: int = 128, seed: int = 1, kind: int = 0, precision: int = 1):
         self.L = lib()
         self.N, self.n3 = N, N ** 3
         self.width, self.modes, self.layers, self.hidden = width, modes, layers, hidden
-        self.kind = kind
+        self.kind, self.precision = kind, precision
         h = C.c_void_p()
         _check(self.L.spectral_fno_create(C.byref(h), N, width, modes, layers, hidden, kind,
-                                          int(seed)), "spectral_fno_create")
+                                          precision, int(seed)), "spectral_fno_create")
         self.h = h
         self.nparams = int(self.L.spectral_fno_num_params(h))
         self.nclasses = int(self.L.spectral_fno_num_classes(h))
@@ -545,13 +552,15 @@ class FourierOperator:
     def save(self, path: str):
         np.savez(path, theta=self.get_params(), sigma=self.output_scale,
                  shape=np.array([self.N, self.width, self.modes, self.layers, self.hidden,
-                                 self.kind]))
+                                 self.kind, self.precision]))
 
     @classmethod
     def load(cls, path: str) -> "FourierOperator":
         d = np.load(path)
-        N, width, modes, layers, hidden, kind = (int(x) for x in d["shape"])
-        net = cls(N, width, modes, layers, hidden, kind=kind)
+        shape = [int(x) for x in d["shape"]]
+        N, width, modes, layers, hidden, kind = shape[:6]
+        precision = shape[6] if len(shape) > 6 else 0   # BF16 before the precision field
+        net = cls(N, width, modes, layers, hidden, kind=kind, precision=precision)
         net.set_params(d["theta"])
         net.output_scale = float(d["sigma"])
         return net

@@ -1093,6 +1093,15 @@ int spectral_graph_capture(spectral_plan *p, int kind, double *f_dev, int B, dou
         return set_error(kErrNotInit, "graph capture of a 1D step needs spectral_1d_setup"),
                kErrNotInit;
     SBTE_TRY(ensure_step(p, nb));
+    if (flags & SPECTRAL_LEARNED) {
+        // a spot check reads its result on the host, which a graph cannot do
+        if (!p->fno || p->levery != 0)
+            return set_error(kErrUnsupported,
+                             "graph capture with SPECTRAL_LEARNED needs a learned operator "
+                             "attached with check_every = 0"),
+                   kErrUnsupported;
+        SBTE_TRY(fno_reserve(p->fno, nb));
+    }
     if (flags & SPECTRAL_FP32) {
         SBTE_TRY(ensure32(p, nb));
         SBTE_TRY(ensure_w32(p->W, p->stream));
@@ -1293,6 +1302,19 @@ int spectral_plan_conv_time(spectral_plan *p, double *total_ms, int *launches)
     *total_ms = tot;
     *launches = (int)p->prof_used;
     p->prof_used = 0;
+    return kOk;
+}
+
+int spectral_moments_device(spectral_plan *p, const double *f_dev, int B, double *out_dev,
+                            void *stream)
+{
+    if (!p || !f_dev || !out_dev || B < 0) {
+        set_error(kErrArg, "spectral_moments_device: bad arguments");
+        return kErrArg;
+    }
+    SBTE_CUDA(cudaSetDevice(p->device));
+    SBTE_LAUNCH(moments_batch(f_dev, B, p->N, p->d_v, p->mom_mass, p->mom_KB, out_dev,
+                              (cudaStream_t)stream), 1);
     return kOk;
 }
 

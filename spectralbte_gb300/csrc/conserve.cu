@@ -209,6 +209,52 @@ maxwellian_kernel(const double *__restrict__ f, double *__restrict__ M,
     }
 }
 
+// The per-instance moments that write_streams / write_streams_inhom print
+// (output.c:156-213,295-404): getDensity, getBulkVelocity, getTemperature
+// (momentRoutines.c:58-69,116-141,168-185), getPressure = rho T (:187-190)
+// and getEnergy's positive and negative parts (:146-165).  out[8 b + ...] =
+// {rho, u_x, u_y, u_z, T, rho T, E+, E-}.  One CTA per instance, FP64.
+__global__ void __launch_bounds__(kThreads)
+moments_kernel(const double *__restrict__ f, int N, const double *__restrict__ v, double mass,
+               double KB, double *__restrict__ out)
+{
+    __shared__ double red[32 * 4];
+    const long long n3 = (long long)N * N * N;
+    const double *fb = f + (long long)blockIdx.x * n3;
+    const double dv = v[1] - v[0];
+    const double dv3 = dv * dv * dv;
+    double s[4] = {0, 0, 0, 0};
+    for (long long x = threadIdx.x; x < n3; x += blockDim.x) {
+        const int i = (int)(x / (N * N)), j = (int)((x / N) % N), k = (int)(x % N);
+        const double w = dv3 * wt(i, N) * wt(j, N) * wt(k, N);
+        const double fx = fb[x];
+        s[0] += w * fx;
+        s[1] += v[i] * w * fx;
+        s[2] += v[j] * w * fx;
+        s[3] += v[k] * w * fx;
+    }
+    block_sum<4>(s, red);
+    const double rho = mass * s[0];
+    const double u0 = mass * (s[1] / rho), u1 = mass * (s[2] / rho), u2 = mass * (s[3] / rho);
+    double t[3] = {0, 0, 0};
+    for (long long x = threadIdx.x; x < n3; x += blockDim.x) {
+        const int i = (int)(x / (N * N)), j = (int)((x / N) % N), k = (int)(x % N);
+        const double w = dv3 * wt(i, N) * wt(j, N) * wt(k, N);
+        const double fx = fb[x];
+        t[0] += ((v[i] - u0) * (v[i] - u0) + (v[j] - u1) * (v[j] - u1) +
+                 (v[k] - u2) * (v[k] - u2)) * w * fx;
+        const double e = w * fx * (v[i] * v[i] + v[j] * v[j] + v[k] * v[k]);
+        if (e > 0) t[1] += e; else t[2] -= e;
+    }
+    block_sum<3>(t, red);
+    if (threadIdx.x == 0) {
+        const double T = (mass * mass / KB) * (t[0] / (3.0 * rho));
+        double *o = out + 8 * (long long)blockIdx.x;
+        o[0] = rho; o[1] = u0; o[2] = u1; o[3] = u2; o[4] = T; o[5] = rho * T;
+        o[6] = t[1]; o[7] = t[2];
+    }
+}
+
 __global__ void axpy_kernel(double *__restrict__ y, const double *__restrict__ x,
                             const double *__restrict__ q, double a_y, double a_x,
                             double a_q, long long n)
@@ -247,6 +293,14 @@ cudaError_t maxwellian_split(const double *f, double *M, double *g,
     if (B < 1) return cudaSuccess;
     maxwellian_kernel<<<B, kThreads, 0, st>>>(f, M, g, Mref, N, v, mass, KB,
                                               moments_out);
+    return cudaGetLastError();
+}
+
+cudaError_t moments_batch(const double *f, int B, int N, const double *v, double mass,
+                          double KB, double *out, cudaStream_t st)
+{
+    if (B < 1) return cudaSuccess;
+    moments_kernel<<<B, kThreads, 0, st>>>(f, N, v, mass, KB, out);
     return cudaGetLastError();
 }
 

@@ -38,6 +38,7 @@
 #include <vector>
 
 using sbte::fno::bf16;
+using sbte::fno::f16;
 
 namespace sbte {
 namespace fno {
@@ -114,11 +115,11 @@ __global__ void from_pb_kernel(const float *__restrict__ y, const float *__restr
     }
 }
 
-__device__ __forceinline__ void st_bf16x8(bf16 *dst, const float (&v)[8])
+template <typename E> __device__ __forceinline__ void st_e8(E *dst, const float (&v)[8])
 {
-    __nv_bfloat162 q[4];
+    typename Elem<E>::T2 q[4];
 #pragma unroll
-    for (int i = 0; i < 4; i++) q[i] = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
+    for (int i = 0; i < 4; i++) q[i] = Elem<E>::cvt2(v[2 * i], v[2 * i + 1]);
     *reinterpret_cast<uint4 *>(dst) = *reinterpret_cast<uint4 *>(q);
 }
 __device__ __forceinline__ void ld_f32x8(const float *src, float (&v)[8])
@@ -129,9 +130,10 @@ __device__ __forceinline__ void ld_f32x8(const float *src, float (&v)[8])
     v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
 }
 
-// h[p][c][b] = bf16(P[c] x[p][b] + bP[c]); 8 instances per thread.
+// h[p][c][b] = E(P[c] x[p][b] + bP[c]); 8 instances per thread.
+template <typename E>
 __global__ void lift_kernel(const float *__restrict__ x, const float *__restrict__ Pw,
-                            const float *__restrict__ bP, bf16 *__restrict__ h, long long P,
+                            const float *__restrict__ bP, E *__restrict__ h, long long P,
                             int C, int Bp)
 {
     const long long n8 = P * C * Bp / 8;
@@ -144,7 +146,7 @@ __global__ void lift_kernel(const float *__restrict__ x, const float *__restrict
         ld_f32x8(x + p * Bp + b, v);
 #pragma unroll
         for (int j = 0; j < 8; j++) v[j] = Pw[c] * v[j] + bP[c];
-        st_bf16x8(h + e, v);
+        st_e8(h + e, v);
     }
 }
 
@@ -166,9 +168,10 @@ template <int MAXC> struct ChanAcc {
     }
 };
 
-// dZ = bf16(dH * gelu'(Z)) (or dH where Z == nullptr); db[c] += sum dZ.
+// dZ = E(dH * gelu'(Z)) (or dH where Z == nullptr); db[c] += sum dZ.
+template <typename E>
 __global__ void gelu_bwd_kernel(const float *__restrict__ dH, const float *__restrict__ Z,
-                                bf16 *__restrict__ dZ, float *db, long long P, int C, int Bp)
+                                E *__restrict__ dZ, float *db, long long P, int C, int Bp)
 {
     __shared__ float sdb[128];
     ChanAcc<128> acc;
@@ -189,14 +192,15 @@ __global__ void gelu_bwd_kernel(const float *__restrict__ dH, const float *__res
 #pragma unroll
         for (int j = 0; j < 8; j++) s += v[j];
         atomicAdd(&sdb[c], s);
-        st_bf16x8(dZ + e, v);
+        st_e8(dZ + e, v);
     }
     acc.flush(db, C);
 }
 
-// Projection backward: dU = bf16(dy q2 gelu'(u)); dq2 += dy gelu(u); dc1 += dy q2 gelu'(u).
+// Projection backward: dU = E(dy q2 gelu'(u)); dq2 += dy gelu(u); dc1 += dy q2 gelu'(u).
+template <typename E>
 __global__ void proj_bwd_kernel(const float *__restrict__ U, const float *__restrict__ dy,
-                                const float *__restrict__ q2, bf16 *__restrict__ dU, float *dq2,
+                                const float *__restrict__ q2, E *__restrict__ dU, float *dq2,
                                 float *dc1, long long P, int Hd, int Bp)
 {
     __shared__ float s1[128], s2[128];
@@ -221,7 +225,7 @@ __global__ void proj_bwd_kernel(const float *__restrict__ U, const float *__rest
         }
         atomicAdd(&s1[c], sq);
         atomicAdd(&s2[c], sc);
-        st_bf16x8(dU + e, o);
+        st_e8(dU + e, o);
     }
     a1.flush(dq2, Hd);
     a2.flush(dc1, Hd);
@@ -230,8 +234,9 @@ __global__ void proj_bwd_kernel(const float *__restrict__ U, const float *__rest
 // Bilinear readout backward: for row r with partner r ^ 8 and pair
 // e = 8 (r / 16) + r % 8, dU_r = dy q2[e] u_{r^8}; dc1[r] += dU_r;
 // dq2[e] += dy u_l u_r (counted on the left row).
+template <typename E>
 __global__ void proj_bwd_bil_kernel(const float *__restrict__ U, const float *__restrict__ dy,
-                                    const float *__restrict__ q2, bf16 *__restrict__ dU,
+                                    const float *__restrict__ q2, E *__restrict__ dU,
                                     float *dq2, float *dc1, long long P, int Hd, int Bp)
 {
     __shared__ float s1[64], s2[128];
@@ -260,7 +265,7 @@ __global__ void proj_bwd_bil_kernel(const float *__restrict__ U, const float *__
         }
         if (!(r & 8)) atomicAdd(&s1[pe], sq);
         atomicAdd(&s2[r], sc);
-        st_bf16x8(dU + e, o);
+        st_e8(dU + e, o);
     }
     a1.flush(dq2, Hd / 2);
     a2.flush(dc1, Hd);
@@ -296,8 +301,12 @@ __global__ void lift_bwd_kernel(const float *__restrict__ dH, const float *__res
     a2.flush(dbP, C);
 }
 
-// den[b] += eps * mean over the B real instances of den (the loss floor).
-__global__ void den_floor_kernel(float *den, int B, float eps)
+// den[b] += eps * mean over the B real instances of den (the loss floor);
+// gs[0] = B mean(den) / 2, the loss scale: the backward pass carries
+// gradients multiplied by gs (the loss gradient 2 (y - t) / (den_b B) times
+// gs is O(y - t)), so that they stay in the 16-bit range; Adam and the
+// gradient read-back divide by gs.
+__global__ void den_finish_kernel(float *den, int B, float eps, float *gs)
 {
     __shared__ float red[32];
     float s = 0.f;
@@ -309,6 +318,7 @@ __global__ void den_floor_kernel(float *den, int B, float eps)
     for (int w = 0; w < (int)(blockDim.x >> 5); w++) tot += red[w];
     __syncthreads();
     for (int b = threadIdx.x; b < B; b += blockDim.x) den[b] += eps * tot / (float)B;
+    if (threadIdx.x == 0) gs[0] = 0.5f * tot * (1.f + eps);
 }
 
 // den[b] = sum_p t[p][b]^2.
@@ -329,9 +339,11 @@ __global__ void den_kernel(const float *__restrict__ t, float *den, long long P,
 // dy = 2 (y - t) / (den_b B) for b < B (0 for padding); loss += sum (y-t)^2 / (den_b B);
 // dc2 += sum dy.
 __global__ void loss_kernel(const float *__restrict__ y, const float *__restrict__ t,
-                            const float *__restrict__ den, float *__restrict__ dy,
-                            double *loss, float *dc2, long long n, int B, int Bp)
+                            const float *__restrict__ den, const float *__restrict__ gs,
+                            float *__restrict__ dy, double *loss, float *dc2, long long n, int B,
+                            int Bp)
 {
+    const float scale = gs[0];
     __shared__ double r1[32];
     __shared__ float r2[32];
     double l = 0.0;
@@ -343,7 +355,7 @@ __global__ void loss_kernel(const float *__restrict__ y, const float *__restrict
         if (b < B) {
             const float r = y[i] - t[i];
             const float inv = 1.f / (den[b] * (float)B);
-            d = 2.f * r * inv;
+            d = 2.f * r * inv * scale;
             l += (double)r * r * inv;
         }
         dy[i] = d;
@@ -371,12 +383,14 @@ __global__ void loss_kernel(const float *__restrict__ y, const float *__restrict
 }
 
 __global__ void adam_kernel(float *__restrict__ p, const float *__restrict__ g,
-                            float *__restrict__ m, float *__restrict__ v, long long n, float lr,
-                            float b1, float b2, float eps, float c1, float c2)
+                            const float *__restrict__ gs, float *__restrict__ m,
+                            float *__restrict__ v, long long n, float lr, float b1, float b2,
+                            float eps, float c1, float c2)
 {
+    const float inv = 1.f / gs[0];
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
-        const float gi = g[i];
+        const float gi = g[i] * inv;
         const float mi = b1 * m[i] + (1.f - b1) * gi;
         const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
         m[i] = mi;
@@ -456,15 +470,15 @@ bool sa_bounds_ok(const SaArgs &a, bool AC)
     return true;
 }
 
-template <int MT, int BN, int WM, int WN, bool AC, bool BC, int EPI>
+template <typename E, int MT, int BN, int WM, int WN, bool AC, bool BC, int EPI, int ST = 3>
 cudaError_t launch_sa(SaArgs a, cudaStream_t st)
 {
     a.KP = (a.K + 15) / 16 * 16;
     if (a.M > MT || a.KP > 128 || a.Nn % 8 != 0 || !view_ok(a.B, a.B.p) ||
         !view_ok(a.C, a.C.p) || !sa_bounds_ok(a, AC))
         return cudaErrorInvalidValue;
-    const size_t sm = gemm_sa_smem<MT, BN, WM, WN, AC, BC, EPI>(a.KP);
-    auto kern = gemm_sa_kernel<MT, BN, WM, WN, AC, BC, EPI>;
+    const size_t sm = gemm_sa_smem<MT, BN, WM, WN, AC, BC, EPI, ST>(a.KP);
+    auto kern = gemm_sa_kernel<E, MT, BN, WM, WN, AC, BC, EPI, ST>;
     if (sm > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)sm);
@@ -477,7 +491,7 @@ cudaError_t launch_sa(SaArgs a, cudaStream_t st)
     return cudaGetLastError();
 }
 
-template <int MT, int NT, int WM, int WN>
+template <typename E, int MT, int NT, int WM, int WN>
 cudaError_t launch_nt(NtArgs a, cudaStream_t st)
 {
     if (a.M > MT || a.N > NT || a.K % 8 || a.a_w % 8 || a.b_w % 8 || a.a_m % 8 || a.b_n % 8 ||
@@ -494,7 +508,7 @@ cudaError_t launch_nt(NtArgs a, cudaStream_t st)
         return cudaErrorInvalidValue;
     const long long total = ((a.K + a.KC - 1) / a.KC) * a.nz;
     const int grid = (int)std::min<long long>(total, 152LL * 4);
-    gemm_nt_kernel<MT, NT, WM, WN><<<grid, WM * WN * 32, 0, st>>>(a);
+    gemm_nt_kernel<E, MT, NT, WM, WN><<<grid, WM * WN * 32, 0, st>>>(a);
     add_launches(1);
     return cudaGetLastError();
 }
@@ -518,6 +532,7 @@ SaArgs sa_base(const float *A, long long sAm, long long sAk, long long imA, int 
     a.K = K;
     a.nz = 1;
     a.nz2 = 1;
+    a.alpha = 1.f;
     return a;
 }
 
@@ -540,17 +555,22 @@ struct spectral_fno_s {
     float floor_eps = 0.f;  // loss: |y - t|^2 / (|t|^2 + floor_eps * mean_b |t_b|^2)
     float *params = nullptr, *grads = nullptr, *am = nullptr, *av = nullptr;
     long long adam_t = 0;
+    int prec = 0;                      // 0: BF16 elements, 1: FP16 elements
     float *F = nullptr, *G = nullptr;  // DFT axis matrices
+    float *Fu = nullptr;               // F without its 1/N (backward transform)
+    float *gs = nullptr;               // loss scale on the device
     int *cls = nullptr;                // class of batch z = (mi*2+part)*Km^2 + mjk
     // activations (capacity cap instances)
     int cap = 0;
     bool cap_train = false;
     float *s = nullptr, *x = nullptr, *t = nullptr, *den = nullptr, *y = nullptr, *dy = nullptr;
-    bf16 *H[9] = {};
+    // 16-bit elements (BF16 or FP16, by prec)
+    uint16_t *H[9] = {};
     float *Z[8] = {};
-    float *S = nullptr, *Up = nullptr, *dH = nullptr;
-    bf16 *T1 = nullptr, *T2 = nullptr, *X[8] = {}, *Y = nullptr, *U1 = nullptr, *U2 = nullptr;
-    bf16 *dU = nullptr, *dZ = nullptr, *GY = nullptr, *GX = nullptr;
+    float *Up = nullptr, *dH = nullptr;
+    uint16_t *S = nullptr;
+    uint16_t *T1 = nullptr, *T2 = nullptr, *X[8] = {}, *Y = nullptr, *U1 = nullptr, *U2 = nullptr;
+    uint16_t *dU = nullptr, *dZ = nullptr, *GY = nullptr, *GX = nullptr;
     double *d_loss = nullptr;
     std::vector<void *> owned;
 
@@ -558,7 +578,8 @@ struct spectral_fno_s {
     {
         for (void *q : owned) cudaFree(q);
         owned.clear();
-        s = x = t = den = y = dy = S = Up = dH = nullptr;
+        s = x = t = den = y = dy = Up = dH = nullptr;
+        S = nullptr;
         for (auto &q : H) q = nullptr;
         for (auto &q : Z) q = nullptr;
         for (auto &q : X) q = nullptr;
@@ -570,7 +591,7 @@ struct spectral_fno_s {
     {
         cudaSetDevice(device);
         free_acts();
-        for (float *q : {params, grads, am, av, F, G}) cudaFree(q);
+        for (float *q : {params, grads, am, av, F, G, Fu, gs}) cudaFree(q);
         cudaFree(cls);
     }
 };
@@ -648,7 +669,7 @@ int ensure(spectral_fno_s *n, int Bp, bool train)
     return kOk;
 }
 
-bf16 *Hbuf(spectral_fno_s *n, int l, bool train) { return train ? n->H[l] : n->H[l & 1]; }
+uint16_t *Hbuf(spectral_fno_s *n, int l, bool train) { return train ? n->H[l] : n->H[l & 1]; }
 
 // Element counts of the activation buffers for Bp instances.
 struct Ext {
@@ -675,44 +696,50 @@ void set_ext(SaArgs &a, long long eA, long long eB, long long eC)
     a.extC = eC;
 }
 
-// The truncated forward transform of in ([p][c][b], BF16) into out
-// ([mi][2][mj mk][c][b]): three axis passes with F (fno.cu header).
-int spectral_fwd(spectral_fno_s *n, const bf16 *in, bf16 *out, int Bp, cudaStream_t st)
+// The truncated forward transform of in ([p][c][b]) into out
+// ([mi][2][mj mk][c][b]): three axis passes with F (fno.cu header).  The
+// backward pass (bwd) keeps the 1/N of the first axis only and applies the
+// unscaled matrix on the other two, so that transforms of small gradients
+// stay far from the 16-bit subnormal range: out is then N^2 times F3 in.
+template <typename E>
+int spectral_fwd(spectral_fno_s *n, const uint16_t *in, uint16_t *out, bool bwd, int Bp,
+                 cudaStream_t st)
 {
     const long long N = n->N, Km = n->Km, CB = (long long)n->C * Bp;
-    const float *F = n->F;
-    const Ext E(n, Bp);
+    const float *F = n->F, *F23 = bwd ? n->Fu : n->F;
+    const Ext ext(n, Bp);
     {  // axis k, real input
         SaArgs a = sa_base(F, N, 1, Km * N, (int)Km, (int)N);
         a.B = sv(in, CB, CB, N * CB);
         a.C = sv(n->T1, CB, CB, 2 * Km * CB, Km * CB);
         a.Nn = N * N * CB;
-        set_ext(a, E.F, E.act, E.t1);
-        FNO_LAUNCH((launch_sa<16, 128, 1, 4, true, false, kEpiCplxBF16>(a, st)));
+        set_ext(a, ext.F, ext.act, ext.t1);
+        FNO_LAUNCH((launch_sa<E, 16, 128, 1, 4, true, false, kEpiCplxBF16>(a, st)));
     }
     {  // axis j
-        SaArgs a = sa_base(F, N, 1, Km * N, (int)Km, (int)N);
+        SaArgs a = sa_base(F23, N, 1, Km * N, (int)Km, (int)N);
         a.B = sv(n->T1, 2 * Km * CB, Km * CB, N * 2 * Km * CB, Km * CB);
         a.C = sv(n->T2, Km * CB, Km * CB, 2 * Km * Km * CB, Km * Km * CB);
         a.Nn = N * Km * CB;
-        set_ext(a, E.F, E.t1, E.t2);
-        FNO_LAUNCH((launch_sa<16, 128, 1, 4, true, true, kEpiCplxBF16>(a, st)));
+        set_ext(a, ext.F, ext.t1, ext.t2);
+        FNO_LAUNCH((launch_sa<E, 16, 128, 1, 4, true, true, kEpiCplxBF16>(a, st)));
     }
     {  // axis i
-        SaArgs a = sa_base(F, N, 1, Km * N, (int)Km, (int)N);
+        SaArgs a = sa_base(F23, N, 1, Km * N, (int)Km, (int)N);
         const long long w = Km * Km * CB;
         a.B = sv(n->T2, 2 * w, w, 0, w);
         a.C = sv(out, 2 * w, w, 0, w);
         a.Nn = w;
-        set_ext(a, E.F, E.t2, E.xm);
-        FNO_LAUNCH((launch_sa<16, 128, 1, 4, true, true, kEpiCplxBF16>(a, st)));
+        set_ext(a, ext.F, ext.t2, ext.xm);
+        FNO_LAUNCH((launch_sa<E, 16, 128, 1, 4, true, true, kEpiCplxBF16>(a, st)));
     }
     return kOk;
 }
 
 // Mode mix out[z][d][b] = sum_c R[cls z] (transposed when tr) in[z][c][b].
-int mode_mix(spectral_fno_s *n, const float *R, bool tr, const bf16 *in, bf16 *out, int Bp,
-             cudaStream_t st)
+template <typename E>
+int mode_mix(spectral_fno_s *n, const float *R, bool tr, const uint16_t *in, uint16_t *out,
+             int Bp, cudaStream_t st)
 {
     const long long C = n->C, Km = n->Km, CB = C * Bp;
     SaArgs a = sa_base(R, tr ? 1 : C, tr ? C : 1, 0, (int)C, (int)C);
@@ -724,71 +751,75 @@ int mode_mix(spectral_fno_s *n, const float *R, bool tr, const bf16 *in, bf16 *o
     a.Nn = Bp;
     a.nz = (int)(2 * Km * Km * Km);
     a.nz2 = (int)(Km * Km);
-    const Ext E(n, Bp);
-    set_ext(a, (long long)n->ncls * C * C, E.xm, E.xm);
-    FNO_LAUNCH((launch_sa<64, 64, 2, 2, false, false, kEpiBF16>(a, st)));
+    const Ext ext(n, Bp);
+    set_ext(a, (long long)n->ncls * C * C, ext.xm, ext.xm);
+    FNO_LAUNCH((launch_sa<E, 64, 64, 2, 2, false, false, kEpiBF16>(a, st)));
     return kOk;
 }
 
 // The inverse transform of in ([mi][2][mj mk][c][b]) to the real part on
-// the grid, stored to (or, when acc, added into) out [p][c][b] FP32.
-int spectral_inv(spectral_fno_s *n, const bf16 *in, float *out, bool acc, int Bp,
-                 cudaStream_t st)
+// the grid [p][c][b]: stored as 16-bit elements to out16 (the forward pass),
+// or added, times alpha, into the FP32 out32 (the backward pass).
+template <typename E>
+int spectral_inv(spectral_fno_s *n, const uint16_t *in, uint16_t *out16, float *out32,
+                 float alpha, int Bp, cudaStream_t st)
 {
     const long long N = n->N, Km = n->Km, CB = (long long)n->C * Bp;
     const float *G = n->G;
-    const Ext E(n, Bp);
+    const Ext ext(n, Bp);
     {  // axis i
         SaArgs a = sa_base(G, Km, 1, N * Km, (int)N, (int)Km);
         const long long w = Km * Km * CB;
         a.B = sv(in, 2 * w, w, 0, w);
         a.C = sv(n->U1, 2 * w, w, 0, w);
         a.Nn = w;
-        set_ext(a, E.G, E.xm, E.t2);
-        FNO_LAUNCH((launch_sa<32, 128, 1, 4, true, true, kEpiCplxBF16>(a, st)));
+        set_ext(a, ext.G, ext.xm, ext.t2);
+        FNO_LAUNCH((launch_sa<E, 32, 128, 1, 4, true, true, kEpiCplxBF16>(a, st)));
     }
     {  // axis j
         SaArgs a = sa_base(G, Km, 1, N * Km, (int)N, (int)Km);
         a.B = sv(n->U1, Km * CB, Km * CB, 2 * Km * Km * CB, Km * Km * CB);
         a.C = sv(n->U2, 2 * Km * CB, Km * CB, N * 2 * Km * CB, Km * CB);
         a.Nn = N * Km * CB;
-        set_ext(a, E.G, E.t2, E.t1);
-        FNO_LAUNCH((launch_sa<32, 128, 1, 4, true, true, kEpiCplxBF16>(a, st)));
+        set_ext(a, ext.G, ext.t2, ext.t1);
+        FNO_LAUNCH((launch_sa<E, 32, 128, 1, 4, true, true, kEpiCplxBF16>(a, st)));
     }
     {  // axis k, real part
         SaArgs a = sa_base(G, Km, 1, N * Km, (int)N, (int)Km);
         a.B = sv(n->U2, CB, CB, 2 * Km * CB, Km * CB);
-        a.C = sv(out, CB, CB, N * CB);
+        a.C = sv(out32 ? (const void *)out32 : (const void *)out16, CB, CB, N * CB);
         a.Nn = N * N * CB;
-        set_ext(a, E.G, E.t1, E.act);
-        if (acc)
-            FNO_LAUNCH((launch_sa<32, 128, 1, 4, true, true, kEpiAccF32>(a, st)));
+        a.alpha = alpha;
+        set_ext(a, ext.G, ext.t1, ext.act);
+        if (out32)
+            FNO_LAUNCH((launch_sa<E, 32, 128, 1, 4, true, true, kEpiAccF32>(a, st)));
         else
-            FNO_LAUNCH((launch_sa<32, 128, 1, 4, true, true, kEpiF32>(a, st)));
+            FNO_LAUNCH((launch_sa<E, 32, 128, 1, 4, true, true, kEpiBF16>(a, st)));
     }
     return kOk;
 }
 
-template <typename T>
+template <typename E, typename T>
 int forward(spectral_fno_s *n, const T *f, int B, int Bp, bool train, cudaStream_t st)
 {
     const long long P = n->P, C = n->C, Hd = n->Hd;
     const float *prm = n->params;
-    const Ext E(n, Bp);
+    const Ext ext(n, Bp);
     inst_max_kernel<T><<<Bp, 256, 0, st>>>(f, P, B, n->s);
     to_pb_kernel<T><<<dim3((unsigned)((P + 31) / 32), (unsigned)((Bp + 31) / 32)),
                       dim3(32, 8), 0, st>>>(f, n->s, 1, 1.f, B, Bp, P, n->x);
     const long long n8 = P * C * Bp / 8;
-    lift_kernel<<<ew_grid(n8), kEw, 0, st>>>(n->x, prm + n->oP, prm + n->obP, Hbuf(n, 0, train),
-                                              P, (int)C, Bp);
+    lift_kernel<E><<<ew_grid(n8), kEw, 0, st>>>(n->x, prm + n->oP, prm + n->obP,
+                                                 reinterpret_cast<E *>(Hbuf(n, 0, train)), P,
+                                                 (int)C, Bp);
     add_launches(3);
     FNO_LAUNCH(cudaGetLastError());
     for (int l = 0; l < n->L; l++) {
-        bf16 *hin = Hbuf(n, l, train), *hout = Hbuf(n, l + 1, train);
-        bf16 *xl = train ? n->X[l] : n->X[0];
-        FNO_TRY(spectral_fwd(n, hin, xl, Bp, st));
-        FNO_TRY(mode_mix(n, prm + n->oR[l], false, xl, n->Y, Bp, st));
-        FNO_TRY(spectral_inv(n, n->Y, n->S, false, Bp, st));
+        uint16_t *hin = Hbuf(n, l, train), *hout = Hbuf(n, l + 1, train);
+        uint16_t *xl = train ? n->X[l] : n->X[0];
+        FNO_TRY(spectral_fwd<E>(n, hin, xl, false, Bp, st));
+        FNO_TRY(mode_mix<E>(n, prm + n->oR[l], false, xl, n->Y, Bp, st));
+        FNO_TRY(spectral_inv<E>(n, n->Y, n->S, nullptr, 1.f, Bp, st));
         SaArgs a = sa_base(prm + n->oW[l], C, 1, 0, (int)C, (int)C);
         a.B = sv(hin, Bp, Bp, C * Bp);
         a.C = sv(hout, Bp, Bp, C * Bp);
@@ -799,8 +830,8 @@ int forward(spectral_fno_s *n, const T *f, int B, int Bp, bool train, cudaStream
         a.zst = (train && gelu) ? n->Z[l] : nullptr;
         a.hout = hout;
         a.act = gelu ? 1 : 0;
-        set_ext(a, E.prm - n->oW[l], E.act, E.act);
-        FNO_LAUNCH((launch_sa<64, 128, 2, 2, false, false, kEpiLayer>(a, st)));
+        set_ext(a, ext.prm - n->oW[l], ext.act, ext.act);
+        FNO_LAUNCH((launch_sa<E, 64, 64, 2, 2, false, false, kEpiLayer>(a, st)));
     }
     SaArgs a = sa_base(prm + n->oQ1, C, 1, 0, (int)Hd, (int)C);
     a.B = sv(Hbuf(n, n->L, train), Bp, Bp, C * Bp);
@@ -812,8 +843,8 @@ int forward(spectral_fno_s *n, const T *f, int B, int Bp, bool train, cudaStream
     a.c2 = prm + n->oc2;
     a.y = n->y;
     a.bil = n->kind;
-    set_ext(a, E.prm - n->oQ1, E.act, train ? E.proj : 0);
-    FNO_LAUNCH((launch_sa<128, 64, 4, 2, false, false, kEpiProj>(a, st)));
+    set_ext(a, ext.prm - n->oQ1, ext.act, train ? ext.proj : 0);
+    FNO_LAUNCH((launch_sa<E, 128, 64, 4, 2, false, false, kEpiProj>(a, st)));
     return kOk;
 }
 
@@ -823,22 +854,24 @@ namespace {
 
 // Gradients of the mean relative squared error of the last training
 // forward pass into n->grads (zeroed here); the loss into n->d_loss.
+template <typename E>
 int backward(spectral_fno_s *n, int B, int Bp, cudaStream_t st)
 {
     const long long P = n->P, C = n->C, Hd = n->Hd, Km = n->Km, CB = C * Bp;
     const float *prm = n->params;
     float *gr = n->grads;
-    const Ext E(n, Bp);
+    const Ext ext(n, Bp);
     FNO_LAUNCH(cudaMemsetAsync(gr, 0, sizeof(float) * n->nparams, st));
     FNO_LAUNCH(cudaMemsetAsync(n->d_loss, 0, sizeof(double), st));
-    loss_kernel<<<ew_grid(P * Bp / 8), kEw, 0, st>>>(n->y, n->t, n->den, n->dy, n->d_loss,
-                                                      gr + n->oc2, P * Bp, B, Bp);
+    loss_kernel<<<ew_grid(P * Bp / 8), kEw, 0, st>>>(n->y, n->t, n->den, n->gs, n->dy,
+                                                      n->d_loss, gr + n->oc2, P * Bp, B, Bp);
+    E *dU = reinterpret_cast<E *>(n->dU);
     if (n->kind == 1)
-        proj_bwd_bil_kernel<<<ew_grid(P * Hd * Bp / 8), kEw, 0, st>>>(
-            n->Up, n->dy, prm + n->oq2, n->dU, gr + n->oq2, gr + n->oc1, P, (int)Hd, Bp);
+        proj_bwd_bil_kernel<E><<<ew_grid(P * Hd * Bp / 8), kEw, 0, st>>>(
+            n->Up, n->dy, prm + n->oq2, dU, gr + n->oq2, gr + n->oc1, P, (int)Hd, Bp);
     else
-        proj_bwd_kernel<<<ew_grid(P * Hd * Bp / 8), kEw, 0, st>>>(
-            n->Up, n->dy, prm + n->oq2, n->dU, gr + n->oq2, gr + n->oc1, P, (int)Hd, Bp);
+        proj_bwd_kernel<E><<<ew_grid(P * Hd * Bp / 8), kEw, 0, st>>>(
+            n->Up, n->dy, prm + n->oq2, dU, gr + n->oq2, gr + n->oc1, P, (int)Hd, Bp);
     add_launches(2);
     FNO_LAUNCH(cudaGetLastError());
     const long long KC = 16384;
@@ -848,21 +881,21 @@ int backward(spectral_fno_s *n, int B, int Bp, cudaStream_t st)
         a.B = n->H[n->L]; a.b_n = Bp; a.b_w = Bp; a.b_blk = CB;
         a.C = gr + n->oQ1; a.c_m = C;
         a.M = (int)Hd; a.N = (int)C; a.K = P * Bp; a.KC = KC; a.nz = 1; a.nz2 = 1; a.alpha = 1.f;
-        a.extA = E.proj; a.extB = E.act;
-        FNO_LAUNCH((launch_nt<128, 64, 4, 2>(a, st)));
+        a.extA = ext.proj; a.extB = ext.act;
+        FNO_LAUNCH((launch_nt<E, 128, 64, 4, 2>(a, st)));
     }
     {  // dH = Q1^T dU
         SaArgs a = sa_base(prm + n->oQ1, 1, C, 0, (int)C, (int)Hd);
         a.B = sv(n->dU, Bp, Bp, Hd * Bp);
         a.C = sv(n->dH, Bp, Bp, CB);
         a.Nn = P * Bp;
-        set_ext(a, E.prm - n->oQ1, E.proj, E.act);
-        FNO_LAUNCH((launch_sa<64, 128, 2, 2, false, false, kEpiF32>(a, st)));
+        set_ext(a, ext.prm - n->oQ1, ext.proj, ext.act);
+        FNO_LAUNCH((launch_sa<E, 64, 64, 2, 2, false, false, kEpiF32>(a, st)));
     }
     for (int l = n->L - 1; l >= 0; l--) {
-        gelu_bwd_kernel<<<ew_grid(P * CB / 8), kEw, 0, st>>>(
-            n->dH, (n->kind == 0 && l < n->L - 1) ? n->Z[l] : nullptr, n->dZ, gr + n->ob[l], P,
-            (int)C, Bp);
+        gelu_bwd_kernel<E><<<ew_grid(P * CB / 8), kEw, 0, st>>>(
+            n->dH, (n->kind == 0 && l < n->L - 1) ? n->Z[l] : nullptr,
+            reinterpret_cast<E *>(n->dZ), gr + n->ob[l], P, (int)C, Bp);
         add_launches(1);
         FNO_LAUNCH(cudaGetLastError());
         {  // dW_l += dZ h_l^T
@@ -871,19 +904,19 @@ int backward(spectral_fno_s *n, int B, int Bp, cudaStream_t st)
             a.B = n->H[l]; a.b_n = Bp; a.b_w = Bp; a.b_blk = CB;
             a.C = gr + n->oW[l]; a.c_m = C;
             a.M = (int)C; a.N = (int)C; a.K = P * Bp; a.KC = KC; a.nz = 1; a.nz2 = 1; a.alpha = 1.f;
-            a.extA = E.act; a.extB = E.act;
-            FNO_LAUNCH((launch_nt<64, 64, 2, 2>(a, st)));
+            a.extA = ext.act; a.extB = ext.act;
+            FNO_LAUNCH((launch_nt<E, 64, 64, 2, 2>(a, st)));
         }
         {  // dH = W_l^T dZ
             SaArgs a = sa_base(prm + n->oW[l], 1, C, 0, (int)C, (int)C);
             a.B = sv(n->dZ, Bp, Bp, CB);
             a.C = sv(n->dH, Bp, Bp, CB);
             a.Nn = P * Bp;
-            set_ext(a, E.prm - n->oW[l], E.act, E.act);
-            FNO_LAUNCH((launch_sa<64, 128, 2, 2, false, false, kEpiF32>(a, st)));
+            set_ext(a, ext.prm - n->oW[l], ext.act, ext.act);
+            FNO_LAUNCH((launch_sa<E, 64, 64, 2, 2, false, false, kEpiF32>(a, st)));
         }
         // spectral path: GY = F dZ; dR += GY X^T per mode class; dH += Re G (R^T GY)
-        FNO_TRY(spectral_fwd(n, n->dZ, n->GY, Bp, st));
+        FNO_TRY(spectral_fwd<E>(n, n->dZ, n->GY, true, Bp, st));
         {
             NtArgs a{};
             const long long w = Km * Km * CB;
@@ -891,14 +924,17 @@ int backward(spectral_fno_s *n, int B, int Bp, cudaStream_t st)
             a.B = n->X[l]; a.b_n = Bp; a.b_w = Bp; a.b_blk = 0; a.b_z1 = w; a.b_z2 = CB;
             a.C = gr + n->oR[l]; a.c_m = C; a.c_tab = n->cls; a.c_tabs = C * C;
             a.M = (int)C; a.N = (int)C; a.K = Bp; a.KC = (Bp + 31) / 32 * 32;
-            // GY = F3 dZ carries the transform's 1/N^3, so dL/dR = N^3 sum Re(GY conj X)
+            // GY = N^2 F3 dZ (the transform keeps one 1/N of F3's N^-3), and
+            // dL/dR = N^3 sum Re((F3 dZ) conj X) = N sum Re(GY conj X)
             a.nz = (int)(2 * Km * Km * Km); a.nz2 = (int)(Km * Km);
-            a.alpha = (float)(n->P);
-            a.extA = E.xm; a.extB = E.xm;
-            FNO_LAUNCH((launch_nt<64, 64, 2, 2>(a, st)));
+            a.alpha = (float)n->N;
+            a.extA = ext.xm; a.extB = ext.xm;
+            FNO_LAUNCH((launch_nt<E, 64, 64, 2, 2>(a, st)));
         }
-        FNO_TRY(mode_mix(n, prm + n->oR[l], true, n->GY, n->GX, Bp, st));
-        FNO_TRY(spectral_inv(n, n->GX, n->dH, true, Bp, st));
+        FNO_TRY(mode_mix<E>(n, prm + n->oR[l], true, n->GY, n->GX, Bp, st));
+        // GX = N^2 R^T F3 dZ, so dH += Re(G3 GX) / N^2
+        FNO_TRY(spectral_inv<E>(n, n->GX, nullptr, n->dH,
+                                1.f / (float)((long long)n->N * n->N), Bp, st));
     }
     lift_bwd_kernel<<<ew_grid(P * CB / 8), kEw, 0, st>>>(n->dH, n->x, gr + n->oP, gr + n->obP,
                                                          P, (int)C, Bp);
@@ -907,24 +943,28 @@ int backward(spectral_fno_s *n, int B, int Bp, cudaStream_t st)
     return kOk;
 }
 
-template <typename T>
+template <typename E, typename T>
 int loss_and_grad(spectral_fno_s *n, const T *f, const T *Q, int B, cudaStream_t st)
 {
     const int Bp = (B + 7) / 8 * 8;
     FNO_TRY(ensure(n, Bp, true));
-    FNO_TRY(forward<T>(n, f, B, Bp, true, st));
+    FNO_TRY((forward<E, T>(n, f, B, Bp, true, st)));
     const long long P = n->P;
     to_pb_kernel<T><<<dim3((unsigned)((P + 31) / 32), (unsigned)((Bp + 31) / 32)), dim3(32, 8),
                       0, st>>>(Q, n->s, 2, 1.f / n->sigma, B, Bp, P, n->t);
     FNO_LAUNCH(cudaMemsetAsync(n->den, 0, sizeof(float) * Bp, st));
     den_kernel<<<152, 256, 0, st>>>(n->t, n->den, P, Bp);
-    add_launches(2);
-    if (n->floor_eps > 0.f) {
-        den_floor_kernel<<<1, 256, 0, st>>>(n->den, B, n->floor_eps);
-        add_launches(1);
-    }
+    den_finish_kernel<<<1, 256, 0, st>>>(n->den, B, n->floor_eps, n->gs);
+    add_launches(3);
     FNO_LAUNCH(cudaGetLastError());
-    return backward(n, B, Bp, st);
+    return backward<E>(n, B, Bp, st);
+}
+
+int train_pass(spectral_fno_s *n, const float *f, const float *Q, int B, cudaStream_t st)
+{
+    if (cudaSetDevice(n->device) != cudaSuccess) return kErrCuda;
+    if (n->prec == 1) return loss_and_grad<f16, float>(n, f, Q, B, st);
+    return loss_and_grad<bf16, float>(n, f, Q, B, st);
 }
 
 unsigned long long splitmix(unsigned long long &s)
@@ -945,7 +985,10 @@ int fno_predict(spectral_fno_s *n, const double *f, double *Q, int B, cudaStream
     if (cudaSetDevice(n->device) != cudaSuccess) return kErrCuda;
     const int Bp = (B + 7) / 8 * 8;
     FNO_TRY(ensure(n, Bp, n->cap_train));
-    FNO_TRY(forward<double>(n, f, B, Bp, n->cap_train, st));
+    if (n->prec == 1)
+        FNO_TRY((forward<f16, double>(n, f, B, Bp, n->cap_train, st)));
+    else
+        FNO_TRY((forward<bf16, double>(n, f, B, Bp, n->cap_train, st)));
     const long long P = n->P;
     from_pb_kernel<<<dim3((unsigned)((P + 31) / 32), (unsigned)((Bp + 31) / 32)), dim3(32, 8), 0,
                      st>>>(n->y, n->s, n->sigma, B, Bp, P, Q);
@@ -955,6 +998,12 @@ int fno_predict(spectral_fno_s *n, const double *f, double *Q, int B, cudaStream
 }
 
 int fno_grid_n(const spectral_fno_s *n) { return n->N; }
+
+int fno_reserve(spectral_fno_s *n, int B)
+{
+    if (cudaSetDevice(n->device) != cudaSuccess) return kErrCuda;
+    return ensure(n, (B + 7) / 8 * 8, n->cap_train);
+}
 
 int rel_l2_device(const double *A, const double *R, long long n3, double *out, cudaStream_t st)
 {
@@ -970,7 +1019,7 @@ int rel_l2_device(const double *A, const double *R, long long n3, double *out, c
 extern "C" {
 
 int spectral_fno_create(spectral_fno **out, int N, int width, int modes, int layers, int hidden,
-                        int kind, unsigned long long seed)
+                        int kind, int precision, unsigned long long seed)
 {
     if (!out) {
         set_error(kErrArg, "spectral_fno_create: null handle pointer");
@@ -979,12 +1028,13 @@ int spectral_fno_create(spectral_fno **out, int N, int width, int modes, int lay
     *out = nullptr;
     if (N < 4 || N > 32 || width < 8 || width > 64 || width % 8 || modes < 2 || modes > 16 ||
         modes % 2 || modes > N || layers < 1 || layers > 8 || hidden < 16 || hidden > 128 ||
-        hidden % 16 || kind < 0 || kind > 1) {
+        hidden % 16 || kind < 0 || kind > 1 || precision < 0 || precision > 1) {
         set_error(kErrArg,
                   "spectral_fno_create: unsupported shape N=%d width=%d modes=%d layers=%d "
-                  "hidden=%d kind=%d (N 4..32, width 8..64 step 8, even modes <= min(16, N), "
-                  "layers 1..8, hidden 16..128 step 16, kind 0 or 1)",
-                  N, width, modes, layers, hidden, kind);
+                  "hidden=%d kind=%d precision=%d (N 4..32, width 8..64 step 8, even modes <= "
+                  "min(16, N), layers 1..8, hidden 16..128 step 16, kind 0 or 1, precision "
+                  "0 (BF16) or 1 (FP16))",
+                  N, width, modes, layers, hidden, kind, precision);
         return kErrArg;
     }
     int ndev = 0;
@@ -995,6 +1045,7 @@ int spectral_fno_create(spectral_fno **out, int N, int width, int modes, int lay
     auto *n = new spectral_fno_s;
     cudaGetDevice(&n->device);
     n->N = N; n->C = width; n->Km = modes; n->L = layers; n->Hd = hidden; n->kind = kind;
+    n->prec = precision;
     n->P = (long long)N * N * N;
     // mode classes by |m|^2
     const int Km = modes;
@@ -1045,7 +1096,7 @@ int spectral_fno_create(spectral_fno **out, int N, int width, int modes, int lay
     for (long long i = 0; i < hidden * C; i++) h[n->oQ1 + i] = uni(1.0 / std::sqrt((double)C));
     for (long long i = 0; i < nq2; i++) h[n->oq2 + i] = uni(1.0 / std::sqrt((double)nq2));
     // DFT axis matrices: F[m][n] = e^{-2 pi i m n / N} / N, G[n][m] = e^{+2 pi i m n / N}
-    std::vector<float> Fh(2 * Km * N), Gh(2 * N * Km);
+    std::vector<float> Fh(2 * Km * N), Gh(2 * N * Km), Fuh(2 * Km * N);
     for (int m = 0; m < Km; m++)
         for (int x = 0; x < N; x++) {
             const int mm = m - Km / 2;
@@ -1053,6 +1104,8 @@ int spectral_fno_create(spectral_fno **out, int N, int width, int modes, int lay
             const double th = 2.0 * M_PI * r / N;
             Fh[m * N + x] = (float)(std::cos(th) / N);
             Fh[Km * N + m * N + x] = (float)(-std::sin(th) / N);
+            Fuh[m * N + x] = (float)std::cos(th);
+            Fuh[Km * N + m * N + x] = (float)(-std::sin(th));
             Gh[x * Km + m] = (float)std::cos(th);
             Gh[N * Km + x * Km + m] = (float)std::sin(th);
         }
@@ -1083,6 +1136,11 @@ int spectral_fno_create(spectral_fno **out, int N, int width, int modes, int lay
     if ((rc = up(&n->av, nullptr, o)) != kOk) return fail(rc);
     if ((rc = up(&n->F, Fh.data(), (long long)Fh.size())) != kOk) return fail(rc);
     if ((rc = up(&n->G, Gh.data(), (long long)Gh.size())) != kOk) return fail(rc);
+    if ((rc = up(&n->Fu, Fuh.data(), (long long)Fuh.size())) != kOk) return fail(rc);
+    {
+        const float one = 1.f;
+        if ((rc = up(&n->gs, &one, 1)) != kOk) return fail(rc);
+    }
     if (cudaMalloc((void **)&n->cls, sizeof(int) * tab.size()) != cudaSuccess ||
         cudaMemcpy(n->cls, tab.data(), sizeof(int) * tab.size(), cudaMemcpyHostToDevice) !=
             cudaSuccess) {
@@ -1102,6 +1160,8 @@ int spectral_fno_destroy(spectral_fno *n)
 long long spectral_fno_num_params(spectral_fno *n) { return n ? n->nparams : 0; }
 
 int spectral_fno_num_classes(spectral_fno *n) { return n ? n->ncls : 0; }
+
+int spectral_fno_precision(spectral_fno *n) { return n ? n->prec : -1; }
 
 int spectral_fno_get_params(spectral_fno *n, float *host)
 {
@@ -1164,12 +1224,16 @@ int spectral_fno_loss_grad(spectral_fno *n, const float *f_dev, const float *Q_d
         set_error(kErrArg, "spectral_fno_loss_grad: bad argument");
         return kErrArg;
     }
-    FNO_TRY(loss_and_grad<float>(n, f_dev, Q_dev, B, 0));
+    FNO_TRY(train_pass(n, f_dev, Q_dev, B, 0));
     SBTE_CUDA(cudaDeviceSynchronize());
     if (loss_out) SBTE_CUDA(cudaMemcpy(loss_out, n->d_loss, sizeof(double), cudaMemcpyDeviceToHost));
-    if (grad_host)
+    if (grad_host) {
+        float gs = 1.f;
+        SBTE_CUDA(cudaMemcpy(&gs, n->gs, sizeof(float), cudaMemcpyDeviceToHost));
         SBTE_CUDA(cudaMemcpy(grad_host, n->grads, sizeof(float) * n->nparams,
                              cudaMemcpyDeviceToHost));
+        for (long long i = 0; i < n->nparams; i++) grad_host[i] /= gs;
+    }
     return kOk;
 }
 
@@ -1181,12 +1245,13 @@ int spectral_fno_train_step(spectral_fno *n, const float *f_dev, const float *Q_
         return kErrArg;
     }
     cudaStream_t st = (cudaStream_t)stream;
-    FNO_TRY(loss_and_grad<float>(n, f_dev, Q_dev, B, st));
+    FNO_TRY(train_pass(n, f_dev, Q_dev, B, st));
     n->adam_t++;
     const float b1 = 0.9f, b2 = 0.999f;
     const float c1 = 1.f - std::pow(b1, (float)n->adam_t), c2 = 1.f - std::pow(b2, (float)n->adam_t);
-    adam_kernel<<<ew_grid(n->nparams / 8 + 1), kEw, 0, st>>>(n->params, n->grads, n->am, n->av,
-                                                             n->nparams, lr, b1, b2, 1e-8f, c1, c2);
+    adam_kernel<<<ew_grid(n->nparams / 8 + 1), kEw, 0, st>>>(n->params, n->grads, n->gs, n->am,
+                                                             n->av, n->nparams, lr, b1, b2, 1e-8f,
+                                                             c1, c2);
     add_launches(1);
     FNO_LAUNCH(cudaGetLastError());
     if (loss_out) {

@@ -22,13 +22,32 @@
 #pragma once
 
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <type_traits>
 
 namespace sbte {
 namespace fno {
 
 using bf16 = __nv_bfloat16;
+using f16 = __half;
+
+// The 16-bit element type of a network: BF16 or FP16 (same tensor-core rate;
+// FP16 keeps 3 more mantissa bits, BF16 the FP32 exponent range).
+template <typename E> struct Elem;
+template <> struct Elem<bf16> {
+    using T2 = __nv_bfloat162;
+    static __device__ __forceinline__ bf16 cvt(float x) { return __float2bfloat16_rn(x); }
+    static __device__ __forceinline__ T2 cvt2(float a, float b) { return __floats2bfloat162_rn(a, b); }
+    static __device__ __forceinline__ float2 f2(T2 v) { return __bfloat1622float2(v); }
+};
+template <> struct Elem<f16> {
+    using T2 = __half2;
+    static __device__ __forceinline__ f16 cvt(float x) { return __float2half_rn(x); }
+    static __device__ __forceinline__ T2 cvt2(float a, float b) { return __floats2half2_rn(a, b); }
+    static __device__ __forceinline__ float2 f2(T2 v) { return __half22float2(v); }
+};
 
 struct StreamView {
     const void *p;
@@ -58,9 +77,10 @@ struct SaArgs {
     int nz, nz2;
     // epilogue operands
     const float *bias;     // kEpiLayer
-    const float *addend;   // kEpiLayer: FP32, same view as C
+    const void *addend;    // kEpiLayer: 16-bit elements, same view as C
     float *zst;            // kEpiLayer / kEpiProj: optional FP32 store, same view as C
-    bf16 *hout;            // kEpiLayer: BF16 store, same view as C
+    void *hout;            // kEpiLayer: 16-bit store, same view as C
+    float alpha;           // kEpiAccF32: C += alpha * result
     int act;               // kEpiLayer: 1 = GELU
     const float *c1, *q2;  // kEpiProj
     const float *c2;       // kEpiProj: one value on the device
@@ -74,9 +94,9 @@ struct SaArgs {
 
 struct NtArgs {
     // A(m, k) = A[zA + m * a_m + (k / a_w) * a_blk + k % a_w]; same for B(n, k)
-    const bf16 *A;
+    const void *A;
     long long a_m, a_blk, a_w, a_z1, a_z2;
-    const bf16 *B;
+    const void *B;
     long long b_n, b_blk, b_w, b_z1, b_z2;
     float *C;              // C[c_tab ? c_tab[z] * c_tabs : 0 + m * c_m + n]
     long long c_m;
@@ -113,26 +133,34 @@ template <int N> __device__ __forceinline__ void cp_async_wait()
 {
     asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
 }
-__device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const bf16 *p)
+__device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const void *p)
 {
     asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
                  : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
                  : "r"(smem_addr(p)));
 }
-__device__ __forceinline__ void ldsm_x4_t(uint32_t (&r)[4], const bf16 *p)
+__device__ __forceinline__ void ldsm_x4_t(uint32_t (&r)[4], const void *p)
 {
     asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
                  : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
                  : "r"(smem_addr(p)));
 }
+template <typename E>
 __device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0,
                                          uint32_t b1)
 {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, "
-        "{%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
-        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+    if constexpr (std::is_same<E, f16>::value)
+        asm volatile(
+            "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, "
+            "{%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+            : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+            : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+    else
+        asm volatile(
+            "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, "
+            "{%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+            : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+            : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
 __device__ __forceinline__ long long view_off(const StreamView &v, long long r, long long n)
@@ -145,12 +173,34 @@ __device__ __forceinline__ long long zoff(long long z, int nz2, long long s1, lo
 }
 
 // ------------------------------------------------------------ gemm_sa ---
-// MT x BN output tile per work item; WM x WN warps; AC / BC: A / B complex.
+// MT x BN output tile per work item; WM x WN warps; AC / BC: A / B complex;
+// an ST-stage cp.async ring over the work items (ST - 1 tiles in flight).
 // Complex output (kEpiCplxBF16) holds re and im accumulators; a complex x
-// complex product with a real epilogue keeps only the real part.
-template <int MT, int BN, int WM, int WN, bool AC, bool BC, int EPI>
+// complex product with a real epilogue keeps only the real part.  16-bit
+// outputs go through a shared-memory tile and leave as 16-byte vectors; the
+// layer epilogue's addend streams in with the B tile, and its tile slot then
+// stages the layer output.
+template <int MT, int BN, int WM, bool AC, bool BC, int EPI, int ST> struct SaLayout {
+    static constexpr int kParts = BC ? 2 : 1;
+    static constexpr bool kAdd = EPI == kEpiLayer;
+    static constexpr bool kOwnStage = EPI == kEpiBF16 || EPI == kEpiCplxBF16;
+    static constexpr int kBP = BN + 8;
+    static constexpr int kStageRows = kOwnStage ? (EPI == kEpiCplxBF16 ? 2 : 1) * MT : 0;
+    // elements of one ring stage for K rounded to KP
+    static __host__ __device__ int stage_elems(int KP) { return kParts * KP * kBP + (kAdd ? MT * kBP : 0); }
+    static __host__ __device__ size_t bytes(int KP)
+    {
+        return 2 * ((size_t)(AC ? 3 : 1) * MT * (KP + 8) + (size_t)ST * stage_elems(KP) +
+                    (size_t)kStageRows * kBP) +
+               (EPI == kEpiProj ? (size_t)WM * BN * 4 : 0);
+    }
+};
+
+template <typename E, int MT, int BN, int WM, int WN, bool AC, bool BC, int EPI, int ST>
 __global__ void __launch_bounds__(WM *WN * 32) gemm_sa_kernel(const SaArgs a)
 {
+    using T2 = typename Elem<E>::T2;
+    using L = SaLayout<MT, BN, WM, AC, BC, EPI, ST>;
     constexpr int NTH = WM * WN * 32;
     constexpr int WR = MT / WM, WC = BN / WN;
     constexpr int FM = WR / 16, FN = WC / 8;
@@ -158,52 +208,70 @@ __global__ void __launch_bounds__(WM *WN * 32) gemm_sa_kernel(const SaArgs a)
     constexpr bool CO = (EPI == kEpiCplxBF16);
     constexpr bool IM = CO || (AC && !BC);  // imaginary accumulator needed
     static_assert(!(AC && !BC) || CO, "complex A x real B gives a complex result");
+    constexpr int PARTS = L::kParts, BP = L::kBP, CH = BN / 8;
+    constexpr bool STG = L::kOwnStage || L::kAdd;
 
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int KP = a.KP, ap = KP + 8, bp = BN + 8;
-    bf16 *sAr = reinterpret_cast<bf16 *>(smem_raw);
-    bf16 *sAi = sAr + MT * ap;
-    bf16 *sAn = sAi + MT * ap;
-    bf16 *sB = sAr + (AC ? 3 : 1) * MT * ap;
-    const int tileB = KP * bp;                 // one part of one stage
-    constexpr int PARTS = BC ? 2 : 1;
-    float *red = reinterpret_cast<float *>(sB + 2 * PARTS * tileB);  // kEpiProj: [WM][BN]
+    const int KP = a.KP, ap = KP + 8;
+    E *sAr = reinterpret_cast<E *>(smem_raw);
+    E *sAi = sAr + MT * ap;
+    E *sAn = sAi + MT * ap;
+    E *ring = sAr + (AC ? 3 : 1) * MT * ap;
+    const int tileB = KP * BP;
+    const int stageE = L::stage_elems(KP);
+    E *own = ring + ST * stageE;  // output staging tile (kOwnStage)
+    float *red = reinterpret_cast<float *>(own + L::kStageRows * BP);  // kEpiProj: [WM][BN]
 
     const long long ntiles = (a.Nn + BN - 1) / BN;
     const long long total = ntiles * a.nz;
     long long item = blockIdx.x;
     if (item >= total) return;
 
-    const bf16 *Bb = static_cast<const bf16 *>(a.B.p);
+    const E *Bb = static_cast<const E *>(a.B.p);
     auto issue = [&](long long it, int stage) {
         const long long z = it / ntiles;
         const long long n0 = (it % ntiles) * BN;
         const long long zb = zoff(z, a.nz2, a.B.s_z1, a.B.s_z2);
-        constexpr int CH = BN / 8;
+        E *base = ring + stage * stageE;
         for (int c = threadIdx.x; c < KP * CH; c += NTH) {
             const int r = c / CH, cn = c % CH;
             const long long n = n0 + cn * 8;
             const bool ok = (r < a.K) && (n < a.Nn);
             const long long off = ok ? zb + view_off(a.B, r, n) : 0;
 #pragma unroll
-            for (int part = 0; part < PARTS; part++) {
-                bf16 *dst = sB + (stage * PARTS + part) * tileB + r * bp + cn * 8;
-                cp_async16(dst, Bb + off + (part ? a.B.im : 0), ok);
+            for (int part = 0; part < PARTS; part++)
+                cp_async16(base + part * tileB + r * BP + cn * 8, Bb + off + (part ? a.B.im : 0),
+                           ok);
+        }
+        if constexpr (L::kAdd) {
+            const long long zc = zoff(z, a.nz2, a.C.s_z1, a.C.s_z2);
+            const E *ad = static_cast<const E *>(a.addend);
+            E *sa = base + PARTS * tileB;
+            for (int c = threadIdx.x; c < MT * CH; c += NTH) {
+                const int r = c / CH, cn = c % CH;
+                const long long n = n0 + cn * 8;
+                const bool ok = (r < a.M) && (n < a.Nn);
+                const long long off = ok ? zc + view_off(a.C, r, n) : 0;
+                cp_async16(sa + r * BP + cn * 8, ad + off, ok);
             }
         }
     };
 
-    issue(item, 0);
-    cp_async_commit();
+#pragma unroll
+    for (int s = 0; s < ST - 1; s++) {
+        const long long it = item + (long long)s * gridDim.x;
+        if (it < total) issue(it, s);
+        cp_async_commit();
+    }
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int wm = warp / WN, wn = warp % WN;
     const int g = lane >> 2, t = lane & 3;
     long long cur_z = -1;
     int stage = 0;
-    for (; item < total; item += gridDim.x, stage ^= 1) {
-        const long long nxt = item + gridDim.x;
-        if (nxt < total) issue(nxt, stage ^ 1);
+    for (; item < total; item += gridDim.x) {
+        const long long pre = item + (long long)(ST - 1) * gridDim.x;
+        if (pre < total) issue(pre, (stage + ST - 1) % ST);
         cp_async_commit();
         const long long z = item / ntiles;
         const long long n0 = (item % ntiles) * BN;
@@ -218,15 +286,15 @@ __global__ void __launch_bounds__(WM *WN * 32) gemm_sa_kernel(const SaArgs a)
                     re = src[0];
                     if (AC) im = a.a_im_sign * src[a.imA];
                 }
-                sAr[m * ap + k] = __float2bfloat16_rn(re);
+                sAr[m * ap + k] = Elem<E>::cvt(re);
                 if (AC) {
-                    sAi[m * ap + k] = __float2bfloat16_rn(im);
-                    sAn[m * ap + k] = __float2bfloat16_rn(-im);
+                    sAi[m * ap + k] = Elem<E>::cvt(im);
+                    sAn[m * ap + k] = Elem<E>::cvt(-im);
                 }
             }
             cur_z = z;
         }
-        cp_async_wait<1>();
+        cp_async_wait<ST - 1>();
         __syncthreads();
 
         float accR[FM][FN][4], accI[IM ? FM : 1][IM ? FN : 1][4];
@@ -239,8 +307,9 @@ __global__ void __launch_bounds__(WM *WN * 32) gemm_sa_kernel(const SaArgs a)
                     accR[i][j][r] = 0.f;
                     if (IM) accI[IM ? i : 0][IM ? j : 0][r] = 0.f;
                 }
-        const bf16 *sBr = sB + (stage * PARTS) * tileB;
-        const bf16 *sBi = sBr + tileB;
+        E *sbase = ring + stage * stageE;
+        const E *sBr = sbase;
+        const E *sBi = sBr + tileB;
         for (int kk = 0; kk < KP; kk += 16) {
             uint32_t ar[FM][4], ai[AC ? FM : 1][4], an[AC ? FM : 1][4];
 #pragma unroll
@@ -258,27 +327,27 @@ __global__ void __launch_bounds__(WM *WN * 32) gemm_sa_kernel(const SaArgs a)
                 uint32_t br[4], bi[4];
                 const int krow = kk + (lane & 15);
                 const int ncol = wn * WC + f2 * 16 + (lane >> 4) * 8;
-                ldsm_x4_t(br, sBr + krow * bp + ncol);
-                if (BC) ldsm_x4_t(bi, sBi + krow * bp + ncol);
+                ldsm_x4_t(br, sBr + krow * BP + ncol);
+                if (BC) ldsm_x4_t(bi, sBi + krow * BP + ncol);
 #pragma unroll
                 for (int h = 0; h < 2; h++) {
                     const int fn = f2 * 2 + h;
 #pragma unroll
                     for (int fm = 0; fm < FM; fm++) {
                         if (!AC) {
-                            mma16816(accR[fm][fn], ar[fm], br[2 * h], br[2 * h + 1]);
+                            mma16816<E>(accR[fm][fn], ar[fm], br[2 * h], br[2 * h + 1]);
                         } else if (!BC) {
-                            mma16816(accR[fm][fn], ar[fm], br[2 * h], br[2 * h + 1]);
-                            mma16816(accI[IM ? fm : 0][IM ? fn : 0], ai[AC ? fm : 0], br[2 * h],
-                                     br[2 * h + 1]);
+                            mma16816<E>(accR[fm][fn], ar[fm], br[2 * h], br[2 * h + 1]);
+                            mma16816<E>(accI[IM ? fm : 0][IM ? fn : 0], ai[AC ? fm : 0],
+                                        br[2 * h], br[2 * h + 1]);
                         } else {
-                            mma16816(accR[fm][fn], ar[fm], br[2 * h], br[2 * h + 1]);
-                            mma16816(accR[fm][fn], an[AC ? fm : 0], bi[2 * h], bi[2 * h + 1]);
+                            mma16816<E>(accR[fm][fn], ar[fm], br[2 * h], br[2 * h + 1]);
+                            mma16816<E>(accR[fm][fn], an[AC ? fm : 0], bi[2 * h], bi[2 * h + 1]);
                             if (CO) {
-                                mma16816(accI[IM ? fm : 0][IM ? fn : 0], ar[fm], bi[2 * h],
-                                         bi[2 * h + 1]);
-                                mma16816(accI[IM ? fm : 0][IM ? fn : 0], ai[AC ? fm : 0],
-                                         br[2 * h], br[2 * h + 1]);
+                                mma16816<E>(accI[IM ? fm : 0][IM ? fn : 0], ar[fm], bi[2 * h],
+                                            bi[2 * h + 1]);
+                                mma16816<E>(accI[IM ? fm : 0][IM ? fn : 0], ai[AC ? fm : 0],
+                                            br[2 * h], br[2 * h + 1]);
                             }
                         }
                     }
@@ -288,7 +357,7 @@ __global__ void __launch_bounds__(WM *WN * 32) gemm_sa_kernel(const SaArgs a)
 
         // ---- epilogue
         const long long zc = zoff(z, a.nz2, a.C.s_z1, a.C.s_z2);
-        if (EPI == kEpiProj) {
+        if constexpr (EPI == kEpiProj) {
             float part[FN][2];
 #pragma unroll
             for (int fn = 0; fn < FN; fn++) part[fn][0] = part[fn][1] = 0.f;
@@ -362,6 +431,51 @@ __global__ void __launch_bounds__(WM *WN * 32) gemm_sa_kernel(const SaArgs a)
                     a.y[n] = s;
                 }
             }
+        } else if constexpr (STG) {
+            // values into the staging tile (rows: re then im for complex output)
+            E *tile = L::kAdd ? sbase + PARTS * tileB : own;
+#pragma unroll
+            for (int fm = 0; fm < FM; fm++)
+#pragma unroll
+                for (int hh = 0; hh < 2; hh++) {
+                    const int m = wm * WR + fm * 16 + g + hh * 8;
+#pragma unroll
+                    for (int fn = 0; fn < FN; fn++) {
+                        const int col = wn * WC + fn * 8 + 2 * t;
+                        const float v0 = accR[fm][fn][2 * hh], v1 = accR[fm][fn][2 * hh + 1];
+                        T2 *dst = reinterpret_cast<T2 *>(tile + m * BP + col);
+                        if constexpr (L::kAdd) {
+                            const long long n = n0 + col;
+                            const float bm = m < a.M ? a.bias[m] : 0.f;
+                            const float2 ad = Elem<E>::f2(*dst);
+                            const float z0 = v0 + bm + ad.x, z1 = v1 + bm + ad.y;
+                            if (a.zst && m < a.M && n < a.Nn)
+                                *reinterpret_cast<float2 *>(a.zst + zc + view_off(a.C, m, n)) =
+                                    make_float2(z0, z1);
+                            *dst = a.act ? Elem<E>::cvt2(gelu_f(z0), gelu_f(z1))
+                                         : Elem<E>::cvt2(z0, z1);
+                        } else {
+                            *dst = Elem<E>::cvt2(v0, v1);
+                            if constexpr (CO)
+                                *reinterpret_cast<T2 *>(tile + (MT + m) * BP + col) =
+                                    Elem<E>::cvt2(accI[IM ? fm : 0][IM ? fn : 0][2 * hh],
+                                                  accI[IM ? fm : 0][IM ? fn : 0][2 * hh + 1]);
+                        }
+                    }
+                }
+            __syncthreads();
+            E *Cg = static_cast<E *>(L::kAdd ? a.hout : const_cast<void *>(a.C.p));
+            constexpr int ROWS = (CO ? 2 : 1) * MT;
+            for (int c = threadIdx.x; c < ROWS * CH; c += NTH) {
+                const int r = c / CH, cn = c % CH;
+                const int m = r % MT;
+                const long long n = n0 + cn * 8;
+                if (m < a.M && n < a.Nn) {
+                    const long long off = zc + view_off(a.C, m, n) + (r >= MT ? a.C.im : 0);
+                    *reinterpret_cast<uint4 *>(Cg + off) =
+                        *reinterpret_cast<const uint4 *>(tile + r * BP + cn * 8);
+                }
+            }
         } else {
 #pragma unroll
             for (int fm = 0; fm < FM; fm++)
@@ -375,64 +489,41 @@ __global__ void __launch_bounds__(WM *WN * 32) gemm_sa_kernel(const SaArgs a)
                         if (n >= a.Nn) continue;
                         const long long off = zc + view_off(a.C, m, n);
                         const float v0 = accR[fm][fn][2 * hh], v1 = accR[fm][fn][2 * hh + 1];
-                        if (EPI == kEpiBF16) {
-                            *reinterpret_cast<__nv_bfloat162 *>(static_cast<bf16 *>(
-                                const_cast<void *>(a.C.p)) + off) = __floats2bfloat162_rn(v0, v1);
-                        } else if (EPI == kEpiCplxBF16) {
-                            bf16 *c = static_cast<bf16 *>(const_cast<void *>(a.C.p));
-                            *reinterpret_cast<__nv_bfloat162 *>(c + off) =
-                                __floats2bfloat162_rn(v0, v1);
-                            *reinterpret_cast<__nv_bfloat162 *>(c + off + a.C.im) =
-                                __floats2bfloat162_rn(accI[IM ? fm : 0][IM ? fn : 0][2 * hh],
-                                                      accI[IM ? fm : 0][IM ? fn : 0][2 * hh + 1]);
-                        } else if (EPI == kEpiF32) {
-                            *reinterpret_cast<float2 *>(static_cast<float *>(
-                                const_cast<void *>(a.C.p)) + off) = make_float2(v0, v1);
-                        } else if (EPI == kEpiAccF32) {
-                            float2 *c = reinterpret_cast<float2 *>(
-                                static_cast<float *>(const_cast<void *>(a.C.p)) + off);
+                        float2 *c = reinterpret_cast<float2 *>(
+                            static_cast<float *>(const_cast<void *>(a.C.p)) + off);
+                        if constexpr (EPI == kEpiF32) {
+                            *c = make_float2(v0, v1);
+                        } else {  // kEpiAccF32
                             float2 o = *c;
-                            o.x += v0;
-                            o.y += v1;
+                            o.x += a.alpha * v0;
+                            o.y += a.alpha * v1;
                             *c = o;
-                        } else if (EPI == kEpiLayer) {
-                            const float bm = a.bias[m];
-                            const float2 ad = *reinterpret_cast<const float2 *>(a.addend + off);
-                            const float z0 = v0 + bm + ad.x, z1 = v1 + bm + ad.y;
-                            if (a.zst)
-                                *reinterpret_cast<float2 *>(a.zst + off) = make_float2(z0, z1);
-                            const float h0 = a.act ? gelu_f(z0) : z0;
-                            const float h1 = a.act ? gelu_f(z1) : z1;
-                            *reinterpret_cast<__nv_bfloat162 *>(a.hout + off) =
-                                __floats2bfloat162_rn(h0, h1);
                         }
                     }
                 }
         }
         __syncthreads();
+        stage = (stage + 1 == ST) ? 0 : stage + 1;
     }
     cp_async_wait<0>();
 }
 
-template <int MT, int BN, int WM, int WN, bool AC, bool BC, int EPI>
+template <int MT, int BN, int WM, int WN, bool AC, bool BC, int EPI, int ST>
 inline size_t gemm_sa_smem(int KP)
 {
-    size_t a = (size_t)(AC ? 3 : 1) * MT * (KP + 8) * 2;
-    size_t b = (size_t)2 * (BC ? 2 : 1) * KP * (BN + 8) * 2;
-    size_t r = (EPI == kEpiProj) ? (size_t)WM * BN * 4 : 0;
-    return a + b + r;
+    return SaLayout<MT, BN, WM, AC, BC, EPI, ST>::bytes(KP);
 }
 
 // ------------------------------------------------------------ gemm_nt ---
-template <int MT, int NT, int WM, int WN>
+template <typename E, int MT, int NT, int WM, int WN>
 __global__ void __launch_bounds__(WM *WN * 32) gemm_nt_kernel(const NtArgs a)
 {
     constexpr int NTH = WM * WN * 32, BK = 32, P = BK + 8;
     constexpr int WR = MT / WM, WC = NT / WN;
     constexpr int FM = WR / 16, FN = WC / 8;
     static_assert(WR % 16 == 0 && WC % 16 == 0, "warp tile");
-    __shared__ __align__(16) bf16 sA[2][MT * P];
-    __shared__ __align__(16) bf16 sB[2][NT * P];
+    __shared__ __align__(16) E sA[2][MT * P];
+    __shared__ __align__(16) E sB[2][NT * P];
 
     const long long nchunks = (a.K + a.KC - 1) / a.KC;
     const long long total = nchunks * a.nz;
@@ -454,13 +545,13 @@ __global__ void __launch_bounds__(WM *WN * 32) gemm_nt_kernel(const NtArgs a)
                     const bool ok = row < a.M && k < k1;
                     const long long off =
                         ok ? zA + row * a.a_m + (k / a.a_w) * a.a_blk + (k % a.a_w) : 0;
-                    cp_async16(&sA[st][row * P + ck * 8], a.A + off, ok);
+                    cp_async16(&sA[st][row * P + ck * 8], static_cast<const E *>(a.A) + off, ok);
                 } else {
                     const int n = row - MT;
                     const bool ok = n < a.N && k < k1;
                     const long long off =
                         ok ? zB + n * a.b_n + (k / a.b_w) * a.b_blk + (k % a.b_w) : 0;
-                    cp_async16(&sB[st][n * P + ck * 8], a.B + off, ok);
+                    cp_async16(&sB[st][n * P + ck * 8], static_cast<const E *>(a.B) + off, ok);
                 }
             }
         };
@@ -493,8 +584,8 @@ __global__ void __launch_bounds__(WM *WN * 32) gemm_nt_kernel(const NtArgs a)
                     ldsm_x4(bq, &sB[st][nrow * P + kk + ((lane >> 3) & 1) * 8]);
 #pragma unroll
                     for (int fm = 0; fm < FM; fm++) {
-                        mma16816(acc[fm][2 * f2], af[fm], bq[0], bq[1]);
-                        mma16816(acc[fm][2 * f2 + 1], af[fm], bq[2], bq[3]);
+                        mma16816<E>(acc[fm][2 * f2], af[fm], bq[0], bq[1]);
+                        mma16816<E>(acc[fm][2 * f2 + 1], af[fm], bq[2], bq[3]);
                     }
                 }
             }

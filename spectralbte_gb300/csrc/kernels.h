@@ -123,6 +123,12 @@ cudaError_t maxwellian_split(const double *f, double *M, double *g,
                              const double *v, double mass, double KB,
                              double *moments_out, cudaStream_t st);
 
+// Output moments of B instances, 8 doubles each: rho, u_x, u_y, u_z, T,
+// rho T, and the positive and negative parts of getEnergy
+// (output.c:156-213, momentRoutines.c:58-190).
+cudaError_t moments_batch(const double *f, int B, int N, const double *v, double mass,
+                          double KB, double *out, cudaStream_t st);
+
 // Euler / RK2 combinations of boltz.c:206-241 on B*N^3 values.
 cudaError_t axpy_update(double *y, const double *x, const double *q,
                         double a_y, double a_x, double a_q, long long n,

@@ -226,6 +226,7 @@ def main(argv=None):
     ap.add_argument("--hidden", type=int, default=128)
     ap.add_argument("--kind", type=int, default=0, help="0: GELU network, 1: bilinear")
     ap.add_argument("--floor", type=float, default=0.1)
+    ap.add_argument("--precision", type=int, default=1, help="0: BF16, 1: FP16 elements")
     ap.add_argument("--pairs", type=int, default=200000)
     ap.add_argument("--heldout", type=int, default=512)
     ap.add_argument("--batch", type=int, default=32)
@@ -249,7 +250,7 @@ def main(argv=None):
         net = FourierOperator.load(a.init)
     else:
         net = FourierOperator(a.n, a.width, a.modes, a.layers, a.hidden, seed=a.seed,
-                              kind=a.kind)
+                              kind=a.kind, precision=a.precision)
         net.output_scale = output_scale(F, Q)
     net.set_loss_floor(a.floor)
     e0 = evaluate(net, plan, Fe, Qe)

@@ -5,6 +5,8 @@ the plan.  Index order is (i, j, k) -> k + N*(j + N*i), with i the x axis.
 """
 from __future__ import annotations
 
+import math
+
 import numpy as np
 
 
@@ -69,3 +71,62 @@ def bkw(v: np.ndarray, K: float = 0.65) -> np.ndarray:
     f = np.exp(-v2 / (2 * K)) / (2.0 * (2 * np.pi * K) ** 1.5) * ((5 * K - 3) / K +
                                                                 (1 - K) * v2 / (K * K))
     return f.reshape(-1)
+
+
+def mesh_1d(nX: int, order: int, length: float = 1.0):
+    """Cell centres x and widths dx of nX uniform cells on [0, length] plus
+    `order` ghost cells on each side (mesh_setup.c:59-160 for one zone on
+    one rank; the right ghosts extend the grid uniformly)."""
+    dx = length / nX
+    x = (np.arange(nX + 2 * order) - order + 0.5) * dx
+    return x, np.full(nX + 2 * order, dx)
+
+
+# (rho_l, ux_l, T_l, rho_r, ux_r, T_r) of the reference's initial fields
+# (initializer.c:297-351, Ma = 1 for case 0)
+_IC = {
+    0: (1.0, -math.sqrt(5.0 / 3.0), 1.0, 1.0, -math.sqrt(5.0 / 3.0), 1.0),
+    2: (1.0, -1.0, 1.0, 1.0, -1.0, 2.0),
+    3: (1.0, 0.0, 1.0, 1.0, 0.0, 1.5),
+    5: (1.0, 0.0, 1.0, 1.0, 0.0, 1.0),
+    6: (1.0, 1.2972, 1.0, 1.297, 1.0, 1.195),
+}
+
+
+def init_1d(v: np.ndarray, nX: int, order: int, ic: int, TWall: float = 1.0,
+            mass: float = 1.0, KB: float = 1.0) -> np.ndarray:
+    """Initial f[nX + 2 order][N^3] of the reference's Init_field cases
+    (initializer.c:296-424): 0 (Ma = 1 shock), 1 (sudden heating), 2, 3 (heat
+    transfer between walls), 5 (Poiseuille), 6 (the Mach-1.2 shock).  Ghost
+    cells stay zero, as in the reference."""
+    N = v.size
+    vx, vy, vz = _mesh(v)
+    out = np.zeros((nX + 2 * order, N ** 3))
+
+    def gauss(rho, ux, T):
+        return (rho * np.exp(-((vx - ux) ** 2 + vy ** 2 + vz ** 2) / T) /
+                ((T * math.pi) * math.sqrt(T * math.pi))).reshape(-1)
+
+    if ic == 1:
+        T = TWall
+        m = (1.0 / mass) * (0.5 * mass / (math.pi * KB * T)) ** 1.5 * np.exp(
+            -(0.5 * mass / (KB * T)) * (vx ** 2 + vy ** 2 + vz ** 2))
+        out[order:nX + order] = m.reshape(-1)
+        return out
+    rl, ul, tl, rr, ur, tr = _IC[ic]
+    if ic == 0:  # the reference's case 0 uses no drift in f (initializer.c:361-373)
+        ul = ur = 0.0
+        Ma = 1.0
+        rl = 4.0 * Ma * Ma / (Ma * Ma + 3.0)
+        tl = (5.0 * Ma * Ma - 1.0) * (Ma * Ma + 3.0) / (16.0 * Ma * Ma)
+    left, right = gauss(rl, ul, tl), gauss(rr, ur, tr)
+    for l in range(order, nX + order):
+        if ic in (0, 6):
+            out[l] = left if l < nX // 2 else right
+        elif ic == 2:
+            out[l] = left
+        elif ic == 3:
+            out[l] = right
+        else:
+            out[l] = left
+    return out

@@ -135,3 +135,33 @@ def test_1d_fp32_step_close_to_fp64(gpu, oracle):
     lo, hi = 2, 10
     x, y = b.cpu().numpy()[lo:hi], a.cpu().numpy()[lo:hi]
     assert rel_l2(x, y) < 1e-3
+
+
+def test_device_moments_match_oracle(gpu, oracle):
+    """spectral_moments_device on every cell of a heat-transport state equals
+    the oracle's getDensity / getBulkVelocity / getTemperature to 1e-12, and
+    getEnergy's two parts to 1e-12 (numpy)."""
+    r, plan, f0, torch = _setup(gpu, oracle, 8, 9.0, 250, 1, 3, 1e-4, 3.2, 1.0)
+    fd = torch.from_numpy(f0.copy()).cuda()
+    for _ in range(3):
+        plan.step_1d(fd, gpu.FP64)
+    out = torch.empty((250, 8), dtype=torch.float64, device="cuda")
+    plan.moments_device(fd[1:251], 250, out)
+    m = out.cpu().numpy()
+    f = fd.cpu().numpy()
+    v = r.g.v
+    wt = np.ones(8)
+    wt[0] = wt[-1] = 0.5
+    dv = v[1] - v[0]
+    w = (wt[:, None, None] * wt[None, :, None] * wt[None, None, :]).reshape(-1) * dv ** 3
+    vx, vy, vz = (a.reshape(-1) for a in np.meshgrid(v, v, v, indexing="ij"))
+    for l in range(250):
+        rho, u, T = oracle.moments(r.g, f[l + 1])
+        got = m[l]
+        assert abs(got[0] - rho) <= 1e-12 * abs(rho)
+        assert np.all(np.abs(got[1:4] - np.asarray(u)) <= 1e-12 * max(1.0, np.abs(u).max()))
+        assert abs(got[4] - T) <= 1e-12 * abs(T)
+        assert abs(got[5] - rho * T) <= 1e-12 * abs(rho * T)
+        e = w * f[l + 1] * (vx ** 2 + vy ** 2 + vz ** 2)
+        assert abs(got[6] - e[e > 0].sum()) <= 1e-12 * e[e > 0].sum()
+        assert abs(got[7] + e[e < 0].sum()) <= 1e-12 * max(1e-300, abs(e).sum())

@@ -10,8 +10,8 @@
   (the lift gradient is a sum with heavy cancellation, accumulated in FP32
   atomics on the device), and the FP64 oracle's within 5e-2; the loss within
   1e-4 relative.  An indexing or formula error shows as an O(1) difference.
-  Both network kinds (GELU, bilinear), three shapes, and batches that are
-  not a multiple of 8 (padding).
+  Both network kinds (GELU, bilinear), both element types (BF16, FP16),
+  three shapes, and batches that are not a multiple of 8 (padding).
 * Training on pairs from the plain operator lowers the held-out error of the
   network well below that of the untrained network.
 * The plan's SPECTRAL_LEARNED path: the output is the conservation
@@ -29,17 +29,19 @@ from oracle import fno_oracle as fo
 pytestmark = pytest.mark.gpu
 
 N, WIDTH, MODES, LAYERS, HIDDEN = 8, 8, 4, 2, 16
-SHAPES = {"small": (8, 8, 4, 2, 16, 0), "wide": (16, 16, 8, 3, 32, 0),
-          "odd": (12, 24, 6, 1, 48, 0), "bil": (8, 8, 4, 2, 16, 1),
-          "wide_bil": (16, 16, 8, 3, 32, 1)}
+# (N, width, modes, layers, hidden, kind, precision)
+SHAPES = {"small": (8, 8, 4, 2, 16, 0, 0), "wide": (16, 16, 8, 3, 32, 0, 0),
+          "odd": (12, 24, 6, 1, 48, 0, 0), "bil": (8, 8, 4, 2, 16, 1, 0),
+          "wide_bil": (16, 16, 8, 3, 32, 1, 0), "small16": (8, 8, 4, 2, 16, 0, 1),
+          "wide16": (16, 16, 8, 3, 32, 0, 1), "odd16": (12, 24, 6, 1, 48, 0, 1)}
 
 
 def _net(gpu, seed=7, sigma=0.5, shape="small"):
-    n, w, m, L, hd, kind = SHAPES[shape]
-    net = gpu.FourierOperator(n, w, m, L, hd, seed=seed, kind=kind)
+    n, w, m, L, hd, kind, prec = SHAPES[shape]
+    net = gpu.FourierOperator(n, w, m, L, hd, seed=seed, kind=kind, precision=prec)
     net.output_scale = sigma
     spec = fo.Spec(N=n, C=w, Km=m, L=L, Hd=hd, kind=kind)
-    return net, spec
+    return net, spec, prec
 
 
 def _data(B, seed, n=N):
@@ -50,17 +52,19 @@ def _data(B, seed, n=N):
 
 
 @pytest.mark.parametrize("B,shape", [(3, "small"), (8, "small"), (13, "small"), (5, "wide"),
-                                     (9, "odd"), (6, "bil"), (4, "wide_bil")])
+                                     (9, "odd"), (6, "bil"), (4, "wide_bil"), (5, "small16"),
+                                     (4, "wide16"), (9, "odd16")])
 def test_forward_matches_oracle(gpu, B, shape):
     import torch
-    net, spec = _net(gpu, shape=shape)
+    net, spec, prec = _net(gpu, shape=shape)
     theta = net.get_params().astype(np.float64)
     f, _ = _data(B, B, spec.N)
     fd = torch.from_numpy(f.astype(np.float64)).cuda()
     Qd = torch.zeros_like(fd)
     net.predict(fd, Qd, B)
     got = Qd.cpu().numpy()
-    want_r = fo.Net(spec, theta, sigma=0.5, rounding=True).predict(f.astype(np.float64))
+    want_r = fo.Net(spec, theta, sigma=0.5, rounding=True, precision=prec).predict(
+        f.astype(np.float64))
     want = fo.Net(spec, theta, sigma=0.5).predict(f.astype(np.float64))
     gap = rel_l2(want_r, want)
     assert rel_l2(got, want_r.reshape(B, -1)) < max(1e-3, gap), gap
@@ -69,15 +73,17 @@ def test_forward_matches_oracle(gpu, B, shape):
 
 @pytest.mark.parametrize("B,shape,floor", [(5, "small", 0.0), (16, "small", 0.3),
                                            (6, "wide", 0.0), (3, "odd", 0.1),
-                                           (7, "bil", 0.1), (4, "wide_bil", 0.0)])
+                                           (7, "bil", 0.1), (4, "wide_bil", 0.0),
+                                           (5, "small16", 0.1), (6, "wide16", 0.1),
+                                           (3, "odd16", 0.1)])
 def test_gradients_match_oracle(gpu, B, shape, floor):
     import torch
-    net, spec = _net(gpu, seed=11, shape=shape)
+    net, spec, prec = _net(gpu, seed=11, shape=shape)
     net.set_loss_floor(floor)
     theta = net.get_params().astype(np.float64)
     f, Q = _data(B, 100 + B, spec.N)
     loss, g = net.loss_grad(torch.from_numpy(f).cuda(), torch.from_numpy(Q).cuda(), B)
-    lr_, gr = fo.Net(spec, theta, sigma=0.5, rounding=True).loss_grad(
+    lr_, gr = fo.Net(spec, theta, sigma=0.5, rounding=True, precision=prec).loss_grad(
         f.astype(np.float64), Q.astype(np.float64), floor)
     l64, g64 = fo.Net(spec, theta, sigma=0.5).loss_grad(f.astype(np.float64),
                                                         Q.astype(np.float64), floor)
@@ -103,7 +109,7 @@ def test_training_lowers_heldout_error(gpu, shape="small"):
     plan = _plan(gpu)
     F, Q, _ = lrn.make_dataset(plan, 768, seed=1, chunk=128)
     Fe, Qe, fam = lrn.make_dataset(plan, 96, seed=999, chunk=96, out_dtype=torch.float64)
-    net, _ = _net(gpu, seed=3, sigma=lrn.output_scale(F, Q), shape=shape)
+    net, _, _ = _net(gpu, seed=3, sigma=lrn.output_scale(F, Q), shape=shape)
     net.set_loss_floor(0.1)
     e0 = lrn.evaluate(net, plan, Fe, Qe)
     log = lrn.train(net, F, Q, steps=1500, batch=16, lr=1e-2, lr_final=3e-4)
@@ -128,7 +134,7 @@ def test_plan_learned_path_and_fallback(gpu):
     import torch
     from spectralbte_gb300 import learned as lrn
     plan = _plan(gpu)
-    net, _ = _net(gpu, seed=5)
+    net, _, _ = _net(gpu, seed=5)
     B = 12
     f = lrn.sample_f(plan.v, "mixture", B, seed=4)
     scale = float(torch.linalg.vector_norm(f, dim=1).mean())
@@ -162,3 +168,41 @@ def test_plan_learned_path_and_fallback(gpu):
     plan.set_learned(None)
     with pytest.raises(gpu.SpectralError):
         plan.computeQ_device(f, Q, B, gpu.FP32 | gpu.LEARNED)
+
+
+def test_1d_steps_with_learned_operator(gpu, oracle):
+    """The 1D-3V step with SPECTRAL_LEARNED: with every check failing it is
+    the plain FP32 step bit for bit; a graph-captured step (no checks)
+    replays the uncaptured one; capture with checks is refused."""
+    import torch
+    nX = 16
+    r = oracle.Run1D(N, 6.0, nX, 2, 3, 2e-3, 0.5)
+    plan = gpu.Plan(N, 6.0, r.g.v, r.g.zeta, nX)
+    plan.generate_weights_iso(1.0)
+    plan.setup_1d(nX, 2, 3, 2e-3, 0.5, r.x, r.dx)
+    f0 = r.init()
+    net, _, _ = _net(gpu, seed=5)
+    a = torch.from_numpy(f0.copy()).cuda()
+    b = torch.from_numpy(f0.copy()).cuda()
+    plan.set_learned(net, tol=1e-12, check_every=1)
+    for _ in range(3):
+        plan.step_1d(a, gpu.FP32)
+        plan.step_1d(b, gpu.FP32 | gpu.LEARNED)
+    torch.cuda.synchronize()
+    assert torch.equal(a, b)
+    st = plan.learned_stats()
+    assert st["calls"] == 6 and st["fallbacks"] == 6
+    plan.set_learned(net, tol=1.0, check_every=0)
+    c = torch.from_numpy(f0.copy()).cuda()
+    d = torch.from_numpy(f0.copy()).cuda()
+    for _ in range(3):
+        plan.step_1d(c, gpu.FP32 | gpu.LEARNED)
+    plan.capture(1, d, flags=gpu.FP32 | gpu.LEARNED)
+    for _ in range(3):
+        plan.launch()
+    torch.cuda.synchronize()
+    assert torch.equal(c, d)
+    assert not torch.equal(c, a)  # the network, not the plain operator, ran
+    plan.set_learned(net, tol=1.0, check_every=1)
+    with pytest.raises(gpu.SpectralError):
+        plan.capture(1, d, flags=gpu.FP32 | gpu.LEARNED)
