@@ -96,6 +96,13 @@ void initialize_weights(int nodes, double *eta, double Lv, double lam,
                         int weightFlag, int isoFlag, double **conv_weights,
                         species species_i, species species_j);
 /* weights.h:45 (weights.c:127) */
+/* aniso_weights.c:37 (definition order; aniso_weights.h:1 swaps Lv and lam,
+   and boltz.c:154 calls it in definition order).  Landau kernel (glance = 0)
+   only: loads Weights/N%d_Aniso_L_v%g_lambda%g_Landau.wts or generates the
+   weights on the GPU and writes that file. */
+void initialize_weights_AnIso(int nodes, double *zeta, double Lv, double lam,
+                              int weightFlag, double **conv_weights,
+                              double glance);
 void dealloc_weights(int N, double **conv_weights);
 /* weights.h:43 (weights.c:265): GPU quadrature into conv_weights rows */
 void generate_conv_weights_iso(double **conv_weights);
@@ -154,6 +161,9 @@ int spectral_plan_get_weights(spectral_plan *plan, double *W_host,
                               long long row0, long long nrows);
 /* Conservation factors for one species of the given mass
    (initialize_conservation with Ns = 1). */
+/* Landau weights (aniso_weights.c:370-425: the 64 x 64-point Gauss-Legendre
+   double integral of gHat3L, no trapezoid factors) for the plan's grid. */
+int spectral_plan_generate_weights_landau(spectral_plan *plan, double lambda);
 int spectral_plan_set_conservation(spectral_plan *plan, double mass);
 
 /* Q for B instances.  f and Q are [B][N^3] FP64 in device memory; for

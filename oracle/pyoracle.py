@@ -66,6 +66,8 @@ def lib() -> C.CDLL:
             "oracle_ghat_integral": (d, [d, d, d, d, d]),
             "oracle_gauss_legendre": (None, [i, _dp, _dp]),
             "oracle_weights_iso": (None, [i, _dp, d, d, d, d, d, d, i, i, _dp, i]),
+            "oracle_weights_landau": (None, [i, _dp, d, d, i, i, _dp]),
+            "oracle_ghat3l": (d, [d, d, d, d, d, d, d, d]),
             "oracle_run_0d": (None, [i, d, _dp, _dp, d, d, i, i, i, _dp, i]),
             "oracle_init_bkw": (None, [i, _dp, d, _dp]),
             "oracle_conserve_batch1": (None, [C.c_void_p, _dp, i]),
@@ -204,6 +206,16 @@ def weights_iso(g: Grid, lam: float, rows=None, d_i=2.0, d_j=2.0, m_i=1.0,
     W = np.zeros((r1 - r0, n3))
     lib().oracle_weights_iso(g.N, _p(g.zeta), g.L_v, float(lam), d_i, d_j,
                              m_i, m_j, r0, r1, _p(W), nthreads)
+    return W
+
+
+def weights_landau(N: int, zeta: np.ndarray, L_v: float, lam: float, rows=None) -> np.ndarray:
+    """Rows of the Landau-kernel weights (aniso_weights.c:370-425); default all."""
+    n3 = N ** 3
+    r0, r1 = (0, n3) if rows is None else rows
+    zeta = np.ascontiguousarray(zeta, dtype=np.float64)
+    W = np.zeros((r1 - r0, n3))
+    lib().oracle_weights_landau(N, _p(zeta), float(L_v), float(lam), r0, r1 - r0, _p(W))
     return W
 
 

@@ -1055,3 +1055,63 @@ void oracle_run_1d(const oracle_1d *p, const double *W, double *f, int nT,
     }
     free(v); free(zeta); free(fconv); free(f1); free(scratch); free(Q);
 }
+
+/* gHat3L (aniso_weights.c:370-400): the Landau-kernel weight, a 64-point
+   Gauss-Legendre rule in r on [0, L_v] around a 64-point rule in theta on
+   [0, pi], as gsl_integration_glfixed applies it (nodes mid + half x_q,
+   result half sum w_q f).  j0 is the C library's Bessel J0, as the
+   reference calls it.  The operation order follows the reference. */
+double oracle_ghat3l(double zeta1, double zeta2, double zeta3, double xi1, double xi2,
+                     double xi3, double L_v, double lambda)
+{
+    static double gx[64], gw[64];
+    static int init = 0;
+    if (!init) {
+#pragma omp critical(oracle_gl64)
+        {
+            if (!init) { oracle_gauss_legendre(64, gx, gw); init = 1; }
+        }
+    }
+    double zetalen2 = zeta3 * zeta3 + zeta2 * zeta2 + zeta1 * zeta1;
+    double xilen2 = xi1 * xi1 + xi2 * xi2 + xi3 * xi3;
+    double xizeta = xi1 * zeta1 + xi2 * zeta2 + xi3 * zeta3;
+    double zetalen = sqrt(zetalen2);
+    double xiperp;
+    if (((xilen2 - xizeta * xizeta / zetalen2) < 0) || (zetalen2 == 0))
+        xiperp = 0;
+    else
+        xiperp = sqrt(xilen2 - xizeta * xizeta / zetalen2);
+    double a0 = xiperp, a1 = zetalen2, a2 = zetalen != 0 ? xizeta / zetalen : 0.0, a3 = zetalen;
+    double rmid = 0.5 * L_v, rhalf = 0.5 * L_v, tmid = 0.5 * M_PI, thalf = 0.5 * M_PI;
+    double outer = 0.0;
+    for (int p = 0; p < 64; p++) {
+        double r = rmid + rhalf * gx[p], inner = 0.0;
+        for (int q = 0; q < 64; q++) {
+            double th = tmid + thalf * gx[q];
+            double f = sin(th) * j0(r * a0 * sin(th)) *
+                       (-r * r * a1 * sin(th) * sin(th) * cos(r * a2 * cos(th)) +
+                        4 * r * a3 * sin(r * a2 * cos(th)) * cos(th));
+            inner += gw[q] * f;
+        }
+        outer += gw[p] * (pow(r, lambda + 2) * (thalf * inner));
+    }
+    return 2.0 * M_PI * (rhalf * outer);
+}
+
+/* Rows [row0, row0 + nrows) of the Landau weights as
+   generate_conv_weights_AnIso fills them (aniso_weights.c:402-425):
+   W[z][n + N (m + N l)] = gHat3L(eta_i, eta_j, eta_k, eta_l, eta_m, eta_n). */
+void oracle_weights_landau(int N, const double *eta, double L_v, double lambda, int row0,
+                           int nrows, double *W)
+{
+    long n3 = (long)N * N * N;
+#pragma omp parallel for schedule(dynamic)
+    for (int zr = 0; zr < nrows; zr++) {
+        int z = row0 + zr, k = z % N, j = ((z - k) / N) % N, i = (z - k - N * j) / (N * N);
+        for (int l = 0; l < N; l++)
+            for (int m = 0; m < N; m++)
+                for (int n = 0; n < N; n++)
+                    W[(long)zr * n3 + n + N * (m + (long)N * l)] =
+                        oracle_ghat3l(eta[i], eta[j], eta[k], eta[l], eta[m], eta[n], L_v, lambda);
+    }
+}

@@ -105,6 +105,10 @@ void oracle_conserve_batch1(const oracle_cons *c, double *Q, int B);
 /* ---- weight quadrature (weights.c:44, 136-160, 181-281) ---------------- */
 /* Gauss-Legendre nodes and weights on [-1,1] (n <= 256). */
 void oracle_gauss_legendre(int n, double *x, double *w);
+double oracle_ghat3l(double zeta1, double zeta2, double zeta3, double xi1, double xi2,
+                     double xi3, double L_v, double lambda);
+void oracle_weights_landau(int N, const double *eta, double L_v, double lambda, int row0,
+                           int nrows, double *W);
 /* Number of 16-point Gauss-Legendre panels the oracle uses on [0, L_v] for an
    integrand whose highest angular frequency is omega. */
 int oracle_quad_panels(double L_v, double omega);

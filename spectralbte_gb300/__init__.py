@@ -125,6 +125,8 @@ def lib() -> C.CDLL:
         "spectral_plan_destroy": (i, [v]),
         "spectral_plan_set_weights": (i, [v, v, i]),
         "spectral_plan_generate_weights_iso": (i, [v, d, d, d, d, d]),
+        "spectral_plan_generate_weights_landau": (i, [v, d]),
+        "initialize_weights_AnIso": (None, [i, _dp, d, d, i, C.POINTER(_dp), d]),
         "spectral_plan_get_weights": (i, [v, _dp, C.c_longlong, C.c_longlong]),
         "spectral_plan_set_conservation": (i, [v, d]),
         "spectral_computeQ_device": (i, [v, v, v, i, i, v]),
@@ -294,6 +296,13 @@ class ReferenceAPI:
             C.memmove(W[r].ctypes.data, table[r], 8 * n3)
         return W
 
+    def initialize_weights_AnIso(self, N, zeta, L_v, lam, weightFlag, table, glance=0.0):
+        """aniso_weights.c:37 (definition argument order)."""
+        zeta = np.ascontiguousarray(zeta, dtype=np.float64)
+        self._keep.append(zeta)
+        self.L.initialize_weights_AnIso(N, _p(zeta), float(L_v), float(lam), int(weightFlag),
+                                        table, float(glance))
+
     def dealloc_weights(self, N, table):
         self.L.dealloc_weights(N, table)
 
@@ -367,6 +376,11 @@ class Plan:
     def generate_weights_iso(self, lam: float, d_i=2.0, d_j=2.0, m_i=1.0, m_j=1.0):
         _check(self.L.spectral_plan_generate_weights_iso(self.h, float(lam), d_i, d_j, m_i, m_j),
                "generate_weights_iso")
+
+    def generate_weights_landau(self, lam: float):
+        """Landau-kernel weights (aniso_weights.c:370-425) on the device."""
+        _check(self.L.spectral_plan_generate_weights_landau(self.h, float(lam)),
+               "generate_weights_landau")
 
     def get_weights(self, row0: int = 0, nrows: Optional[int] = None) -> np.ndarray:
         nrows = self.n3 - row0 if nrows is None else nrows

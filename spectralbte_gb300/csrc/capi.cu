@@ -338,6 +338,51 @@ struct IsoWeightSpec {
 };
 
 // Quadrature on the GPU into wd.w64.
+// Landau weights of aniso_weights.c:370-425 into wd (FP64 rows on the device).
+static int generate_landau_device(WeightsDev &wd, int N, double L_v, double lambda,
+                                  const double *zeta_host, cudaStream_t st)
+{
+    const long long n3 = (long long)N * N * N;
+    if (wd.N != N || !wd.w64) {
+        wd.release();
+        SBTE_TRY(dalloc(&wd.w64, (size_t)(n3 * n3)));
+        wd.N = N;
+    }
+    dfree(wd.w32);
+    dfree(wd.w32x2);
+    std::vector<double> gx, gw;
+    gl_nodes(64, gx, gw);  // gsl_integration_glfixed_table_alloc(64), aniso_weights.c:44
+    double *d_zeta = nullptr, *d_gx = nullptr, *d_gw = nullptr;
+    int rc = kOk;
+    if ((rc = dalloc(&d_zeta, N)) || (rc = dalloc(&d_gx, 64)) || (rc = dalloc(&d_gw, 64))) {
+        dfree(d_zeta); dfree(d_gx); dfree(d_gw);
+        return rc;
+    }
+    cudaMemcpyAsync(d_zeta, zeta_host, sizeof(double) * N, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(d_gx, gx.data(), sizeof(double) * 64, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(d_gw, gw.data(), sizeof(double) * 64, cudaMemcpyHostToDevice, st);
+    // 4096 quadrature points per entry: rows in chunks of about 2^18 entries
+    const long long chunk = std::max<long long>(1, (1LL << 18) / n3);
+    for (long long r0 = 0; r0 < n3 && rc == kOk; r0 += chunk) {
+        const int nr = (int)std::min<long long>(chunk, n3 - r0);
+        cudaError_t e = weights_landau(wd.w64 + r0 * n3, (int)r0, nr, d_zeta, N, L_v, lambda,
+                                       d_gx, d_gw, st);
+        if (e != cudaSuccess) {
+            set_error(kErrCuda, "weights_landau: %s", cudaGetErrorString(e));
+            rc = kErrCuda;
+        } else {
+            count(1);
+        }
+    }
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (rc == kOk && e != cudaSuccess) {
+        set_error(kErrCuda, "weights_landau: %s", cudaGetErrorString(e));
+        rc = kErrCuda;
+    }
+    dfree(d_zeta); dfree(d_gx); dfree(d_gw);
+    return rc;
+}
+
 static int generate_iso_device(WeightsDev &wd, const IsoWeightSpec &s,
                                cudaStream_t st)
 {
@@ -947,6 +992,16 @@ int spectral_plan_generate_weights_iso(spectral_plan *p, double lambda, double d
     s.m_j = m_j;
     s.zeta = p->zeta;
     return generate_iso_device(p->W, s, p->stream);
+}
+
+int spectral_plan_generate_weights_landau(spectral_plan *p, double lambda)
+{
+    if (!p) {
+        set_error(kErrArg, "spectral_plan_generate_weights_landau: null plan");
+        return kErrArg;
+    }
+    SBTE_CUDA(cudaSetDevice(p->device));
+    return generate_landau_device(p->W, p->N, p->L_v, lambda, p->zeta.data(), p->stream);
 }
 
 int spectral_plan_get_weights(spectral_plan *p, double *W_host, long long row0,
@@ -1760,6 +1815,76 @@ void initialize_weights(int nodes, double *eta, double Lv, double lam, int weigh
     if (ensure_device() != kOk ||
         upload_weights(g_w.dev[conv_weights], nodes, nullptr, conv_weights, false, st) != kOk)
         report("initialize_weights");
+}
+
+// aniso_weights.c:37-150 for the Landau kernel (glance == 0): load
+// Weights/N%d_Aniso_L_v%g_lambda%g_Landau.wts (the name of aniso_weights.c:66,
+// which differs in case from the one weights.c:73 writes) unless weightFlag
+// forces regeneration; otherwise generate on the GPU and write the file.
+// The grazing-collision (Coulomb) weights of glance != 0 need the nested
+// adaptive quadrature of aniso_weights.c:150-350 and are not provided here.
+void initialize_weights_AnIso(int nodes, double *zeta, double Lv, double lam, int weightFlag,
+                              double **conv_weights, double glance)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    const long long n3 = (long long)nodes * nodes * nodes;
+    if (glance != 0.0) {
+        set_error(kErrUnsupported,
+                  "initialize_weights_AnIso: grazing-collision weights (glance=%g) are not "
+                  "generated by this library; only the Landau kernel (glance=0) is", glance);
+        report("initialize_weights_AnIso");
+        return;
+    }
+    for (long long i = 0; i < n3; i++)  // aniso_weights.c:60-62
+        conv_weights[i] = (double *)malloc(sizeof(double) * n3);
+    char name[256];
+    snprintf(name, sizeof(name), "Weights/N%d_Aniso_L_v%g_lambda%g_Landau.wts", nodes, Lv, lam);
+    FILE *fid = nullptr;
+    cudaStream_t st = g_coll.plan ? g_coll.plan->stream : nullptr;
+    if (weightFlag == 0 && (fid = fopen(name, "r"))) {
+        for (long long i = 0; i < n3; i++) {
+            if ((long long)fread(conv_weights[i], sizeof(double), n3, fid) != n3) {
+                set_error(kErrWeights, "short read of weight file %s", name);
+                report("initialize_weights_AnIso");
+                fclose(fid);
+                return;
+            }
+        }
+        fclose(fid);
+        if (ensure_device() != kOk ||
+            upload_weights(g_w.dev[conv_weights], nodes, nullptr, conv_weights, false, st) != kOk)
+            report("initialize_weights_AnIso");
+        return;
+    }
+    if (ensure_device() != kOk) {
+        report("initialize_weights_AnIso");
+        return;
+    }
+    WeightsDev &wd = g_w.dev[conv_weights];
+    if (generate_landau_device(wd, nodes, Lv, lam, zeta, st) != kOk) {
+        report("initialize_weights_AnIso");
+        return;
+    }
+    for (long long r = 0; r < n3; r++) {
+        if (cudaMemcpy(conv_weights[r], wd.w64 + r * n3, sizeof(double) * n3,
+                       cudaMemcpyDeviceToHost) != cudaSuccess) {
+            set_error(kErrCuda, "initialize_weights_AnIso: weights D2H failed");
+            report("initialize_weights_AnIso");
+            return;
+        }
+    }
+    fid = fopen(name, "w");
+    if (!fid) {
+        set_error(kErrWeights, "cannot open %s for writing", name);
+        report("initialize_weights_AnIso");
+        return;
+    }
+    for (long long i = 0; i < n3; i++) fwrite(conv_weights[i], sizeof(double), n3, fid);
+    if (fflush(fid) != 0) {
+        set_error(kErrWeights, "storing the weights in %s failed", name);
+        report("initialize_weights_AnIso");
+    }
+    fclose(fid);
 }
 
 void dealloc_weights(int N, double **conv_weights)

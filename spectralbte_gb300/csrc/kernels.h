@@ -170,4 +170,11 @@ cudaError_t weights_iso(double *W, int row0, int nrows, const double *zeta,
                         const double *glw, double *loss_scratch,
                         cudaStream_t st);
 
+// Landau weights (aniso_weights.c:370-425) for rows [row0, row0 + nrows)
+// into W[row - row0][N^3] (FP64); glx, glw: the 64-point Gauss-Legendre rule
+// on [-1, 1] (device).
+cudaError_t weights_landau(double *W, int row0, int nrows, const double *zeta, int N,
+                           double L_v, double lambda, const double *glx, const double *glw,
+                           cudaStream_t st);
+
 }  // namespace sbte

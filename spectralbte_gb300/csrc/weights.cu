@@ -138,7 +138,75 @@ rows_kernel(double *__restrict__ W, int row0, const double *__restrict__ zeta,
     }
 }
 
+// Landau weights (gHat3L, aniso_weights.c:370-400, as generate_conv_weights_AnIso
+// fills them, :402-425): one thread per (zeta, xi) entry,
+//   W = 2 pi  GL64_{r in [0, L_v]} r^{lambda+2}  GL64_{theta in [0, pi]}
+//         sin(th) J0(r xi_perp sin th) (-r^2 |zeta|^2 sin^2 th cos(r a cos th)
+//                                       + 4 r |zeta| sin(r a cos th) cos th),
+// a = xi.zeta/|zeta|, xi_perp = |xi - a zeta/|zeta||, with the reference's
+// 64-point Gauss-Legendre rule (gsl_integration_glfixed) on both axes and its
+// operation order.  No trapezoid weights and no prefactor, as in the reference.
+__global__ void __launch_bounds__(256)
+landau_kernel(double *__restrict__ W, int row0, int nrows, const double *__restrict__ zeta,
+              int N, double L_v, double lambda, const double *__restrict__ glx,
+              const double *__restrict__ glw)
+{
+    __shared__ double sx[64], sw[64];
+    for (int q = threadIdx.x; q < 64; q += blockDim.x) {
+        sx[q] = glx[q];
+        sw[q] = glw[q];
+    }
+    __syncthreads();
+    const long long n3 = (long long)N * N * N;
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (long long)nrows * n3) return;
+    const long long z = row0 + e / n3, x = e % n3;
+    const int k = (int)(z % N), j = (int)((z / N) % N), i = (int)(z / ((long long)N * N));
+    const int n = (int)(x % N), m = (int)((x / N) % N), l = (int)(x / ((long long)N * N));
+    const double z1 = zeta[i], z2 = zeta[j], z3 = zeta[k];
+    const double x1 = zeta[l], x2 = zeta[m], x3 = zeta[n];
+    const double zetalen2 = z3 * z3 + z2 * z2 + z1 * z1;
+    const double xilen2 = x1 * x1 + x2 * x2 + x3 * x3;
+    const double xizeta = x1 * z1 + x2 * z2 + x3 * z3;
+    const double zetalen = sqrt(zetalen2);
+    double xiperp;
+    if (((xilen2 - xizeta * xizeta / zetalen2) < 0) || (zetalen2 == 0))
+        xiperp = 0;
+    else
+        xiperp = sqrt(xilen2 - xizeta * xizeta / zetalen2);
+    const double a0 = xiperp, a1 = zetalen2, a2 = zetalen != 0 ? xizeta / zetalen : 0.0,
+                 a3 = zetalen;
+    const double rmid = 0.5 * L_v, rhalf = 0.5 * L_v;
+    const double tmid = 0.5 * M_PI, thalf = 0.5 * M_PI;
+    double outer = 0.0;
+    for (int p = 0; p < 64; p++) {
+        const double r = rmid + rhalf * sx[p];
+        double inner = 0.0;
+        for (int q = 0; q < 64; q++) {
+            const double th = tmid + thalf * sx[q];
+            const double st = sin(th), ct = cos(th);
+            const double f = st * j0(r * a0 * st) *
+                             (-r * r * a1 * st * st * cos(r * a2 * ct) +
+                              4 * r * a3 * sin(r * a2 * ct) * ct);
+            inner += sw[q] * f;
+        }
+        outer += sw[p] * (pow(r, lambda + 2) * (thalf * inner));
+    }
+    W[e] = 2.0 * M_PI * (rhalf * outer);
+}
+
 }  // namespace
+
+cudaError_t weights_landau(double *W, int row0, int nrows, const double *zeta, int N,
+                           double L_v, double lambda, const double *glx, const double *glw,
+                           cudaStream_t st)
+{
+    const long long total = (long long)nrows * N * N * N;
+    if (total <= 0) return cudaSuccess;
+    landau_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(W, row0, nrows, zeta, N, L_v,
+                                                                   lambda, glx, glw);
+    return cudaGetLastError();
+}
 
 int weights_panels_needed(const WeightParams &wp)
 {

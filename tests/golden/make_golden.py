@@ -16,7 +16,12 @@ reference functions through ctypes and writes:
                        ComputeQ_maxPreserve and conserveAllMoments for grids
                        N = 6, 7, 8 (both fixtures' settings) and 16;
   moments_BKW8.txt, moments_heat_transport.txt
-                       copies of the reference's golden moment tables.
+                       copies of the reference's golden moment tables;
+  golden_landau.npz    Landau-kernel weights from the reference's own
+                       initialize_weights_AnIso (aniso_weights.c, glance = 0,
+                       64-point Gauss-Legendre through the GSL stand-in) on
+                       two small grids (python make_golden.py REF --landau
+                       writes only this file).
 
 For N other than 8, W comes from the oracle's quadrature (pinned to the .wts
 fixtures).  Tests regenerate it the same way, or on the GPU.
@@ -136,6 +141,34 @@ def two_maxwellian(g: po.Grid, rng, jitter=0.05):
     return np.ascontiguousarray(f.reshape(-1))
 
 
+def landau(ref_dir="/root/reference"):
+    """golden_landau.npz: the reference's initialize_weights_AnIso, run in a
+    scratch directory (it writes Weights/N*_Aniso_*_Landau.wts there)."""
+    import tempfile
+    assert po.build_ref(ref_dir), "reference sources not found"
+    L = C.CDLL(os.path.join(ROOT, "oracle", "_ref", "libspectral_ref.so"))
+    L.initialize_weights_AnIso.argtypes = [C.c_int, _dp, C.c_double, C.c_double, C.c_int,
+                                           C.POINTER(_dp), C.c_double]
+    out = {}
+    cwd = os.getcwd()
+    for name, N, L_v, lam in (("n4", 4, 4.0, 0.0), ("n5", 5, 3.0, 1.0)):
+        g = po.Grid(N, L_v, "0d")
+        rows = (_dp * g.n3)()
+        with tempfile.TemporaryDirectory() as d:
+            os.makedirs(os.path.join(d, "Weights"))
+            os.chdir(d)
+            try:
+                L.initialize_weights_AnIso(N, po._p(g.zeta), L_v, lam, 1, rows, 0.0)
+            finally:
+                os.chdir(cwd)
+        W = np.stack([np.ctypeslib.as_array(rows[i], shape=(g.n3,)).copy() for i in range(g.n3)])
+        out[f"{name}_meta"] = np.array([N, L_v, lam])
+        out[f"{name}_zeta"] = g.zeta.copy()
+        out[f"{name}_W"] = W
+        print("landau", name, W.shape, np.abs(W).max())
+    np.savez_compressed(os.path.join(HERE, "golden_landau.npz"), **out)
+
+
 def main(ref_dir="/root/reference"):
     assert po.build_ref(ref_dir), "reference sources not found"
     po.build()
@@ -197,4 +230,9 @@ def main(ref_dir="/root/reference"):
 
 
 if __name__ == "__main__":
-    main(*sys.argv[1:])
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    if "--landau" in sys.argv:
+        landau(*args)
+    else:
+        main(*args)
+        landau(*args)

@@ -303,3 +303,37 @@ def test_group_computeQ_matches_per_plan_calls(gpu, oracle):
     torch.cuda.synchronize()
     for a, b in zip(Qs, Qr):
         assert torch.equal(a, b)
+
+
+def test_landau_weights_on_device(gpu, ref_api, tmp_path, monkeypatch):
+    """Landau-kernel weights (aniso_weights.c:370-425) on the GPU against the
+    reference's own initialize_weights_AnIso (tests/golden/golden_landau.npz),
+    through the plan API and through the drop-in symbol, which also writes and
+    re-reads Weights/N*_Aniso_L_v*_lambda*_Landau.wts."""
+    from conftest import GOLDEN
+    d = np.load(os.path.join(GOLDEN, "golden_landau.npz"))
+    for name in ("n4", "n5"):
+        N, L_v, lam = d[f"{name}_meta"]
+        N = int(N)
+        zeta, ref = d[f"{name}_zeta"], d[f"{name}_W"]
+        v, _ = gpu.grid_0d(N, L_v)
+        plan = gpu.Plan(N, L_v, v, zeta, 1)
+        plan.generate_weights_landau(lam)
+        W = plan.get_weights()
+        assert np.abs(W - ref).max() <= 1e-12 * np.abs(ref).max(), name
+        plan.close()
+    monkeypatch.chdir(tmp_path)
+    os.makedirs("Weights")
+    N, L_v, lam = (float(x) for x in d["n4_meta"])
+    N = int(N)
+    tables = ref_api.alloc_weights(N, 1)
+    ref_api.initialize_weights_AnIso(N, d["n4_zeta"], L_v, lam, 0, tables[0])
+    fname = "Weights/N4_Aniso_L_v4_lambda0_Landau.wts"
+    assert os.path.getsize(fname) == 8 * 64 * 64
+    Wf = np.fromfile(fname).reshape(64, 64)
+    assert np.abs(Wf - d["n4_W"]).max() <= 1e-12 * np.abs(d["n4_W"]).max()
+    tables2 = ref_api.alloc_weights(N, 1)
+    ref_api.initialize_weights_AnIso(N, d["n4_zeta"], L_v, lam, 0, tables2[0])  # loads the file
+    assert np.array_equal(ref_api.table_to_numpy(tables2[0], N), Wf)
+    ref_api.dealloc_weights(N, tables[0])
+    ref_api.dealloc_weights(N, tables2[0])

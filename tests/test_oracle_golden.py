@@ -132,3 +132,16 @@ def test_heat_transport_golden_moments(oracle):
     assert real.sum() > 10
     assert np.all(np.abs(ux[real] - wux[real]) <= 1e-6 * np.abs(wux[real]))
     assert np.all(np.abs(ux[~real] - wux[~real]) < 1e-13)
+
+
+def test_landau_weights_match_reference(oracle):
+    """The oracle's gHat3L restatement against the reference's own
+    initialize_weights_AnIso (aniso_weights.c, Landau kernel), N = 4 and 5."""
+    import os
+    from conftest import GOLDEN
+    d = np.load(os.path.join(GOLDEN, "golden_landau.npz"))
+    for name in ("n4", "n5"):
+        N, L_v, lam = d[f"{name}_meta"]
+        W = oracle.weights_landau(int(N), d[f"{name}_zeta"], L_v, lam)
+        ref = d[f"{name}_W"]
+        assert np.abs(W - ref).max() <= 1e-13 * np.abs(ref).max(), name
