@@ -74,8 +74,8 @@ conserve_batch_kernel(double *__restrict__ Q, const double *__restrict__ v,
     double *Qb = Q + (long long)blockIdx.x * n3;
     const double dv = cp.dv, mass = cp.mass[0];
     double m[5] = {0, 0, 0, 0, 0};
-    for (long long x = threadIdx.x; x < n3; x += blockDim.x) {
-        const int i = (int)(x / (N * N)), j = (int)((x / N) % N), k = (int)(x % N);
+    for (int x = threadIdx.x; x < (int)n3; x += blockDim.x) {
+        const int i = x / (N * N), j = (x / N) % N, k = x % N;
         const double prefact = wt(i, N) * wt(j, N) * wt(k, N) * dv * dv * dv * mass;
         const double q = Qb[x];
         m[0] += q * prefact;
@@ -93,8 +93,8 @@ conserve_batch_kernel(double *__restrict__ Q, const double *__restrict__ v,
     }
     __syncthreads();
     const double l0 = lam[0], l1 = lam[1], l2 = lam[2], l3 = lam[3], l4 = lam[4];
-    for (long long x = threadIdx.x; x < n3; x += blockDim.x) {
-        const int i = (int)(x / (N * N)), j = (int)((x / N) % N), k = (int)(x % N);
+    for (int x = threadIdx.x; x < (int)n3; x += blockDim.x) {
+        const int i = x / (N * N), j = (x / N) % N, k = x % N;
         const double prefact = wt(i, N) * wt(j, N) * wt(k, N) * dv * dv * dv * mass / 1;
         const double t0 = prefact, t1 = prefact * v[i], t2 = prefact * v[j],
                      t3 = prefact * v[k],
@@ -114,8 +114,8 @@ conserve_species_kernel(double **__restrict__ Qp, const double *__restrict__ v,
     const long long n3 = (long long)N * N * N;
     const double dv = cp.dv;
     double m[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    for (long long x = threadIdx.x; x < n3; x += blockDim.x) {
-        const int i = (int)(x / (N * N)), j = (int)((x / N) % N), k = (int)(x % N);
+    for (int x = threadIdx.x; x < (int)n3; x += blockDim.x) {
+        const int i = x / (N * N), j = (x / N) % N, k = x % N;
         for (int s = 0; s < Ns; s++) {
             const double prefact = wt(i, N) * wt(j, N) * wt(k, N) * dv * dv * dv * cp.mass[s];
             const double tm = prefact, tx = prefact * v[i], ty = prefact * v[j],
@@ -139,8 +139,8 @@ conserve_species_kernel(double **__restrict__ Qp, const double *__restrict__ v,
         for (int t = 0; t < 8; t++) lam[t] = b[t];
     }
     __syncthreads();
-    for (long long x = threadIdx.x; x < n3; x += blockDim.x) {
-        const int i = (int)(x / (N * N)), j = (int)((x / N) % N), k = (int)(x % N);
+    for (int x = threadIdx.x; x < (int)n3; x += blockDim.x) {
+        const int i = x / (N * N), j = (x / N) % N, k = x % N;
         for (int s = 0; s < Ns; s++) {
             const double prefact = wt(i, N) * wt(j, N) * wt(k, N) * dv * dv * dv * cp.mass[s] / Ns;
             const double tm = prefact, tx = prefact * v[i], ty = prefact * v[j],
@@ -168,8 +168,8 @@ maxwellian_kernel(const double *__restrict__ f, double *__restrict__ M,
     const double dv3 = dv * dv * dv;
     // density and first moments (getDensity, getBulkVelocity)
     double s[4] = {0, 0, 0, 0};
-    for (long long x = threadIdx.x; x < n3; x += blockDim.x) {
-        const int i = (int)(x / (N * N)), j = (int)((x / N) % N), k = (int)(x % N);
+    for (int x = threadIdx.x; x < (int)n3; x += blockDim.x) {
+        const int i = x / (N * N), j = (x / N) % N, k = x % N;
         const double w = dv3 * wt(i, N) * wt(j, N) * wt(k, N);
         const double fx = f[off + x];
         s[0] += w * fx;
@@ -183,8 +183,8 @@ maxwellian_kernel(const double *__restrict__ f, double *__restrict__ M,
                  u2 = mass * (s[3] / rho);
     // temperature (getTemperature)
     double tt[1] = {0};
-    for (long long x = threadIdx.x; x < n3; x += blockDim.x) {
-        const int i = (int)(x / (N * N)), j = (int)((x / N) % N), k = (int)(x % N);
+    for (int x = threadIdx.x; x < (int)n3; x += blockDim.x) {
+        const int i = x / (N * N), j = (x / N) % N, k = x % N;
         const double t = (v[i] - u0) * (v[i] - u0) + (v[j] - u1) * (v[j] - u1) +
                          (v[k] - u2) * (v[k] - u2);
         tt[0] += t * dv3 * wt(i, N) * wt(j, N) * wt(k, N) * f[off + x];
@@ -192,8 +192,8 @@ maxwellian_kernel(const double *__restrict__ f, double *__restrict__ M,
     block_sum<1>(tt, red);
     const double T = (mass * mass / KB) * (tt[0] / (3.0 * rho));
     const double pre = rho * pow(0.5 / (M_PI * T), 1.5);
-    for (long long x = threadIdx.x; x < n3; x += blockDim.x) {
-        const int i = (int)(x / (N * N)), j = (int)((x / N) % N), k = (int)(x % N);
+    for (int x = threadIdx.x; x < (int)n3; x += blockDim.x) {
+        const int i = x / (N * N), j = (x / N) % N, k = x % N;
         const double Mx = pre * exp(-(0.5 / T) * ((v[i] - u0) * (v[i] - u0) +
                                                  (v[j] - u1) * (v[j] - u1) +
                                                  (v[k] - u2) * (v[k] - u2)));
@@ -224,8 +224,8 @@ moments_kernel(const double *__restrict__ f, int N, const double *__restrict__ v
     const double dv = v[1] - v[0];
     const double dv3 = dv * dv * dv;
     double s[4] = {0, 0, 0, 0};
-    for (long long x = threadIdx.x; x < n3; x += blockDim.x) {
-        const int i = (int)(x / (N * N)), j = (int)((x / N) % N), k = (int)(x % N);
+    for (int x = threadIdx.x; x < (int)n3; x += blockDim.x) {
+        const int i = x / (N * N), j = (x / N) % N, k = x % N;
         const double w = dv3 * wt(i, N) * wt(j, N) * wt(k, N);
         const double fx = fb[x];
         s[0] += w * fx;
@@ -237,8 +237,8 @@ moments_kernel(const double *__restrict__ f, int N, const double *__restrict__ v
     const double rho = mass * s[0];
     const double u0 = mass * (s[1] / rho), u1 = mass * (s[2] / rho), u2 = mass * (s[3] / rho);
     double t[3] = {0, 0, 0};
-    for (long long x = threadIdx.x; x < n3; x += blockDim.x) {
-        const int i = (int)(x / (N * N)), j = (int)((x / N) % N), k = (int)(x % N);
+    for (int x = threadIdx.x; x < (int)n3; x += blockDim.x) {
+        const int i = x / (N * N), j = (x / N) % N, k = x % N;
         const double w = dv3 * wt(i, N) * wt(j, N) * wt(k, N);
         const double fx = fb[x];
         t[0] += ((v[i] - u0) * (v[i] - u0) + (v[j] - u1) * (v[j] - u1) +

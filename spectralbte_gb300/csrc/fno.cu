@@ -477,6 +477,13 @@ cudaError_t launch_sa(SaArgs a, cudaStream_t st)
     if (a.M > MT || a.KP > 128 || a.Nn % 8 != 0 || !view_ok(a.B, a.B.p) ||
         !view_ok(a.C, a.C.p) || !sa_bounds_ok(a, AC))
         return cudaErrorInvalidValue;
+    // 32-bit index arithmetic on the device: n, items and block indices
+    const long long items = ((a.Nn + BN - 1) / BN) * a.nz;
+    if (a.Nn >= (1LL << 31) || items >= (1LL << 31) || a.B.w >= (1LL << 31) ||
+        a.C.w >= (1LL << 31))
+        return cudaErrorInvalidValue;
+    fastdiv_init((unsigned)a.B.w, a.B.wm, a.B.ws);
+    fastdiv_init((unsigned)a.C.w, a.C.wm, a.C.ws);
     const size_t sm = gemm_sa_smem<MT, BN, WM, WN, AC, BC, EPI, ST>(a.KP);
     auto kern = gemm_sa_kernel<E, MT, BN, WM, WN, AC, BC, EPI, ST>;
     if (sm > 48 * 1024) {
@@ -506,6 +513,10 @@ cudaError_t launch_nt(NtArgs a, cudaStream_t st)
     if ((a.extA > 0 && ext(a.M, a.a_m, a.a_w, a.a_blk, a.a_z1, a.a_z2) > a.extA) ||
         (a.extB > 0 && ext(a.N, a.b_n, a.b_w, a.b_blk, a.b_z1, a.b_z2) > a.extB))
         return cudaErrorInvalidValue;
+    if (a.K >= (1LL << 31) || a.a_w >= (1LL << 31) || a.b_w >= (1LL << 31))
+        return cudaErrorInvalidValue;
+    fastdiv_init((unsigned)a.a_w, a.awm, a.aws);
+    fastdiv_init((unsigned)a.b_w, a.bwm, a.bws);
     const long long total = ((a.K + a.KC - 1) / a.KC) * a.nz;
     const int grid = (int)std::min<long long>(total, 152LL * 4);
     gemm_nt_kernel<E, MT, NT, WM, WN><<<grid, WM * WN * 32, 0, st>>>(a);

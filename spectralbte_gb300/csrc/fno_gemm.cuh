@@ -19,6 +19,10 @@
 // i.e. n runs over blocks of w contiguous elements (w a multiple of 8).
 // Complex tensors store the real and imaginary parts as two such views im
 // elements apart.  Batches: z -> (z / nz2) * s_z1 + (z % nz2) * s_z2.
+// n / w is evaluated with a multiply-high by a magic number precomputed on
+// the host (division by an invariant integer, Granlund and Montgomery
+// 1994), on 32-bit n: a 64-bit integer division costs tens of instructions
+// per 16-byte chunk and made these kernels issue-bound.
 #pragma once
 
 #include <cuda_bf16.h>
@@ -52,7 +56,22 @@ template <> struct Elem<f16> {
 struct StreamView {
     const void *p;
     long long s_r, s_blk, w, im, s_z1, s_z2;
+    unsigned wm, ws;  // n / w = (umulhi(n, wm) + n) >> ws   (set by fastdiv_init)
 };
+
+// Magic multiplier and shift for unsigned 32-bit division by d >= 1:
+// s = ceil(log2 d), m = floor(2^32 (2^s - d) / d) + 1; then for every
+// 32-bit n, n / d = (umulhi(n, m) + n) >> s, the sum taken in 64 bits.
+inline void fastdiv_init(unsigned d, unsigned &m, unsigned &s)
+{
+    s = 0;
+    while ((1ull << s) < d) s++;
+    m = (unsigned)(((1ull << 32) * ((1ull << s) - d)) / d + 1);
+}
+__device__ __forceinline__ unsigned fastdiv(unsigned n, unsigned m, unsigned s)
+{
+    return (unsigned)(((unsigned long long)__umulhi(n, m) + n) >> s);
+}
 
 enum Epi : int {
     kEpiBF16 = 0,     // real output, BF16 store
@@ -107,6 +126,7 @@ struct NtArgs {
     int nz, nz2;
     float alpha;
     long long extA, extB, extC;  // host-side bounds check (element counts)
+    unsigned awm, aws, bwm, bws;  // fast division by a_w and b_w (fastdiv_init)
 };
 
 __device__ __forceinline__ float gelu_f(float x)
@@ -165,11 +185,14 @@ __device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], 
 
 __device__ __forceinline__ long long view_off(const StreamView &v, long long r, long long n)
 {
-    return r * v.s_r + (n / v.w) * v.s_blk + (n % v.w);
+    const unsigned nn = (unsigned)n;
+    const unsigned q = fastdiv(nn, v.wm, v.ws);
+    return r * v.s_r + (long long)q * v.s_blk + (long long)(nn - q * (unsigned)v.w);
 }
 __device__ __forceinline__ long long zoff(long long z, int nz2, long long s1, long long s2)
 {
-    return (z / nz2) * s1 + (z % nz2) * s2;
+    const unsigned q = (unsigned)z / (unsigned)nz2;  // z < 2^31 (checked on the host)
+    return (long long)q * s1 + (long long)((unsigned)z - q * (unsigned)nz2) * s2;
 }
 
 // ------------------------------------------------------------ gemm_sa ---
@@ -222,15 +245,15 @@ __global__ void __launch_bounds__(WM *WN * 32) gemm_sa_kernel(const SaArgs a)
     E *own = ring + ST * stageE;  // output staging tile (kOwnStage)
     float *red = reinterpret_cast<float *>(own + L::kStageRows * BP);  // kEpiProj: [WM][BN]
 
-    const long long ntiles = (a.Nn + BN - 1) / BN;
-    const long long total = ntiles * a.nz;
-    long long item = blockIdx.x;
+    const unsigned ntiles = (unsigned)((a.Nn + BN - 1) / BN);
+    const unsigned total = ntiles * (unsigned)a.nz;
+    unsigned item = blockIdx.x;
     if (item >= total) return;
 
     const E *Bb = static_cast<const E *>(a.B.p);
-    auto issue = [&](long long it, int stage) {
-        const long long z = it / ntiles;
-        const long long n0 = (it % ntiles) * BN;
+    auto issue = [&](unsigned it, int stage) {
+        const unsigned z = it / ntiles;
+        const long long n0 = (long long)(it - z * ntiles) * BN;
         const long long zb = zoff(z, a.nz2, a.B.s_z1, a.B.s_z2);
         E *base = ring + stage * stageE;
         for (int c = threadIdx.x; c < KP * CH; c += NTH) {
@@ -259,7 +282,7 @@ __global__ void __launch_bounds__(WM *WN * 32) gemm_sa_kernel(const SaArgs a)
 
 #pragma unroll
     for (int s = 0; s < ST - 1; s++) {
-        const long long it = item + (long long)s * gridDim.x;
+        const unsigned it = item + (unsigned)s * gridDim.x;
         if (it < total) issue(it, s);
         cp_async_commit();
     }
@@ -270,12 +293,12 @@ __global__ void __launch_bounds__(WM *WN * 32) gemm_sa_kernel(const SaArgs a)
     long long cur_z = -1;
     int stage = 0;
     for (; item < total; item += gridDim.x) {
-        const long long pre = item + (long long)(ST - 1) * gridDim.x;
+        const unsigned pre = item + (unsigned)(ST - 1) * gridDim.x;
         if (pre < total) issue(pre, (stage + ST - 1) % ST);
         cp_async_commit();
-        const long long z = item / ntiles;
-        const long long n0 = (item % ntiles) * BN;
-        if (cur_z < 0 || (a.a_tab && z != cur_z)) {
+        const unsigned z = item / ntiles;
+        const long long n0 = (long long)(item - z * ntiles) * BN;
+        if (cur_z < 0 || (a.a_tab && (long long)z != cur_z)) {
             __syncthreads();
             const long long aoff = a.a_tab ? (long long)a.a_tab[z] * a.s_atab : 0;
             for (int e = threadIdx.x; e < MT * KP; e += NTH) {
@@ -543,14 +566,20 @@ __global__ void __launch_bounds__(WM *WN * 32) gemm_nt_kernel(const NtArgs a)
                 const long long k = kt + ck * 8;
                 if (row < MT) {
                     const bool ok = row < a.M && k < k1;
+                    const unsigned kq = fastdiv((unsigned)k, a.awm, a.aws);
                     const long long off =
-                        ok ? zA + row * a.a_m + (k / a.a_w) * a.a_blk + (k % a.a_w) : 0;
+                        ok ? zA + row * a.a_m + (long long)kq * a.a_blk +
+                                 (long long)((unsigned)k - kq * (unsigned)a.a_w)
+                           : 0;
                     cp_async16(&sA[st][row * P + ck * 8], static_cast<const E *>(a.A) + off, ok);
                 } else {
                     const int n = row - MT;
                     const bool ok = n < a.N && k < k1;
+                    const unsigned kq = fastdiv((unsigned)k, a.bwm, a.bws);
                     const long long off =
-                        ok ? zB + n * a.b_n + (k / a.b_w) * a.b_blk + (k % a.b_w) : 0;
+                        ok ? zB + n * a.b_n + (long long)kq * a.b_blk +
+                                 (long long)((unsigned)k - kq * (unsigned)a.b_w)
+                           : 0;
                     cp_async16(&sB[st][n * P + ck * 8], static_cast<const E *>(a.B) + off, ok);
                 }
             }
