@@ -1090,6 +1090,9 @@ int spectral_1d_setup(spectral_plan *p, int nX, int order, int ic, double dt, do
 {
     if (!p || nX < 3 || (order != 1 && order != 2) || !x || !dx || Kn <= 0)
         return set_error(kErrArg, "spectral_1d_setup: bad arguments"), kErrArg;
+    if ((long long)(nX + 2 * order) * p->n3 >= (1LL << 31))  // 32-bit cell indexing
+        return set_error(kErrArg, "spectral_1d_setup: (nX + 2 order) N^3 must stay below 2^31"),
+               kErrArg;
     SBTE_CUDA(cudaSetDevice(p->device));
     const int nc = nX + 2 * order;
     TransportParams tp{p->N, nX, order, ic, dt, T0, T1, TWall, mass,

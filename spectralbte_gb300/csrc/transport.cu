@@ -46,9 +46,9 @@ diffuse_bc_kernel(BcJob j0, BcJob j1, int njobs, const double *__restrict__ v, i
     const long long nh = (long long)half * N * N;
     const double h_v = v[1] - v[0];
     double s = 0.0;
-    for (long long t = threadIdx.x; t < nh; t += blockDim.x) {
-        const int i = ilo + (int)(t / (N * N));
-        const int jj = (int)((t / N) % N), k = (int)(t % N);
+    for (int t = threadIdx.x; t < (int)nh; t += blockDim.x) {
+        const int i = ilo + t / (N * N);
+        const int jj = (t / N) % N, k = t % N;
         s += v[i] * wtn(i, N) * wtn(jj, N) * wtn(k, N) * h_v * h_v * h_v *
              j.in[k + (long long)N * (jj + (long long)N * i)];
     }
@@ -62,9 +62,9 @@ diffuse_bc_kernel(BcJob j0, BcJob j1, int njobs, const double *__restrict__ v, i
     const double pre = sigmaW * pow(0.5 * mass / (M_PI * KB * j.TW), 1.5);
     const double ex = -0.5 * mass / (KB * j.TW);
     const int olo = j.right ? 0 : half;
-    for (long long t = threadIdx.x; t < nh; t += blockDim.x) {
-        const int i = olo + (int)(t / (N * N));
-        const int jj = (int)((t / N) % N), k = (int)(t % N);
+    for (int t = threadIdx.x; t < (int)nh; t += blockDim.x) {
+        const int i = olo + t / (N * N);
+        const int jj = (t / N) % N, k = t % N;
         j.out[k + (long long)N * (jj + (long long)N * i)] =
             pre * exp(ex * (v[i] * v[i] + v[jj] * v[jj] + v[k] * v[k]));
     }
@@ -79,9 +79,10 @@ __global__ void upwind1_kernel(const double *__restrict__ f, double *__restrict_
     const long long total = (long long)nX * n3;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
          t += (long long)gridDim.x * blockDim.x) {
-        const int l = 1 + (int)(t / n3);
-        const long long q = t % n3;
-        const int i = (int)(q / (N * N)), j = (int)((q / N) % N);
+        const unsigned tc = (unsigned)t / (unsigned)n3;  // 32-bit: nX N^3 < 2^31
+        const int l = 1 + (int)tc;
+        const long long q = (long long)((unsigned)t - tc * (unsigned)n3);
+        const int i = (int)q / (N * N), j = ((int)q / N) % N;
         const double *fl = f + (long long)l * n3;
         const double CFL = dt * v[i] / dx[l];
         double r;
@@ -119,7 +120,7 @@ __global__ void wall_values_kernel(const double *__restrict__ f, double *__restr
          t += (long long)gridDim.x * blockDim.x) {
         const bool right = t >= n3;
         const long long q = right ? t - n3 : t;
-        const int i = (int)(q / (N * N));
+        const int i = (int)q / (N * N);
         const bool upper = i >= N / 2;
         if (!right) {
             const double s1 = slope_at(f, x, 2, q, n3);
@@ -146,9 +147,10 @@ __global__ void upwind2_kernel(const double *__restrict__ f, double *__restrict_
     const double h_v = v[1] - v[0];
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
          t += (long long)gridDim.x * blockDim.x) {
-        const int l = 2 + (int)(t / n3);
-        const long long q = t % n3;
-        const int i = (int)(q / (N * N)), j = (int)((q / N) % N);
+        const unsigned tc = (unsigned)t / (unsigned)n3;  // 32-bit: nX N^3 < 2^31
+        const int l = 2 + (int)tc;
+        const long long q = (long long)((unsigned)t - tc * (unsigned)n3);
+        const int i = (int)q / (N * N), j = ((int)q / N) % N;
         const double *fl = f + (long long)l * n3;
         const double CFL = 0.5 * dt * v[i] / dx[l];
         double r;
