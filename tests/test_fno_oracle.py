@@ -125,3 +125,23 @@ def test_layout_matches_library_count(lib_built):
     assert n1 == want - Hd // 2
     assert cls.shape == (12, 12, 12) and cls.max() == ncls - 1
     assert "spectral_fno_create" in sb.declared_symbols()
+
+
+def test_gelu_erf_approximation_bound():
+    """The device GELU's erf (Abramowitz and Stegun 7.1.26, fno_gemm.cuh
+    erf_as), evaluated in float32 with the same constants, stays within
+    1e-6 of the exact erf on [-12, 12]."""
+    import re
+    from scipy.special import erf
+    src = open(__import__("os").path.join(__import__("os").path.dirname(__file__), "..",
+                                          "spectralbte_gb300", "csrc", "fno_gemm.cuh")).read()
+    body = src[src.index("float erf_as("):src.index("float gelu_f(")]
+    consts = [float(c[:-1]) for c in re.findall(r"-?\d+\.\d+f", body)]
+    p, a5, a4, a3, a2, a1 = consts[0], consts[2], consts[3], consts[4], consts[5], consts[6]
+    f32 = np.float32
+    x = np.linspace(-12, 12, 400001).astype(f32)
+    ax = np.abs(x)
+    t = (f32(1) / (f32(p) * ax + f32(1))).astype(f32)
+    poly = ((((f32(a5) * t + f32(a4)) * t + f32(a3)) * t + f32(a2)) * t + f32(a1)) * t
+    r = np.copysign((f32(1) - poly * np.exp(-(ax * ax)).astype(f32)).astype(f32), x)
+    assert np.abs(r - erf(x.astype(np.float64))).max() < 1e-6
