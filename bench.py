@@ -400,6 +400,52 @@ def run_learned_only(args):
     return 0
 
 
+def run_bkw(args):
+    """Config 1: 0D Maxwell molecules, N=16, L_v=5, one BKW instance (K=0.65),
+    dt = 0.01, 200 RK2 steps of the plain FP64 operator with maxPreserve and
+    conservation, one CUDA graph per step; the analytic BKW solution
+    (K(t) = 1 - exp(-t/6), initializer.c:121-135) judges the result."""
+    import math
+    import torch
+    import spectralbte_gb300 as sb
+    from spectralbte_gb300 import workloads as wl
+    torch.cuda.set_device(0)
+    N, L_v, dt = 16, 5.0, 0.01
+    steps = args.nsteps or 200
+    v, zeta = sb.grid_0d(N, L_v)
+    plan = sb.Plan(N, L_v, v, zeta, 1)
+    plan.generate_weights_iso(0.0)
+    K0 = 0.65
+    t0 = -6.0 * math.log(1.0 - K0)
+    f0 = wl.bkw(v, K0)
+    fd = torch.from_numpy(f0[None].copy()).cuda()
+    flags = sb.FP64 | sb.MAXPRESERVE
+    plan.capture(0, fd, 1, dt, 1.0, 2, flags)
+    torch.cuda.synchronize()
+    k0 = sb.kernel_launches()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        plan.launch()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    fa = wl.bkw(v, 1.0 - math.exp(-(t0 + steps * dt) / 6.0))
+    f = fd.cpu().numpy()[0]
+    err = float(np.linalg.norm(f - fa) / np.linalg.norm(fa))
+    print(json.dumps({
+        "metric": "0D time steps/s (config 1, FP64)", "impl": "ours", "value": 1e3 / ms,
+        "unit": "steps/s", "ms_per_step": ms, "steps": steps, "n_gpus": 1,
+        "higher_is_better": True, "dtype": "f64", "data": "synthetic (BKW, K=0.65)",
+        "config": {"workload": "0D Maxwell molecules, N=16, L_v=5, dt=0.01, RK2, maxPreserve",
+                   "N": N, "L_v": L_v, "lambda": 0.0},
+        "gpu_launches": sb.kernel_launches() - k0,
+        "rel_l2_vs_analytic_bkw": err,
+        "rel_l2_change_over_run": float(np.linalg.norm(f0 - fa) / np.linalg.norm(fa))}),
+        flush=True)
+    return 0
+
+
 CFG_1D = {
     # config 3: the reference's Mach-1.2 shock (Init_field 6), minmod transport
     "shock": dict(N=24, L_v=6.0, lam=1.0, nX=128, order=2, ic=6, dt=0.001, Kn=0.1, steps=500,
@@ -699,7 +745,7 @@ def main():
     ap.add_argument("--cpu-rows", type=int, default=2048)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="n32",
-                    choices=["n32", "uneven", "learned", "shock", "heat"])
+                    choices=["n32", "uneven", "learned", "shock", "heat", "bkw"])
     ap.add_argument("--nsteps", type=int, default=0,
                     help="time steps of the shock / heat workloads (default: the config's)")
     ap.add_argument("--learned", default="",
@@ -714,6 +760,8 @@ def main():
         return run_learned_only(args)
     if args.workload in CFG_1D and args.impl != "reference":
         return run_1d(args)
+    if args.workload == "bkw" and args.impl != "reference":
+        return run_bkw(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

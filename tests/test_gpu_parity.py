@@ -337,3 +337,32 @@ def test_landau_weights_on_device(gpu, ref_api, tmp_path, monkeypatch):
     assert np.array_equal(ref_api.table_to_numpy(tables2[0], N), Wf)
     ref_api.dealloc_weights(N, tables[0])
     ref_api.dealloc_weights(N, tables2[0])
+
+
+def test_config1_bkw_tracks_analytic_solution(gpu):
+    """Config 1: 0D Maxwell molecules (lambda = 0), N = 16, L_v = 5, BKW data
+    with K = 0.65, dt = 0.01, 200 RK2 steps of the plain FP64 operator with
+    maxPreserve and conservation.  The reference's BKW case follows
+    K(t) = 1 - exp(-t/6) (initializer.c:121-135), so K = 0.65 is the
+    solution at t0 = -6 ln 0.35, and after 200 steps f must match the
+    analytic BKW distribution at t0 + 2 to the discretisation error (5e-3,
+    against a 24% change of f over the run)."""
+    import math
+    import torch
+    from spectralbte_gb300 import workloads as wl
+    N, L_v, dt, nT = 16, 5.0, 0.01, 200
+    v, zeta = gpu.grid_0d(N, L_v)
+    plan = gpu.Plan(N, L_v, v, zeta, 1)
+    plan.generate_weights_iso(0.0)
+    K0 = 0.65
+    t0 = -6.0 * math.log(1.0 - K0)
+    f0 = wl.bkw(v, K0)
+    fd = torch.from_numpy(f0[None].copy()).cuda()
+    for _ in range(nT):
+        plan.step_device(fd, 1, dt, 1.0, 2, gpu.FP64 | gpu.MAXPRESERVE)
+    fa = wl.bkw(v, 1.0 - math.exp(-(t0 + nT * dt) / 6.0))
+    f = fd.cpu().numpy()[0]
+    err, change = rel_l2(f, fa), rel_l2(f0, fa)
+    assert change > 0.2
+    assert err < 5e-3 and err < 0.05 * change, (err, change)
+    plan.close()
