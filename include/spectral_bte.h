@@ -173,7 +173,11 @@ int spectral_plan_set_conservation(spectral_plan *plan, double mass);
    Asynchronous with respect to the host. */
 int spectral_computeQ_device(spectral_plan *plan, const double *f_dev,
                              double *Q_dev, int B, int flags, void *stream);
-/* Same with host arrays: copies in, computes, copies out, synchronises. */
+/* Same with host arrays: copies in, computes, copies out, synchronises.  The
+   batch runs in chunks of whole instance groups on the plan's stream, with
+   the copies on two other streams, so that each chunk's copies overlap the
+   neighbouring chunks' compute (pinned host memory makes the copies
+   asynchronous). */
 int spectral_computeQ_host(spectral_plan *plan, const double *f_host,
                            double *Q_host, int B, int flags);
 /* conserveAllMoments on [B][N^3] device arrays, FP64, in place. */

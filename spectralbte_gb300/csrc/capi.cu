@@ -498,6 +498,8 @@ struct spectral_plan_s {
     // host staging for spectral_computeQ_host
     int caphost = 0;
     double *d_fh = nullptr, *d_Qh = nullptr;
+    cudaStream_t copy_in = nullptr, copy_out = nullptr;  // host transfers of computeQ_host
+    std::vector<cudaEvent_t> host_events;
     // learned operator (spectral_plan_set_learned) and its spot-check state
     spectral_fno_s *fno = nullptr;
     double ltol = 1e-3;
@@ -522,6 +524,9 @@ struct spectral_plan_s {
         dfree(qacc); dfree(tmp32);
         for (auto &p : r32) dfree(p);
         dfree(sQ); dfree(sf1); dfree(d_fh); dfree(d_Qh);
+        for (cudaEvent_t e : host_events) cudaEventDestroy(e);
+        if (copy_in) cudaStreamDestroy(copy_in);
+        if (copy_out) cudaStreamDestroy(copy_out);
         dfree(lq); dfree(d_lerr);
         dfree(d_x); dfree(d_dx); dfree(fconv); dfree(f1); dfree(ftmp); dfree(f_l); dfree(f_r);
         if (graph_exec) cudaGraphExecDestroy(graph_exec);
@@ -1044,10 +1049,39 @@ int spectral_computeQ_host(spectral_plan *p, const double *f_host, double *Q_hos
         SBTE_TRY(dalloc(&p->d_Qh, (size_t)B * p->n3));
         p->caphost = B;
     }
-    const size_t bytes = sizeof(double) * (size_t)B * p->n3;
-    SBTE_CUDA(cudaMemcpyAsync(p->d_fh, f_host, bytes, cudaMemcpyHostToDevice, p->stream));
-    SBTE_TRY(computeQ_dev(p, p->d_fh, p->d_Qh, B, flags, p->stream));
-    SBTE_CUDA(cudaMemcpyAsync(Q_host, p->d_Qh, bytes, cudaMemcpyDeviceToHost, p->stream));
+    // Chunks of whole instance groups: the copy of chunk c + 1 in and of chunk
+    // c - 1 out overlap the compute of chunk c.  Every group streams W once
+    // whichever chunk it sits in, so chunking adds no work.
+    if (!p->copy_in) {
+        SBTE_CUDA(cudaStreamCreateWithFlags(&p->copy_in, cudaStreamNonBlocking));
+        SBTE_CUDA(cudaStreamCreateWithFlags(&p->copy_out, cudaStreamNonBlocking));
+    }
+    const int bg = (flags & SPECTRAL_FP32) ? std::max(32, p->tune.bg) : 8;
+    int chunk = B;
+    if (B >= 4 * bg) chunk = std::max(bg, (B / 8) / bg * bg);
+    const int nch = (B + chunk - 1) / chunk;
+    while ((int)p->host_events.size() < 2 * nch) {
+        cudaEvent_t e;
+        SBTE_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        p->host_events.push_back(e);
+    }
+    const long long n3 = p->n3;
+    for (int c = 0; c < nch; c++) {
+        const long long b0 = (long long)c * chunk;
+        const int nb = (int)std::min<long long>(chunk, B - b0);
+        const size_t bytes = sizeof(double) * (size_t)nb * n3;
+        cudaEvent_t in = p->host_events[2 * c], done = p->host_events[2 * c + 1];
+        SBTE_CUDA(cudaMemcpyAsync(p->d_fh + b0 * n3, f_host + b0 * n3, bytes,
+                                  cudaMemcpyHostToDevice, p->copy_in));
+        SBTE_CUDA(cudaEventRecord(in, p->copy_in));
+        SBTE_CUDA(cudaStreamWaitEvent(p->stream, in, 0));
+        SBTE_TRY(computeQ_dev(p, p->d_fh + b0 * n3, p->d_Qh + b0 * n3, nb, flags, p->stream));
+        SBTE_CUDA(cudaEventRecord(done, p->stream));
+        SBTE_CUDA(cudaStreamWaitEvent(p->copy_out, done, 0));
+        SBTE_CUDA(cudaMemcpyAsync(Q_host + b0 * n3, p->d_Qh + b0 * n3, bytes,
+                                  cudaMemcpyDeviceToHost, p->copy_out));
+    }
+    SBTE_CUDA(cudaStreamSynchronize(p->copy_out));
     SBTE_CUDA(cudaStreamSynchronize(p->stream));
     return kOk;
 }

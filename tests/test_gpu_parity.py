@@ -366,3 +366,25 @@ def test_config1_bkw_tracks_analytic_solution(gpu):
     assert change > 0.2
     assert err < 5e-3 and err < 0.05 * change, (err, change)
     plan.close()
+
+
+@pytest.mark.parametrize("B,flags", [(5, 4), (70, 5), (300, 5), (300, 4)])
+def test_computeQ_host_equals_device(gpu, oracle, B, flags):
+    """spectral_computeQ_host (chunked so that host copies overlap compute)
+    returns the device path's result bit for bit, for single-chunk and
+    multi-chunk batches with a ragged last chunk; flags 4 = FP64 + conserve,
+    5 = FP32 + conserve."""
+    import torch
+    N, L_v = 8, 5.0
+    g = oracle.Grid(N, L_v, "0d")
+    plan = gpu.Plan(N, L_v, g.v, g.zeta, B)
+    plan.generate_weights_iso(1.0)
+    rng = np.random.default_rng(B)
+    f = np.stack([oracle.init_bkw(g) * (1 + 0.05 * rng.uniform(-1, 1, g.n3)) for _ in range(B)])
+    Qh = plan.computeQ_host(f, flags)
+    fd = torch.from_numpy(f).cuda()
+    Qd = torch.empty_like(fd)
+    plan.computeQ_device(fd, Qd, B, flags)
+    torch.cuda.synchronize()
+    assert np.array_equal(Qh, Qd.cpu().numpy())
+    plan.close()
