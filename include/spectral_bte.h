@@ -296,6 +296,10 @@ int spectral_fno_create(spectral_fno **net, int N, int width, int modes,
                         int layers, int hidden, int kind, int precision,
                         unsigned long long seed);
 int spectral_fno_precision(spectral_fno *net);
+/* At N = 32, width 64, 12 modes the last inverse transform of each layer runs
+   fused with its channel mix (on by default); 0 selects the unfused kernels,
+   which every shape uses otherwise. */
+int spectral_fno_set_fused(spectral_fno *net, int on);
 int spectral_fno_destroy(spectral_fno *net);
 long long spectral_fno_num_params(spectral_fno *net);
 int spectral_fno_num_classes(spectral_fno *net);

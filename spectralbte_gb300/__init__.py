@@ -150,6 +150,7 @@ def lib() -> C.CDLL:
         # learned operator
         "spectral_fno_create": (i, [pp, i, i, i, i, i, i, i, C.c_ulonglong]),
         "spectral_fno_precision": (i, [v]),
+        "spectral_fno_set_fused": (i, [v, i]),
         "spectral_fno_destroy": (i, [v]),
         "spectral_fno_num_params": (C.c_longlong, [v]),
         "spectral_fno_num_classes": (i, [v]),
@@ -537,6 +538,9 @@ class FourierOperator:
     @output_scale.setter
     def output_scale(self, sigma: float):
         _check(self.L.spectral_fno_set_output_scale(self.h, float(sigma)), "fno_set_output_scale")
+
+    def set_fused(self, on: bool):
+        _check(self.L.spectral_fno_set_fused(self.h, 1 if on else 0), "fno_set_fused")
 
     def set_loss_floor(self, eps: float):
         _check(self.L.spectral_fno_set_loss_floor(self.h, float(eps)), "fno_set_loss_floor")

@@ -27,6 +27,7 @@
 // contiguous stream (fno_gemm.cuh), and every weight gradient a gemm_nt.
 #include "common.cuh"
 #include "fno.h"
+#include "fno_fused.cuh"
 #include "fno_gemm.cuh"
 #include "kernels.h"
 #include "../../include/spectral_bte.h"
@@ -558,6 +559,7 @@ struct spectral_fno_s {
     int device = 0;
     int N = 0, C = 0, Km = 0, L = 0, Hd = 0, ncls = 0;
     int kind = 0;  // 0: GELU layers and readout; 1: linear layers, bilinear readout
+    bool fused = true;  // fused last inverse pass + channel mix where the shape allows
     long long P = 0;
     long long nparams = 0;
     long long oP = 0, obP = 0, oW[8] = {}, ob[8] = {}, oR[8] = {}, oQ1 = 0, oc1 = 0, oq2 = 0,
@@ -773,7 +775,7 @@ int mode_mix(spectral_fno_s *n, const float *R, bool tr, const uint16_t *in, uin
 // or added, times alpha, into the FP32 out32 (the backward pass).
 template <typename E>
 int spectral_inv(spectral_fno_s *n, const uint16_t *in, uint16_t *out16, float *out32,
-                 float alpha, int Bp, cudaStream_t st)
+                 float alpha, int Bp, cudaStream_t st, bool stop_at_u2 = false)
 {
     const long long N = n->N, Km = n->Km, CB = (long long)n->C * Bp;
     const float *G = n->G;
@@ -795,6 +797,7 @@ int spectral_inv(spectral_fno_s *n, const uint16_t *in, uint16_t *out16, float *
         set_ext(a, ext.G, ext.t2, ext.t1);
         FNO_LAUNCH((launch_sa<E, 32, 128, 1, 4, true, true, kEpiCplxBF16>(a, st)));
     }
+    if (stop_at_u2) return kOk;
     {  // axis k, real part
         SaArgs a = sa_base(G, Km, 1, N * Km, (int)N, (int)Km);
         a.B = sv(n->U2, CB, CB, 2 * Km * CB, Km * CB);
@@ -807,6 +810,43 @@ int spectral_inv(spectral_fno_s *n, const uint16_t *in, uint16_t *out16, float *
         else
             FNO_LAUNCH((launch_sa<E, 32, 128, 1, 4, true, true, kEpiBF16>(a, st)));
     }
+    return kOk;
+}
+
+bool fused_shape(const spectral_fno_s *n)
+{
+    return n->fused && n->N == 32 && n->C == 64 && n->Km == 12;
+}
+
+// Last inverse axis pass + channel mix + bias + activation of layer l
+// (fno_fused.cuh), from U2 and the layer input to the layer output.
+template <typename E>
+int fused_layer(spectral_fno_s *n, int l, const uint16_t *hin, uint16_t *hout, float *zst,
+                bool act, int Bp, cudaStream_t st)
+{
+    using L = FusedLayout<E, 32, 64, 12>;
+    if (Bp % 8 || n->N != 32 || n->C != 64 || n->Km != 12) {
+        set_error(kErrArg, "fused layer: shape N=%d C=%d Km=%d Bp=%d", n->N, n->C, n->Km, Bp);
+        return kErrArg;
+    }
+    auto kern = fused_layer_kernel<E, 32, 64, 12>;
+    FNO_LAUNCH(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)L::bytes));
+    FusedArgs a;
+    a.U2 = n->U2;
+    a.H = hin;
+    a.Hout = hout;
+    a.zst = zst;
+    a.G = n->G;
+    a.W = n->params + n->oW[l];
+    a.bias = n->params + n->ob[l];
+    a.act = act ? 1 : 0;
+    a.Bp = Bp;
+    const long long items = 32LL * 32 * (Bp / 8);
+    const int grid = (int)std::min<long long>(items, 152LL * 2);
+    kern<<<grid, L::NTH, L::bytes, st>>>(a);
+    add_launches(1);
+    FNO_LAUNCH(cudaGetLastError());
     return kOk;
 }
 
@@ -830,6 +870,13 @@ int forward(spectral_fno_s *n, const T *f, int B, int Bp, bool train, cudaStream
         uint16_t *xl = train ? n->X[l] : n->X[0];
         FNO_TRY(spectral_fwd<E>(n, hin, xl, false, Bp, st));
         FNO_TRY(mode_mix<E>(n, prm + n->oR[l], false, xl, n->Y, Bp, st));
+        const bool gelu = n->kind == 0 && l < n->L - 1;
+        if (fused_shape(n)) {
+            FNO_TRY(spectral_inv<E>(n, n->Y, nullptr, nullptr, 1.f, Bp, st, true));
+            FNO_TRY(fused_layer<E>(n, l, hin, hout, (train && gelu) ? n->Z[l] : nullptr, gelu,
+                                   Bp, st));
+            continue;
+        }
         FNO_TRY(spectral_inv<E>(n, n->Y, n->S, nullptr, 1.f, Bp, st));
         SaArgs a = sa_base(prm + n->oW[l], C, 1, 0, (int)C, (int)C);
         a.B = sv(hin, Bp, Bp, C * Bp);
@@ -837,7 +884,6 @@ int forward(spectral_fno_s *n, const T *f, int B, int Bp, bool train, cudaStream
         a.Nn = P * Bp;
         a.bias = prm + n->ob[l];
         a.addend = n->S;
-        const bool gelu = n->kind == 0 && l < n->L - 1;
         a.zst = (train && gelu) ? n->Z[l] : nullptr;
         a.hout = hout;
         a.act = gelu ? 1 : 0;
@@ -1173,6 +1219,16 @@ long long spectral_fno_num_params(spectral_fno *n) { return n ? n->nparams : 0; 
 int spectral_fno_num_classes(spectral_fno *n) { return n ? n->ncls : 0; }
 
 int spectral_fno_precision(spectral_fno *n) { return n ? n->prec : -1; }
+
+int spectral_fno_set_fused(spectral_fno *n, int on)
+{
+    if (!n) {
+        set_error(kErrArg, "spectral_fno_set_fused: null handle");
+        return kErrArg;
+    }
+    n->fused = on != 0;
+    return kOk;
+}
 
 int spectral_fno_get_params(spectral_fno *n, float *host)
 {
