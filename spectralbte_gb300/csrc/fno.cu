@@ -716,12 +716,12 @@ void set_ext(SaArgs &a, long long eA, long long eB, long long eC)
 // stay far from the 16-bit subnormal range: out is then N^2 times F3 in.
 template <typename E>
 int spectral_fwd(spectral_fno_s *n, const uint16_t *in, uint16_t *out, bool bwd, int Bp,
-                 cudaStream_t st)
+                 cudaStream_t st, bool t1_ready = false)
 {
     const long long N = n->N, Km = n->Km, CB = (long long)n->C * Bp;
     const float *F = n->F, *F23 = bwd ? n->Fu : n->F;
     const Ext ext(n, Bp);
-    {  // axis k, real input
+    if (!t1_ready) {  // axis k, real input (T1 may come from the previous fused layer)
         SaArgs a = sa_base(F, N, 1, Km * N, (int)Km, (int)N);
         a.B = sv(in, CB, CB, N * CB);
         a.C = sv(n->T1, CB, CB, 2 * Km * CB, Km * CB);
@@ -822,7 +822,7 @@ bool fused_shape(const spectral_fno_s *n)
 // (fno_fused.cuh), from U2 and the layer input to the layer output.
 template <typename E>
 int fused_layer(spectral_fno_s *n, int l, const uint16_t *hin, uint16_t *hout, float *zst,
-                bool act, int Bp, cudaStream_t st)
+                bool act, bool t1_next, int Bp, cudaStream_t st)
 {
     using L = FusedLayout<E, 32, 64, 12>;
     if (Bp % 8 || n->N != 32 || n->C != 64 || n->Km != 12) {
@@ -838,6 +838,8 @@ int fused_layer(spectral_fno_s *n, int l, const uint16_t *hin, uint16_t *hout, f
     a.Hout = hout;
     a.zst = zst;
     a.G = n->G;
+    a.F = n->F;
+    a.T1 = t1_next ? n->T1 : nullptr;
     a.W = n->params + n->oW[l];
     a.bias = n->params + n->ob[l];
     a.act = act ? 1 : 0;
@@ -865,16 +867,20 @@ int forward(spectral_fno_s *n, const T *f, int B, int Bp, bool train, cudaStream
                                                  (int)C, Bp);
     add_launches(3);
     FNO_LAUNCH(cudaGetLastError());
+    bool t1_ready = false;  // T1 of this layer written by the previous fused layer
     for (int l = 0; l < n->L; l++) {
         uint16_t *hin = Hbuf(n, l, train), *hout = Hbuf(n, l + 1, train);
         uint16_t *xl = train ? n->X[l] : n->X[0];
-        FNO_TRY(spectral_fwd<E>(n, hin, xl, false, Bp, st));
+        FNO_TRY(spectral_fwd<E>(n, hin, xl, false, Bp, st, t1_ready));
+        t1_ready = false;
         FNO_TRY(mode_mix<E>(n, prm + n->oR[l], false, xl, n->Y, Bp, st));
         const bool gelu = n->kind == 0 && l < n->L - 1;
         if (fused_shape(n)) {
             FNO_TRY(spectral_inv<E>(n, n->Y, nullptr, nullptr, 1.f, Bp, st, true));
+            const bool t1_next = l < n->L - 1;
             FNO_TRY(fused_layer<E>(n, l, hin, hout, (train && gelu) ? n->Z[l] : nullptr, gelu,
-                                   Bp, st));
+                                   t1_next, Bp, st));
+            t1_ready = t1_next;
             continue;
         }
         FNO_TRY(spectral_inv<E>(n, n->Y, n->S, nullptr, 1.f, Bp, st));
