@@ -328,6 +328,24 @@ def run_learned(args, plan, fd, Qd, B, flags, peaks):
     torch.cuda.synchronize()
     ms_checked = (time.perf_counter() - t0) * 1e3 / steps
     st = plan.learned_stats()
+    # the same system through the host-buffer C ABI: computeQ_host runs the
+    # batch in chunks, one spot check per batch
+    nchunks = max(1, -(-B // max(64, (B // 4) // 64 * 64))) if B >= 512 else 1
+    plan.set_learned(net, tol=1e-3, check_every=nchunks)
+    f_pin = torch.empty(fd.shape, dtype=torch.float64).pin_memory()
+    f_pin.copy_(fd.cpu())
+    Q_pin = torch.empty_like(f_pin).pin_memory()
+    import ctypes as C
+    dp = C.POINTER(C.c_double)
+    fptr = C.cast(f_pin.numpy().ctypes.data, dp)
+    qptr = C.cast(Q_pin.numpy().ctypes.data, dp)
+    L = sb.lib()
+    assert L.spectral_computeQ_host(plan.h, fptr, qptr, B, lf) == 0  # warm
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        assert L.spectral_computeQ_host(plan.h, fptr, qptr, B, lf) == 0
+    e2e = B * steps / (time.perf_counter() - t0)
+    st_e2e = plan.learned_stats()
     plan.set_learned(None)
     w = learned_work(net.N, net.width, net.modes, net.layers, net.hidden)
     tflops = w["flops"] * B / (ms / 1e3) / 1e12
@@ -345,7 +363,10 @@ def run_learned(args, plan, fd, Qd, B, flags, peaks):
         "accepted": bool(float(rel.max()) <= 1e-3),
         "spot_checked": {"value": B / (ms_checked / 1e3), "unit": UNIT,
                          "calls": st["calls"], "fallbacks": st["fallbacks"],
-                         "last_check_rel_l2": st["last_err"]},
+                         "last_check_rel_l2": st["last_err"],
+                         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 8 * B * net.n3,
+                                 "d2h_bytes_per_step": 8 * B * net.n3,
+                                 "fallbacks": st_e2e["fallbacks"], "calls": st_e2e["calls"]}},
         "roofline": {"bound": "hbm", "achieved": gbs, "peak": float(peaks["hbm_gbs"]),
                      "unit": "GB/s", "frac": gbs / float(peaks["hbm_gbs"]),
                      "algorithmic_bytes_per_eval": w["bytes"],
@@ -672,10 +693,23 @@ def run_ours(args):
                           f"{threads} threads) plus full transforms and projection of one "
                           f"instance, median of 3, extrapolated to one evaluation")}
 
+    # The headline is the FP32+learned system (spot-checked network, plain FP32
+    # fallback) when the network meets the tolerance on every instance of this
+    # workload; otherwise the plain FP32 operator, which always does.
+    fp32_line = {"value": value, "unit": UNIT, "ms_per_step": ms_total / args.steps,
+                 "e2e": e2e_value, "rel_l2_vs_fp64_max": max(rel)}
+    headline = "plain FP32 operator (every instance within rel-L2 1e-3)"
+    h_value, h_e2e, h_ms = value, e2e_value, ms_total / args.steps
+    if learned and learned.get("accepted") and world == 1:
+        sc = learned["spot_checked"]
+        headline = ("FP32+learned: the network with a plain-FP32 spot check each batch "
+                    "(fallback on failure); network rel-L2 <= 1e-3 on every instance here")
+        h_value, h_e2e, h_ms = sc["value"], sc["e2e"]["value"], B / sc["value"] * 1e3
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_total / args.steps,
+        "metric": METRIC, "value": h_value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": h_ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "headline_path": headline, "fp32_plain": fp32_line,
         "dtype": "fp32 (FP64 moments and conservation)", "data": "synthetic",
         "config": {
             "workload": (f"0D hard spheres (lambda=1), N={N}, L_v={L_v}, discontinuous "
@@ -712,7 +746,7 @@ def run_ours(args):
                     "frac": hbm_achieved / float(peaks["hbm_gbs"]),
                     "algorithmic": f"W FP32 {w_bytes:.3e} B per launch"},
         },
-        "e2e": {"value": e2e_value, "unit": UNIT,
+        "e2e": {"value": h_e2e, "unit": UNIT,
                 "h2d_bytes_per_step": 8 * B * n3, "d2h_bytes_per_step": 8 * B * n3},
         "gpu_launches": launches,
         "clocks": clk,
@@ -724,6 +758,13 @@ def run_ours(args):
     }
     if learned is not None:
         line["learned"] = learned
+        if learned.get("accepted") and world == 1:
+            # the headline path's roofline is the network's (HBM-bound, all its kernels);
+            # the convolution's stays with the plain-operator figures
+            line["fp32_plain"]["roofline"] = line["roofline"]
+            lr = dict(learned["roofline"])
+            lr["kernel"] = "learned operator, all kernels of one evaluation (aggregate)"
+            line["roofline"] = lr
     if cpu:
         line["cpu_baseline"] = cpu
     print(json.dumps(line), flush=True)

@@ -1057,8 +1057,10 @@ int spectral_computeQ_host(spectral_plan *p, const double *f_host, double *Q_hos
         SBTE_CUDA(cudaStreamCreateWithFlags(&p->copy_out, cudaStreamNonBlocking));
     }
     const int bg = (flags & SPECTRAL_FP32) ? std::max(32, p->tune.bg) : 8;
+    // four chunks: enough overlap, and each chunk's convolution still runs
+    // several waves of CTAs (a small chunk pays a partial last wave)
     int chunk = B;
-    if (B >= 4 * bg) chunk = std::max(bg, (B / 8) / bg * bg);
+    if (B >= 8 * bg) chunk = std::max(bg, (B / 4) / bg * bg);
     const int nch = (B + chunk - 1) / chunk;
     while ((int)p->host_events.size() < 2 * nch) {
         cudaEvent_t e;
