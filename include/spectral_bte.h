@@ -296,9 +296,11 @@ int spectral_fno_create(spectral_fno **net, int N, int width, int modes,
                         int layers, int hidden, int kind, int precision,
                         unsigned long long seed);
 int spectral_fno_precision(spectral_fno *net);
-/* At N = 32, width 64, 12 modes the last inverse transform of each layer runs
-   fused with its channel mix (on by default); 0 selects the unfused kernels,
-   which every shape uses otherwise. */
+/* At N = 32, width 64, 12 modes, on = 1 runs the last inverse transform of
+   each layer fused with its channel mix and the next layer's first forward
+   axis pass (fewer bytes, fewer launches, the same time on a GB300 as the
+   separate kernels; off by default).  Every other shape uses the separate
+   kernels. */
 int spectral_fno_set_fused(spectral_fno *net, int on);
 int spectral_fno_destroy(spectral_fno *net);
 long long spectral_fno_num_params(spectral_fno *net);

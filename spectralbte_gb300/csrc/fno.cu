@@ -559,7 +559,7 @@ struct spectral_fno_s {
     int device = 0;
     int N = 0, C = 0, Km = 0, L = 0, Hd = 0, ncls = 0;
     int kind = 0;  // 0: GELU layers and readout; 1: linear layers, bilinear readout
-    bool fused = true;  // fused last inverse pass + channel mix where the shape allows
+    bool fused = false;  // fused last inverse pass + channel mix (spectral_fno_set_fused)
     long long P = 0;
     long long nparams = 0;
     long long oP = 0, obP = 0, oW[8] = {}, ob[8] = {}, oR[8] = {}, oQ1 = 0, oc1 = 0, oq2 = 0,
