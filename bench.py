@@ -441,9 +441,10 @@ def run_bkw(args):
     f0 = wl.bkw(v, K0)
     fd = torch.from_numpy(f0[None].copy()).cuda()
     flags = sb.FP64 | sb.MAXPRESERVE
+    kc = sb.kernel_launches()
     plan.capture(0, fd, 1, dt, 1.0, 2, flags)
+    per_step = sb.kernel_launches() - kc   # kernels in the captured step
     torch.cuda.synchronize()
-    k0 = sb.kernel_launches()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     for _ in range(steps):
@@ -460,7 +461,7 @@ def run_bkw(args):
         "higher_is_better": True, "dtype": "f64", "data": "synthetic (BKW, K=0.65)",
         "config": {"workload": "0D Maxwell molecules, N=16, L_v=5, dt=0.01, RK2, maxPreserve",
                    "N": N, "L_v": L_v, "lambda": 0.0},
-        "gpu_launches": sb.kernel_launches() - k0,
+        "gpu_launches": per_step * steps,
         "rel_l2_vs_analytic_bkw": err,
         "rel_l2_change_over_run": float(np.linalg.norm(f0 - fa) / np.linalg.norm(fa))}),
         flush=True)
@@ -499,10 +500,11 @@ def run_1d(args):
 
     def run(flags, nsteps):
         f = torch.from_numpy(f0).cuda()
+        kc = sb.kernel_launches()
         plan.capture(1, f, flags=flags)
+        per_step = sb.kernel_launches() - kc   # kernels in the captured step
         plan.launch()  # warm-up step
         torch.cuda.synchronize()
-        k0 = sb.kernel_launches()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
         for _ in range(nsteps - 1):
@@ -512,7 +514,7 @@ def run_1d(args):
         ms = e0.elapsed_time(e1) / max(1, nsteps - 1)
         mom = torch.empty((nX, 8), dtype=torch.float64, device="cuda")
         plan.moments_device(f[order:order + nX], nX, mom)
-        return f, ms, mom.cpu().numpy(), sb.kernel_launches() - k0
+        return f, ms, mom.cpu().numpy(), per_step * (nsteps - 1)
 
     f, ms, mom, launches = run(sb.FP32, steps)
     rho = mom[:, 0]
