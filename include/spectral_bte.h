@@ -97,9 +97,13 @@ void initialize_weights(int nodes, double *eta, double Lv, double lam,
                         species species_i, species species_j);
 /* weights.h:45 (weights.c:127) */
 /* aniso_weights.c:37 (definition order; aniso_weights.h:1 swaps Lv and lam,
-   and boltz.c:154 calls it in definition order).  Landau kernel (glance = 0)
-   only: loads Weights/N%d_Aniso_L_v%g_lambda%g_Landau.wts or generates the
-   weights on the GPU and writes that file. */
+   and boltz.c:154 calls it in definition order).  Loads
+   Weights/N%d_Aniso_L_v%g_lambda%g_Landau.wts (glance = 0) or
+   Weights/N%d_AnIso_L_v%g_lambda%g_glance%g.wts (glance != 0), or generates
+   the weights on the GPU and writes that file.  The weights are the Landau
+   kernel for every glance, as in the reference: its generator branches on a
+   file-scope glance (aniso_weights.c:31,417) that the parameter shadows and
+   nothing sets. */
 void initialize_weights_AnIso(int nodes, double *zeta, double Lv, double lam,
                               int weightFlag, double **conv_weights,
                               double glance);

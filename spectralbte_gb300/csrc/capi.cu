@@ -1856,28 +1856,29 @@ void initialize_weights(int nodes, double *eta, double Lv, double lam, int weigh
         report("initialize_weights");
 }
 
-// aniso_weights.c:37-150 for the Landau kernel (glance == 0): load
-// Weights/N%d_Aniso_L_v%g_lambda%g_Landau.wts (the name of aniso_weights.c:66,
-// which differs in case from the one weights.c:73 writes) unless weightFlag
-// forces regeneration; otherwise generate on the GPU and write the file.
-// The grazing-collision (Coulomb) weights of glance != 0 need the nested
-// adaptive quadrature of aniso_weights.c:150-350 and are not provided here.
+// aniso_weights.c:37-150: load the cached file unless weightFlag forces
+// regeneration; otherwise generate on the GPU and write the file. The name is
+// Weights/N%d_Aniso_L_v%g_lambda%g_Landau.wts for glance == 0 (aniso_weights.c:66,
+// which differs in case from the one weights.c:73 writes) and
+// Weights/N%d_AnIso_L_v%g_lambda%g_glance%g.wts otherwise (:68).
+// The weights are the Landau kernel for every glance: the generator's branch
+// (aniso_weights.c:417) reads the file-scope `static double glance` (:31), which
+// the parameter of the same name shadows and nothing assigns, so the grazing
+// (Coulomb) quadrature of :150-350 is never reached. The reference built from its
+// own sources gives identical weights for glance 0 and 0.3.
 void initialize_weights_AnIso(int nodes, double *zeta, double Lv, double lam, int weightFlag,
                               double **conv_weights, double glance)
 {
     std::lock_guard<std::mutex> lk(g_mu);
     const long long n3 = (long long)nodes * nodes * nodes;
-    if (glance != 0.0) {
-        set_error(kErrUnsupported,
-                  "initialize_weights_AnIso: grazing-collision weights (glance=%g) are not "
-                  "generated by this library; only the Landau kernel (glance=0) is", glance);
-        report("initialize_weights_AnIso");
-        return;
-    }
     for (long long i = 0; i < n3; i++)  // aniso_weights.c:60-62
         conv_weights[i] = (double *)malloc(sizeof(double) * n3);
     char name[256];
-    snprintf(name, sizeof(name), "Weights/N%d_Aniso_L_v%g_lambda%g_Landau.wts", nodes, Lv, lam);
+    if (glance == 0.0)
+        snprintf(name, sizeof(name), "Weights/N%d_Aniso_L_v%g_lambda%g_Landau.wts", nodes, Lv, lam);
+    else
+        snprintf(name, sizeof(name), "Weights/N%d_AnIso_L_v%g_lambda%g_glance%g.wts", nodes, Lv,
+                 lam, glance);
     FILE *fid = nullptr;
     cudaStream_t st = g_coll.plan ? g_coll.plan->stream : nullptr;
     if (weightFlag == 0 && (fid = fopen(name, "r"))) {

@@ -151,18 +151,23 @@ def landau(ref_dir="/root/reference"):
                                            C.POINTER(_dp), C.c_double]
     out = {}
     cwd = os.getcwd()
-    for name, N, L_v, lam in (("n4", 4, 4.0, 0.0), ("n5", 5, 3.0, 1.0)):
+    # g4 passes a non-zero glance: the reference then writes the *_glance*.wts
+    # name, and its generator still takes the Landau branch.
+    for name, N, L_v, lam, glance in (("n4", 4, 4.0, 0.0, 0.0), ("n5", 5, 3.0, 1.0, 0.0),
+                                      ("g4", 4, 4.0, 0.0, 0.3)):
         g = po.Grid(N, L_v, "0d")
         rows = (_dp * g.n3)()
         with tempfile.TemporaryDirectory() as d:
             os.makedirs(os.path.join(d, "Weights"))
             os.chdir(d)
             try:
-                L.initialize_weights_AnIso(N, po._p(g.zeta), L_v, lam, 1, rows, 0.0)
+                L.initialize_weights_AnIso(N, po._p(g.zeta), L_v, lam, 1, rows, glance)
             finally:
                 os.chdir(cwd)
+            (fname,) = os.listdir(os.path.join(d, "Weights"))
         W = np.stack([np.ctypeslib.as_array(rows[i], shape=(g.n3,)).copy() for i in range(g.n3)])
-        out[f"{name}_meta"] = np.array([N, L_v, lam])
+        out[f"{name}_meta"] = np.array([N, L_v, lam, glance])
+        out[f"{name}_file"] = np.array("Weights/" + fname)
         out[f"{name}_zeta"] = g.zeta.copy()
         out[f"{name}_W"] = W
         print("landau", name, W.shape, np.abs(W).max())

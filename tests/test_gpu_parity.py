@@ -313,7 +313,7 @@ def test_landau_weights_on_device(gpu, ref_api, tmp_path, monkeypatch):
     from conftest import GOLDEN
     d = np.load(os.path.join(GOLDEN, "golden_landau.npz"))
     for name in ("n4", "n5"):
-        N, L_v, lam = d[f"{name}_meta"]
+        N, L_v, lam, _glance = d[f"{name}_meta"]
         N = int(N)
         zeta, ref = d[f"{name}_zeta"], d[f"{name}_W"]
         v, _ = gpu.grid_0d(N, L_v)
@@ -324,19 +324,23 @@ def test_landau_weights_on_device(gpu, ref_api, tmp_path, monkeypatch):
         plan.close()
     monkeypatch.chdir(tmp_path)
     os.makedirs("Weights")
-    N, L_v, lam = (float(x) for x in d["n4_meta"])
-    N = int(N)
-    tables = ref_api.alloc_weights(N, 1)
-    ref_api.initialize_weights_AnIso(N, d["n4_zeta"], L_v, lam, 0, tables[0])
-    fname = "Weights/N4_Aniso_L_v4_lambda0_Landau.wts"
-    assert os.path.getsize(fname) == 8 * 64 * 64
-    Wf = np.fromfile(fname).reshape(64, 64)
-    assert np.abs(Wf - d["n4_W"]).max() <= 1e-12 * np.abs(d["n4_W"]).max()
-    tables2 = ref_api.alloc_weights(N, 1)
-    ref_api.initialize_weights_AnIso(N, d["n4_zeta"], L_v, lam, 0, tables2[0])  # loads the file
-    assert np.array_equal(ref_api.table_to_numpy(tables2[0], N), Wf)
-    ref_api.dealloc_weights(N, tables[0])
-    ref_api.dealloc_weights(N, tables2[0])
+    for name in ("n4", "g4"):  # g4: glance 0.3, same weights under another name
+        N, L_v, lam, glance = (float(x) for x in d[f"{name}_meta"])
+        N = int(N)
+        tables = ref_api.alloc_weights(N, 1)
+        ref_api.initialize_weights_AnIso(N, d[f"{name}_zeta"], L_v, lam, 0, tables[0], glance)
+        fname = str(d[f"{name}_file"])
+        assert os.path.getsize(fname) == 8 * 64 * 64
+        Wf = np.fromfile(fname).reshape(64, 64)
+        assert np.abs(Wf - d[f"{name}_W"]).max() <= 1e-12 * np.abs(d[f"{name}_W"]).max()
+        tables2 = ref_api.alloc_weights(N, 1)
+        ref_api.initialize_weights_AnIso(N, d[f"{name}_zeta"], L_v, lam, 0, tables2[0],
+                                         glance)  # loads the file
+        assert np.array_equal(ref_api.table_to_numpy(tables2[0], N), Wf)
+        ref_api.dealloc_weights(N, tables[0])
+        ref_api.dealloc_weights(N, tables2[0])
+    assert sorted(os.listdir("Weights")) == sorted(
+        os.path.basename(str(d[k])) for k in ("n4_file", "g4_file"))
 
 
 def test_config1_bkw_tracks_analytic_solution(gpu):

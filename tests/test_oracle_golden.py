@@ -140,8 +140,21 @@ def test_landau_weights_match_reference(oracle):
     import os
     from conftest import GOLDEN
     d = np.load(os.path.join(GOLDEN, "golden_landau.npz"))
-    for name in ("n4", "n5"):
-        N, L_v, lam = d[f"{name}_meta"]
+    for name in ("n4", "n5", "g4"):
+        N, L_v, lam, _glance = d[f"{name}_meta"]
         W = oracle.weights_landau(int(N), d[f"{name}_zeta"], L_v, lam)
         ref = d[f"{name}_W"]
         assert np.abs(W - ref).max() <= 1e-13 * np.abs(ref).max(), name
+
+
+def test_landau_weights_ignore_glance_in_reference():
+    """The reference's generator branches on a file-scope glance that its
+    parameter shadows (aniso_weights.c:31,37,417), so glance = 0.3 gives the
+    Landau weights under the *_glance0.3.wts name (:68)."""
+    import os
+    from conftest import GOLDEN
+    d = np.load(os.path.join(GOLDEN, "golden_landau.npz"))
+    assert d["g4_meta"][3] == 0.3
+    assert np.array_equal(d["g4_W"], d["n4_W"])
+    assert str(d["g4_file"]) == "Weights/N4_AnIso_L_v4_lambda0_glance0.3.wts"
+    assert str(d["n4_file"]) == "Weights/N4_Aniso_L_v4_lambda0_Landau.wts"
