@@ -54,13 +54,18 @@ NCU_TRAFFIC = {
     3: {"bytes": 3.135992e9 + 75.185664e6, "N": 24, "B": 128, "bg": 32,
         "kernel": "conv_ws_kernel"},
 }
+# The same kernel in its symmetric (row-pair) form streams the partner-summed
+# table, about half of W; no capture of it yet, so its traffic is left out.
+NCU_TRAFFIC_SYM = {}
 KERNEL_NAME = {1: "conv_f32_kernel", 2: "conv_ws_kernel", 3: "conv_ws_kernel",
                4: "conv_x4_kernel"}
 
 
-def scaled_traffic(variant: int, N: int, B: int, bg: int):
+def scaled_traffic(variant: int, N: int, B: int, bg: int, sym: bool = False):
     """Per-launch DRAM bytes at (N, B, bg) from the capture of the same kernel."""
-    cap = NCU_TRAFFIC.get(1 if variant == 1 else 3)
+    cap = (NCU_TRAFFIC_SYM if sym else NCU_TRAFFIC).get(1 if variant == 1 else 3)
+    if cap is None:
+        return None, None
     groups = -(-B // bg)
     cap_groups = -(-cap["B"] // cap["bg"])
     return cap["bytes"] / cap_groups * groups * (N / cap["N"]) ** 6, cap
@@ -591,12 +596,14 @@ def run_ours(args):
     fd = torch.from_numpy(f_host).cuda()
     Qd = torch.empty_like(fd)
     flags = sb.FP32 | sb.CONSERVE
+    plan.set_symmetric(not args.no_sym)
     if args.tuning:
         variant, bg, zs, stages, flush = (int(x) for x in args.tuning.split(","))
         plan.set_tuning(bg, stages, flush, variant=variant, zs=zs)
         tuned = (variant, bg, zs, stages, flush)
     else:
         tuned = plan.autotune(B, sb.FP32)
+    sym = (not args.no_sym) and tuned[0] in (2, 3)
 
     for _ in range(args.warmup):
         plan.computeQ_device(fd, Qd, B, flags)
@@ -673,13 +680,23 @@ def run_ours(args):
     if rank != 0:
         return 0
     conv_avg_s = conv_ms / max(conv_n, 1) / 1e3
-    flops = 10.0 * float(n3) ** 2 * B        # collisions.c:162-163, 10 flops/term
+    flops_ref = 10.0 * float(n3) ** 2 * B    # collisions.c:162-163, 10 flops/term
+    if sym:
+        # row-pair form: (N^6 + N^4)/2 terms per instance, 10 flops each
+        flops = 5.0 * (float(N) ** 6 + float(N) ** 4) * B
+        w_bytes = 4.0 * N ** 2 * (N ** 4 + N ** 2) / 2   # the partner-summed table
+        algo = (f"5*(N^6+N^4)*B flop per launch = {flops:.3e} (row-pair form: each pair of "
+                f"xi-rows with the same product of transforms runs once; the reference's count "
+                f"10*N^6*B = {flops_ref:.3e} is the 'effective' figure)")
+    else:
+        flops = flops_ref
+        w_bytes = 4.0 * float(n3) ** 2           # one FP32 W pass per launch
+        algo = f"10*N^6*B flop per launch = {flops:.3e}"
     achieved = flops / conv_avg_s / 1e12
     sm_max = float(peaks.get("sm_max_mhz", 2070.0))
     fp32_nominal = N_SM * FP32_LANES * 2 * sm_max * 1e6 / 1e12
     fp32_peak = fma_rate
-    w_bytes = 4.0 * float(n3) ** 2           # one FP32 W pass per launch
-    traffic, tcap = scaled_traffic(tuned[0], N, B, tuned[1])
+    traffic, tcap = scaled_traffic(tuned[0], N, B, tuned[1], sym)
     hbm_achieved = w_bytes / conv_avg_s / 1e9
 
     cpu = None
@@ -718,9 +735,10 @@ def run_ours(args):
                          f"two-Maxwellian +-5% jitter, {B} instances per GPU"),
             "N": N, "L_v": L_v, "lambda": lam, "batch_per_gpu": B,
             "parallelism": f"{world} independent GPU(s), instances sharded",
-            "l2": "inputs larger than L2 (W FP32 4.3 GB, f 256 MB at B=1024)",
+            "l2": (f"inputs larger than L2 (weight table {w_bytes / 1e9:.2f} GB, f "
+                   f"{8 * B * n3 / 1e6:.0f} MB)"),
             "tuning": {"variant": tuned[0], "bg": tuned[1], "zs": tuned[2],
-                       "stages": tuned[3], "flush": tuned[4]},
+                       "stages": tuned[3], "flush": tuned[4], "symmetric": sym},
 
         },
         "roofline": {
@@ -737,13 +755,15 @@ def run_ours(args):
             "frac_of_nominal": achieved / fp32_nominal,
             "nominal_source": (f"{N_SM} SMs x {FP32_LANES} lanes x 2 flop x {sm_max:.0f} MHz "
                                f"({peak_src} sm_max_mhz)"),
-            "algorithmic": f"10*N^6*B flop per launch = {flops:.3e}",
+            "algorithmic": algo,
+            "effective_tflops": flops_ref / conv_avg_s / 1e12,
             "launch_ms": conv_avg_s * 1e3,
             "traffic": traffic,
-            "traffic_note": (f"bytes per launch, scaled by N^6 x instance groups from the ncu "
-                             f"capture of {tcap['kernel']} at N=24, B=128, bg={tcap['bg']}; W is "
-                             f"re-read once per instance group of {tuned[1]}, from HBM, far "
-                             f"below the HBM peak"),
+            "traffic_note": ((f"bytes per launch, scaled by N^6 x instance groups from the ncu "
+                              f"capture of {tcap['kernel']} at N=24, B=128, bg={tcap['bg']}; W "
+                              f"is re-read once per instance group of {tuned[1]}, from HBM, far "
+                              f"below the HBM peak") if tcap else
+                             "no ncu capture of this form yet"),
             "hbm": {"achieved": hbm_achieved, "peak": float(peaks["hbm_gbs"]), "unit": "GB/s",
                     "frac": hbm_achieved / float(peaks["hbm_gbs"]),
                     "algorithmic": f"W FP32 {w_bytes:.3e} B per launch"},
@@ -796,6 +816,8 @@ def main():
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--tuning", default="",
                     help="variant,bg,zs,stages,flush of the FP32 convolution (default: autotune)")
+    ap.add_argument("--no-sym", action="store_true",
+                    help="run every xi-row of the FP32 convolution (no row-pair form)")
     args = ap.parse_args()
     if args.workload == "uneven" and args.impl != "reference":
         return run_uneven(args)

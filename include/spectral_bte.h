@@ -237,6 +237,14 @@ int spectral_plan_set_tuning(spectral_plan *plan, int variant, int bg, int zs,
                              int stages, int flush);
 int spectral_plan_autotune(spectral_plan *plan, int B, int flags,
                            int *chosen);
+/* Symmetric form of the warp-specialised FP32 convolution (variants 2, 3;
+   on by default).  Every FP32 call here has g = f, and for a fixed zeta the
+   xi-rows r and (zeta + N/2 - r) mod N see the same product of transforms,
+   so one pass over a row pair with the two weight tiles summed (in FP64,
+   one rounding) replaces two: (N^2 + F)/2 of the N^2 rows per zeta-row
+   (F = 0 or 4 self-paired rows).  The same sum in another order; off runs
+   every row with the plain tiled weights. */
+int spectral_plan_set_symmetric(spectral_plan *plan, int on);
 
 /* Device status word of the last call: bit 0 = a bounded device wait gave
    up, bit 1 = non-finite output.  Cleared by the read. */

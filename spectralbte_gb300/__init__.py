@@ -135,6 +135,7 @@ def lib() -> C.CDLL:
         "spectral_step_device": (i, [v, v, i, d, d, i, i, v]),
         "spectral_plan_set_tuning": (i, [v, i, i, i, i, i]),
         "spectral_plan_autotune": (i, [v, i, i, C.POINTER(C.c_int)]),
+        "spectral_plan_set_symmetric": (i, [v, i]),
         "spectral_plan_status": (i, [v, C.POINTER(C.c_uint)]),
         "spectral_plan_sync": (i, [v]),
         "spectral_plan_set_profiling": (i, [v, i]),
@@ -416,6 +417,10 @@ class Plan:
                    zs: int = 0):
         _check(self.L.spectral_plan_set_tuning(self.h, variant, bg, zs, stages, flush),
                "set_tuning")
+
+    def set_symmetric(self, on: bool):
+        """Symmetric (row-pair) form of the FP32 convolution, variants 2, 3."""
+        _check(self.L.spectral_plan_set_symmetric(self.h, int(bool(on))), "set_symmetric")
 
     def autotune(self, B: int, flags: int = FP32) -> tuple:
         """(variant, bg, zs, stages, flush) of the fastest FP32 shape."""

@@ -260,11 +260,13 @@ struct WeightsDev {
     double *w64 = nullptr;   // row-major [N^3][N^3]
     float *w32 = nullptr;    // tiled FP32 (built on first FP32 use)
     float2 *w32x2 = nullptr; // tiled (w, w) pairs (built on first variant-4 use)
+    float *wsym = nullptr;   // partner-summed FP32 tiles (built on first symmetric use)
     void release()
     {
         dfree(w64);
         dfree(w32);
         dfree(w32x2);
+        dfree(wsym);
         N = 0;
     }
 };
@@ -281,6 +283,7 @@ static int upload_weights(WeightsDev &wd, int N, const double *flat,
     }
     dfree(wd.w32);
     dfree(wd.w32x2);
+    dfree(wd.wsym);
     if (flat) {
         SBTE_CUDA(cudaMemcpyAsync(wd.w64, flat, sizeof(double) * n3 * n3,
                                   flat_on_device ? cudaMemcpyDeviceToDevice
@@ -321,6 +324,16 @@ static int ensure_w32(WeightsDev &wd, cudaStream_t st)
     return kOk;
 }
 
+static int ensure_wsym(WeightsDev &wd, cudaStream_t st)
+{
+    if (wd.wsym) return kOk;
+    const long long nn = (long long)wd.N * wd.N;
+    SBTE_TRY(dalloc(&wd.wsym, (size_t)(nn * sym_max_slots(wd.N) * nn)));
+    SBTE_LAUNCH(weights_to_sym_f32(wd.w64, wd.wsym, wd.N, st), 1);
+    SBTE_CUDA(cudaStreamSynchronize(st));
+    return kOk;
+}
+
 static int ensure_w32x2(WeightsDev &wd, cudaStream_t st)
 {
     if (wd.w32x2) return kOk;
@@ -350,6 +363,7 @@ static int generate_landau_device(WeightsDev &wd, int N, double L_v, double lamb
     }
     dfree(wd.w32);
     dfree(wd.w32x2);
+    dfree(wd.wsym);
     std::vector<double> gx, gw;
     gl_nodes(64, gx, gw);  // gsl_integration_glfixed_table_alloc(64), aniso_weights.c:44
     double *d_zeta = nullptr, *d_gx = nullptr, *d_gw = nullptr;
@@ -395,6 +409,7 @@ static int generate_iso_device(WeightsDev &wd, const IsoWeightSpec &s,
     }
     dfree(wd.w32);
     dfree(wd.w32x2);
+    dfree(wd.wsym);
     WeightParams wp;
     wp.N = N;
     wp.L_v = s.L_v;
@@ -465,6 +480,7 @@ struct spectral_plan_s {
     bool cons_ready = false;
     double mom_mass = 1.0, mom_KB = 1.0;
     ConvF32Config tune{64, 3, 16};
+    int sym = 1;  // symmetric convolution form for variants 2, 3 (g = f)
     unsigned int *d_status = nullptr;
     // FP64 scratch: capacity cap64 instances
     int cap64 = 0;
@@ -729,13 +745,15 @@ static int q_fp64(spectral_plan_s *p, const WeightsDev &W, const double *fdev,
 
 // Q for B instances with the FP32 batched convolution and FP32 transforms
 // (f = g).  Moments, Maxwellian split and conservation stay FP64.
-static int q_fp32(spectral_plan_s *p, const double *fdev, double *Qdev, int B,
-                  bool maxpreserve, cudaStream_t st)
+// The convolution configuration a call runs with: the plan's tuning, or,
+// where the two-pair form does not fit in shared memory, a narrower instance
+// group; plus the symmetric form where the variant has it and the plan
+// allows it.  Builds the weight table that configuration reads.
+static int resolve_f32(spectral_plan_s *p, bool maxpreserve, ConvF32Config &cfg,
+                       const float *&Wt, cudaStream_t st)
 {
-    SBTE_TRY(ensure32(p, B));
-    SBTE_TRY(ensure_w32(p->W, st));
     const int N = p->N;
-    ConvF32Config cfg = p->tune;
+    cfg = p->tune;
     if (!conv_f32_supported(N, cfg, maxpreserve)) {
         // the two-pair form stages twice the rows: fall back to a narrower
         // instance group that fits in shared memory
@@ -752,13 +770,34 @@ static int q_fp32(spectral_plan_s *p, const double *fdev, double *Qdev, int B,
             return kErrUnsupported;
         }
     }
+    cfg.sym = (p->sym && (cfg.variant == 2 || cfg.variant == 3)) ? 1 : 0;
+    Wt = nullptr;
+    if (cfg.variant == 4) {
+        SBTE_TRY(ensure_w32x2(p->W, st));
+    } else if (cfg.sym) {
+        SBTE_TRY(ensure_wsym(p->W, st));
+        Wt = p->W.wsym;
+    } else {
+        SBTE_TRY(ensure_w32(p->W, st));
+        Wt = p->W.w32;
+    }
+    return kOk;
+}
+
+static int q_fp32(spectral_plan_s *p, const double *fdev, double *Qdev, int B,
+                  bool maxpreserve, cudaStream_t st)
+{
+    SBTE_TRY(ensure32(p, B));
+    const int N = p->N;
+    ConvF32Config cfg;
+    const float *Wt = nullptr;
+    SBTE_TRY(resolve_f32(p, maxpreserve, cfg, Wt, st));
     const int bg = cfg.bg;
     const int groups = (B + bg - 1) / bg;
     const float pf_f = (float)p->pf_fwd, pf_i = (float)p->pf_inv;
     float2 *P = p->c32[0], *R = p->c32[1], *S = p->c32[2];
     if (cfg.variant == 4) {
         SBTE_TRY(ensure32x4(p, B));
-        SBTE_TRY(ensure_w32x2(p->W, st));
         float4 *P4 = p->c32x4[0], *R4 = p->c32x4[1], *S4 = p->c32x4[2], *T4 = p->c32x4[3];
         const double *gsrc = fdev;
         if (maxpreserve) {
@@ -795,7 +834,7 @@ static int q_fp32(spectral_plan_s *p, const double *fdev, double *Qdev, int B,
             SBTE_CUDA(cudaMemsetAsync(p->qacc, 0, sizeof(double2) * (size_t)groups * bg * p->n3, st));
         auto *ev = prof_slot(p);
         if (ev) cudaEventRecord(ev->first, st);
-        SBTE_LAUNCH(conv_f32_batched(p->W.w32, P, P, nullptr, nullptr, p->qacc, N, B, cfg,
+        SBTE_LAUNCH(conv_f32_batched(Wt, P, P, nullptr, nullptr, p->qacc, N, B, cfg,
                                      p->d_status, st), 1);
         if (ev) cudaEventRecord(ev->second, st);
     } else {
@@ -813,7 +852,7 @@ static int q_fp32(spectral_plan_s *p, const double *fdev, double *Qdev, int B,
             SBTE_CUDA(cudaMemsetAsync(p->qacc, 0, sizeof(double2) * (size_t)groups * bg * p->n3, st));
         auto *ev = prof_slot(p);
         if (ev) cudaEventRecord(ev->first, st);
-        SBTE_LAUNCH(conv_f32_batched(p->W.w32, P, R, S, P, p->qacc, N, B, cfg, p->d_status,
+        SBTE_LAUNCH(conv_f32_batched(Wt, P, R, S, P, p->qacc, N, B, cfg, p->d_status,
                                      st), 1);
         if (ev) cudaEventRecord(ev->second, st);
     }
@@ -1198,11 +1237,12 @@ int spectral_graph_capture(spectral_plan *p, int kind, double *f_dev, int B, dou
     }
     if (flags & SPECTRAL_FP32) {
         SBTE_TRY(ensure32(p, nb));
-        SBTE_TRY(ensure_w32(p->W, p->stream));
-        if (p->tune.variant == 4) {
-            SBTE_TRY(ensure32x4(p, nb));
-            SBTE_TRY(ensure_w32x2(p->W, p->stream));
-        }
+        ConvF32Config cfg;
+        const float *Wt = nullptr;
+        // build the weight table of the configuration the step will run
+        // (a capture cannot synchronise the stream)
+        SBTE_TRY(resolve_f32(p, (flags & SPECTRAL_MAXPRESERVE) != 0, cfg, Wt, p->stream));
+        if (cfg.variant == 4) SBTE_TRY(ensure32x4(p, nb));
     } else {
         SBTE_TRY(ensure64(p, nb));
     }
@@ -1295,13 +1335,19 @@ int spectral_plan_set_tuning(spectral_plan *p, int variant, int bg, int zs, int 
     return kOk;
 }
 
+int spectral_plan_set_symmetric(spectral_plan *p, int on)
+{
+    if (!p) return set_error(kErrArg, "null plan"), kErrArg;
+    p->sym = on ? 1 : 0;
+    return kOk;
+}
+
 int spectral_plan_autotune(spectral_plan *p, int B, int flags, int *chosen)
 {
     if (!p || B < 1) return set_error(kErrArg, "bad arguments"), kErrArg;
     if (!p->W.w64) return set_error(kErrWeights, "autotune: no weights"), kErrWeights;
     SBTE_CUDA(cudaSetDevice(p->device));
     SBTE_TRY(ensure32(p, B));
-    SBTE_TRY(ensure_w32(p->W, p->stream));
     const bool two = (flags & SPECTRAL_MAXPRESERVE) != 0;
     const ConvF32Config cands[] = {
         {32, 2, 16},       {64, 2, 16},       {64, 3, 16},       {128, 2, 16},
@@ -1313,8 +1359,18 @@ int spectral_plan_autotune(spectral_plan *p, int B, int flags, int *chosen)
     SBTE_CUDA(cudaEventCreate(&e1));
     float best = 1e30f;
     ConvF32Config bestc = p->tune;
-    for (const auto &c : cands) {
+    for (ConvF32Config c : cands) {
         if (!conv_f32_supported(p->N, c, two)) continue;
+        // time each variant in the form the plan would run it
+        c.sym = (p->sym && (c.variant == 2 || c.variant == 3)) ? 1 : 0;
+        const float *Wt = nullptr;
+        if (c.sym) {
+            SBTE_TRY(ensure_wsym(p->W, p->stream));
+            Wt = p->W.wsym;
+        } else if (c.variant != 4) {
+            SBTE_TRY(ensure_w32(p->W, p->stream));
+            Wt = p->W.w32;
+        }
         float2 *P = p->c32[0], *R = p->c32[1], *S = p->c32[2];
         float ms_total = 0.f;
         for (int rep = 0; rep < 3; rep++) {
@@ -1332,7 +1388,7 @@ int spectral_plan_autotune(spectral_plan *p, int B, int flags, int *chosen)
                     ? conv_x4(p->W.w32x2, p->c32x4[0], p->c32x4[1], two ? p->c32x4[2] : nullptr,
                               two ? p->c32x4[3] : nullptr, p->qacc, p->N, B, c.bg, c.zs,
                               c.stages, c.flush, p->d_status, p->stream)
-                    : conv_f32_batched(p->W.w32, P, R, two ? S : nullptr, two ? P : nullptr,
+                    : conv_f32_batched(Wt, P, R, two ? S : nullptr, two ? P : nullptr,
                                        p->qacc, p->N, B, c, p->d_status, p->stream);
             cudaEventRecord(e1, p->stream);
             if (e != cudaSuccess) {

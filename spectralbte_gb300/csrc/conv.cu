@@ -331,6 +331,45 @@ __global__ void tile_weights_kernel(const double *__restrict__ W,
     }
 }
 
+// One CTA per zeta-row (zx, zy): list the run rows in order (sym_slots of
+// them), then fill Wsym[zrow][slot][zz][xz].  FP64 sum, one FP32 rounding.
+__global__ void sym_weights_kernel(const double *__restrict__ W, float *__restrict__ Wsym, int N)
+{
+    __shared__ short rows[32 * 32 / 2 + 2];
+    __shared__ int nrows;
+    const int nn = N * N, h = N / 2;
+    const long long n3 = (long long)nn * N;
+    const int zrow = blockIdx.x, zx = zrow / N, zy = zrow % N;
+    const int ms = sym_max_slots(N);
+    if (threadIdx.x == 0) {
+        int k = 0;
+        for (int r = 0; r < nn && k < ms; r++) {
+            const int sx = (zx + h - r / N + N) % N, sy = (zy + h - r % N + N) % N;
+            if (sx * N + sy >= r) rows[k++] = (short)r;
+        }
+        nrows = k;
+    }
+    __syncthreads();
+    const int nr = nrows;
+    float *out = Wsym + (long long)zrow * ms * nn;
+    for (int t = threadIdx.x; t < ms * nn; t += blockDim.x) {
+        const int slot = t / nn, zz = (t % nn) / N, xz = t % N;
+        double w = 0.0;
+        if (slot < nr) {
+            const int r = rows[slot];
+            const int sx = (zx + h - r / N + N) % N, sy = (zy + h - r % N + N) % N;
+            const int sr = sx * N + sy;
+            const long long zrow_off = ((long long)zrow * N + zz) * n3;
+            w = W[zrow_off + (long long)r * N + xz];
+            if (sr != r) {
+                const int sz = (zz + h - xz + N) % N;
+                w += W[zrow_off + (long long)sr * N + sz];
+            }
+        }
+        out[t] = (float)w;
+    }
+}
+
 __global__ void tile_weights_x2_kernel(const double *__restrict__ W,
                                        float2 *__restrict__ W2, int N)
 {
@@ -400,7 +439,8 @@ cudaError_t conv_f32_batched(const float *Wblk, const float2 *P,
     if (!conv_f32_supported(N, cfg, two) || B < 1) return cudaErrorInvalidValue;
     if (cfg.variant == 2 || cfg.variant == 3)
         return conv_ws(Wblk, P, R, S, T, qacc, N, B, cfg.bg, cfg.zs, cfg.variant == 2,
-                       cfg.stages, cfg.flush, status, st);
+                       cfg.stages, cfg.flush, cfg.sym, status, st);
+    if (cfg.sym) return cudaErrorInvalidValue;  // the symmetric form is variants 2, 3 only
     switch (N) {
     case 8:
         return two ? dispatch_bg<8, true>(Wblk, P, R, S, T, qacc, B, cfg, status, st)
@@ -422,6 +462,13 @@ cudaError_t weights_to_tiled_f32(const double *W, float *Wblk, int N,
                                  cudaStream_t st)
 {
     tile_weights_kernel<<<152 * 8, 256, 0, st>>>(W, Wblk, N);
+    return cudaGetLastError();
+}
+
+cudaError_t weights_to_sym_f32(const double *W, float *Wsym, int N, cudaStream_t st)
+{
+    if (N % 2 != 0 || N > 32 || N < 2) return cudaErrorInvalidValue;
+    sym_weights_kernel<<<N * N, 256, 0, st>>>(W, Wsym, N);
     return cudaGetLastError();
 }
 

@@ -24,6 +24,17 @@
 //    wrap arithmetic remains.
 //  * FP32 partial sums go to an FP64 accumulator every `flush` xi-rows.  The
 //    first flush stores, later flushes add, so no memset is needed.
+//  * Symmetric form (sym != 0).  For a fixed zeta the partner map
+//    sigma(xi) = (zeta + N/2 - xi) mod N (per axis) is an involution, and the
+//    product the sum weights is symmetric in (xi, sigma(xi)) whenever g = f:
+//    ghat[xi] fhat[sigma xi] for Q(f,f), and ghat[xi] fhat[sigma xi] +
+//    Mhat[xi] ghat[sigma xi] with fhat = Mhat + ghat for the maxPreserve sum.
+//    So the xi-rows pair up as (r, sigma(r)), and one pass over row r with
+//    the tile W[zeta][r][zz][xz] + W[zeta][sigma r][zz][sigma_z(xz)] covers
+//    both.  The producer skips every row whose partner precedes it, and the
+//    CTA runs (N^2 + F)/2 slots instead of N^2, where F (0 or 4) counts the
+//    rows that are their own partner.  Wblk is then the pre-summed table of
+//    weights_to_sym_f32.
 #include "common.cuh"
 #include "kernels.h"
 #include "mbarrier.cuh"
@@ -55,7 +66,7 @@ template <int N, int BG, int ZS, bool TWO, bool PACKED, int STG>
 __global__ void __launch_bounds__(WsLayout<N, BG, ZS, TWO, PACKED, STG>::kThreads)
 conv_ws_kernel(const float *__restrict__ Wblk, const float2 *__restrict__ P,
                const float2 *__restrict__ R, const float2 *__restrict__ S,
-               const float2 *__restrict__ T, double2 *__restrict__ qacc, int flush,
+               const float2 *__restrict__ T, double2 *__restrict__ qacc, int flush, int sym,
                unsigned int *__restrict__ status)
 {
     using L = WsLayout<N, BG, ZS, TWO, PACKED, STG>;
@@ -76,6 +87,8 @@ conv_ws_kernel(const float *__restrict__ Wblk, const float2 *__restrict__ P,
     const int zrow = blockIdx.x;
     const int zx = zrow / N, zy = zrow % N;
     const long long grp = blockIdx.y;
+    // slots this CTA runs: every xi-row, or one per partner pair
+    const int nslot = sym ? sym_slots(N, zx, zy) : NN;
 
     if (tid == 0) {
         for (int s = 0; s < ST; s++) {
@@ -89,30 +102,33 @@ conv_ws_kernel(const float *__restrict__ Wblk, const float2 *__restrict__ P,
     if (warp == NCW) {
         // ------------------------------------------------------ producer
         if ((tid & 31) != 0) return;
-        const float *Wbase = Wblk + (long long)zrow * NN * NN;
+        const float *Wbase = Wblk + (long long)zrow * (sym ? sym_max_slots(N) : NN) * NN;
         const float2 *Pg = P + grp * N3 * BG;
         const float2 *Rg = R + grp * N3 * BG;
         const float2 *Sg = TWO ? S + grp * N3 * BG : nullptr;
         const float2 *Tg = TWO ? T + grp * N3 * BG : nullptr;
-        for (int it = 0; it < NN; it++) {
-            const int s = it % ST;
-            if (it >= ST) {
-                if (!mbar_wait_bounded(&empty[s], (uint32_t)(((it / ST) - 1) & 1))) {
-                    atomicOr(status, kStatusTimeout);
-                    return;
-                }
-            }
-            unsigned char *base = smem + s * L::kStageBytes;
+        int slot = 0;
+        for (int it = 0; it < NN && slot < nslot; it++) {
             const int xx = it / N, xy = it % N;
             const int fx = (zx + H - xx < 0) ? zx + H - xx + N
                            : (zx + H - xx > N - 1 ? zx + H - xx - N : zx + H - xx);
             const int fy = (zy + H - xy < 0) ? zy + H - xy + N
                            : (zy + H - xy > N - 1 ? zy + H - xy - N : zy + H - xy);
+            if (sym && fx * N + fy < it) continue;  // covered by its partner row
+            const int s = slot % ST;
+            if (slot >= ST) {
+                if (!mbar_wait_bounded(&empty[s], (uint32_t)(((slot / ST) - 1) & 1))) {
+                    atomicOr(status, kStatusTimeout);
+                    return;
+                }
+            }
+            unsigned char *base = smem + s * L::kStageBytes;
             const long long prow = (long long)it * N * BG;
             const long long rrow = ((long long)fx * N + fy) * N * BG;
             mbar_expect_tx(&full[s], L::kStageBytes);
             unsigned char *d = base;
-            bulk_g2s(d, Wbase + (long long)it * NN, L::kWBytes, &full[s]);
+            bulk_g2s(d, Wbase + (long long)slot * NN, L::kWBytes, &full[s]);
+            slot++;
             d += L::kWBytes;
             bulk_g2s(d, Pg + prow, L::kRowBytes, &full[s]);
             d += L::kRowBytes;
@@ -164,7 +180,7 @@ conv_ws_kernel(const float *__restrict__ Wblk, const float2 *__restrict__ P,
         first_flush = false;
     };
 
-    for (int it = 0; it < NN; it++) {
+    for (int it = 0; it < nslot; it++) {
         const int s = it % ST;
         if (!mbar_wait_bounded(&full[s], (uint32_t)((it / ST) & 1))) {
             atomicOr(status, kStatusTimeout);
@@ -281,7 +297,7 @@ conv_ws_kernel(const float *__restrict__ Wblk, const float2 *__restrict__ P,
 
 template <int N, int BG, int ZS, bool TWO, bool PACKED, int ST>
 cudaError_t launch_ws(const float *Wblk, const float2 *P, const float2 *R, const float2 *S,
-                      const float2 *T, double2 *qacc, int B, int flush, unsigned *status,
+                      const float2 *T, double2 *qacc, int B, int flush, int sym, unsigned *status,
                       cudaStream_t st)
 {
     using L = WsLayout<N, BG, ZS, TWO, PACKED, ST>;
@@ -291,7 +307,7 @@ cudaError_t launch_ws(const float *Wblk, const float2 *P, const float2 *R, const
                                          (int)smem);
     if (e != cudaSuccess) return e;
     dim3 grid(N * N, (B + BG - 1) / BG);
-    kern<<<grid, L::kThreads, smem, st>>>(Wblk, P, R, S, T, qacc, flush, status);
+    kern<<<grid, L::kThreads, smem, st>>>(Wblk, P, R, S, T, qacc, flush, sym, status);
     return cudaGetLastError();
 }
 
@@ -326,16 +342,16 @@ bool conv_ws_supported(int N, int bg, int zs, bool packed, int stages, bool two)
 
 cudaError_t conv_ws(const float *Wblk, const float2 *P, const float2 *R, const float2 *S,
                     const float2 *T, double2 *qacc, int N, int B, int bg, int zs, bool packed,
-                    int stages, int flush, unsigned int *status, cudaStream_t st)
+                    int stages, int flush, int sym, unsigned int *status, cudaStream_t st)
 {
     const bool two = (S != nullptr);
     if (!conv_ws_supported(N, bg, zs, packed, stages, two) || B < 1) return cudaErrorInvalidValue;
 #define SBTE_WS_L(NN, BGV, ZSV, PK, STV)                                                    \
     if (N == NN && bg == BGV && zs == ZSV && packed == (PK != 0) && stages == STV)         \
         return two ? launch_ws<NN, BGV, ZSV, true, PK != 0, STV>(Wblk, P, R, S, T, qacc, B,  \
-                                                                 flush, status, st)       \
+                                                                 flush, sym, status, st)  \
                    : launch_ws<NN, BGV, ZSV, false, PK != 0, STV>(Wblk, P, R, S, T, qacc, B, \
-                                                                  flush, status, st);
+                                                                  flush, sym, status, st);
     SBTE_WS_SHAPES(SBTE_WS_L)
 #undef SBTE_WS_L
     return cudaErrorInvalidValue;

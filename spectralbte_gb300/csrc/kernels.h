@@ -64,6 +64,8 @@ struct ConvF32Config {
                       // packed FP32x2 math; 3: warp-specialised, scalar math;
                       // 4: warp-specialised, FP32x2 on expanded operands
     int zs = 0;       // variants 2, 3: zeta_z values per thread (8 or 16)
+    int sym = 0;      // variants 2, 3: symmetric form over partner xi-rows
+                      // (Wblk is then the table of weights_to_sym_f32)
 };
 cudaError_t conv_f32_batched(const float *Wblk, const float2 *P,
                              const float2 *R, const float2 *S,
@@ -79,8 +81,27 @@ bool conv_ws_supported(int N, int bg, int zs, bool packed, int stages,
                        bool two_pairs);
 cudaError_t conv_ws(const float *Wblk, const float2 *P, const float2 *R,
                     const float2 *S, const float2 *T, double2 *qacc, int N, int B,
-                    int bg, int zs, bool packed, int stages, int flush,
+                    int bg, int zs, bool packed, int stages, int flush, int sym,
                     unsigned int *status, cudaStream_t st);
+
+// Symmetric form of the convolution for g = f (both Q(f,f) and the
+// maxPreserve sum).  For zeta-row (zx, zy) the xi-row partner map is
+// r = (xx, xy) -> (sx, sy), s_a = (z_a + N/2 - x_a) mod N; a row is run
+// when its partner does not precede it (flat index sx*N+sy >= xx*N+xy).
+// For even N an axis has two self-partnered values when z_a + N/2 is even
+// and none otherwise, so a zeta-row runs N^2/2 + 2 slots when both axes
+// have them and N^2/2 otherwise.
+__host__ __device__ inline int sym_slots(int N, int zx, int zy)
+{
+    const int h = N / 2;
+    return (N * N) / 2 + ((((zx + h) & 1) == 0 && ((zy + h) & 1) == 0) ? 2 : 0);
+}
+__host__ __device__ inline int sym_max_slots(int N) { return (N * N) / 2 + 2; }
+// Wsym[zrow][slot][zz][xz] (FP32) for the slots in run order: the tile of
+// row r plus, when r is not its own partner, the partner's tile with xz
+// mapped through s_z = (zz + N/2 - xz) mod N, summed in FP64.  Slots beyond
+// sym_slots of a zeta-row are zero.  N even; size N^2 * sym_max_slots * N^2.
+cudaError_t weights_to_sym_f32(const double *W, float *Wsym, int N, cudaStream_t st);
 
 // The expanded-operand FP32x2 convolution (variant 4): W tiled with every
 // value as a (w, w) pair; P, S in the G4 form and R, T in the F4 form

@@ -197,6 +197,37 @@ def test_plan_fp32_matches_fp64(gpu, oracle, N, L_v, lam, B, mp):
     plan.close()
 
 
+@pytest.mark.parametrize("N,L_v,lam,B", [(16, 5.0, 1.0, 37), (24, 6.0, 0.0, 70),
+                                         (32, 6.0, 1.0, 130)])
+@pytest.mark.parametrize("mp", [False, True])
+def test_fp32_symmetric_form_matches_plain_rows(gpu, oracle, N, L_v, lam, B, mp):
+    """The row-pair form of the warp-specialised kernels (the default) against
+    the same kernels over every xi-row, and both against FP64: the same sum in
+    another order, so both stay at FP32 rounding distance from FP64."""
+    import torch
+    g, plan, _ = plan_for(gpu, oracle, N, L_v, lam, B)
+    f = _two_max_batch(g, B, 9)
+    fd = torch.from_numpy(f).cuda()
+    Q64, Qs, Qp = (torch.empty_like(fd) for _ in range(3))
+    extra = gpu.MAXPRESERVE if mp else 0
+    plan.computeQ_device(fd, Q64, B, gpu.FP64 | extra)
+    b = Q64.cpu().numpy()
+    for variant, bg, zs, stages in [(3, 64, 8, 3), (2, 32, 8, 2), (3, 32, 8, 3)]:
+        plan.set_tuning(bg, stages, 16, variant=variant, zs=zs)
+        plan.set_symmetric(True)
+        plan.computeQ_device(fd, Qs, B, gpu.FP32 | extra)
+        plan.set_symmetric(False)
+        plan.computeQ_device(fd, Qp, B, gpu.FP32 | extra)
+        s, p = Qs.cpu().numpy(), Qp.cpu().numpy()
+        es = max(rel_l2(s[i], b[i]) for i in range(B))
+        ep = max(rel_l2(p[i], b[i]) for i in range(B))
+        assert es < 1e-5 and ep < 1e-5, (variant, es, ep)
+        assert es <= 2.0 * ep + 1e-7, (variant, es, ep)
+        assert max(rel_l2(s[i], p[i]) for i in range(B)) < 1e-5
+    assert plan.status() == 0
+    plan.close()
+
+
 def test_fp32_unsupported_n_is_an_error(gpu, oracle):
     import torch
     g = oracle.Grid(7, 4.5, "0d")
