@@ -55,8 +55,11 @@ NCU_TRAFFIC = {
         "kernel": "conv_ws_kernel"},
 }
 # The same kernel in its symmetric (row-pair) form streams the partner-summed
-# table, about half of W; no capture of it yet, so its traffic is left out.
-NCU_TRAFFIC_SYM = {}
+# table, N^2 (N^4 + N^2)/2 FP32 values (profiles/conv_ws_sym_n24_b128_ncu.md).
+NCU_TRAFFIC_SYM = {
+    3: {"bytes": 1.551603e9 + 45.4912e6, "N": 24, "B": 128, "bg": 32,
+        "kernel": "conv_ws_kernel (row-pair form)"},
+}
 KERNEL_NAME = {1: "conv_f32_kernel", 2: "conv_ws_kernel", 3: "conv_ws_kernel",
                4: "conv_x4_kernel"}
 
@@ -68,7 +71,9 @@ def scaled_traffic(variant: int, N: int, B: int, bg: int, sym: bool = False):
         return None, None
     groups = -(-B // bg)
     cap_groups = -(-cap["B"] // cap["bg"])
-    return cap["bytes"] / cap_groups * groups * (N / cap["N"]) ** 6, cap
+    n0 = cap["N"]
+    size = ((N ** 6 + N ** 4) / (n0 ** 6 + n0 ** 4)) if sym else (N / n0) ** 6
+    return cap["bytes"] / cap_groups * groups * size, cap
 
 
 def load_peaks():
@@ -760,9 +765,9 @@ def run_ours(args):
             "launch_ms": conv_avg_s * 1e3,
             "traffic": traffic,
             "traffic_note": ((f"bytes per launch, scaled by N^6 x instance groups from the ncu "
-                              f"capture of {tcap['kernel']} at N=24, B=128, bg={tcap['bg']}; W "
-                              f"is re-read once per instance group of {tuned[1]}, from HBM, far "
-                              f"below the HBM peak") if tcap else
+                              f"capture of {tcap['kernel']} at N=24, B=128, bg={tcap['bg']}; "
+                              f"the weight table is re-read once per instance group of "
+                              f"{tuned[1]}, from HBM, far below the HBM peak") if tcap else
                              "no ncu capture of this form yet"),
             "hbm": {"achieved": hbm_achieved, "peak": float(peaks["hbm_gbs"]), "unit": "GB/s",
                     "frac": hbm_achieved / float(peaks["hbm_gbs"]),
