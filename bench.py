@@ -76,6 +76,41 @@ def scaled_traffic(variant: int, N: int, B: int, bg: int, sym: bool = False):
     return cap["bytes"] / cap_groups * groups * size, cap
 
 
+def run_maxpreserve(plan, fd, Qd, B, B64, Q64, steps=3):
+    """ComputeQ_maxPreserve semantics (collisions.c:178-210) + conservation on
+    the same instances: the FP32 batched path on all B (CUDA events, after one
+    warm-up) and the plain FP64 path on the first B64, with their rel-L2."""
+    import torch
+    flags32 = sb.FP32 | sb.MAXPRESERVE | sb.CONSERVE
+    flags64 = sb.FP64 | sb.MAXPRESERVE | sb.CONSERVE
+    plan.computeQ_device(fd, Qd, B, flags32)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        plan.computeQ_device(fd, Qd, B, flags32)
+    e1.record()
+    torch.cuda.synchronize()
+    ms32 = e0.elapsed_time(e1) / steps
+    plan.computeQ_device(fd[:B64], Q64, B64, flags64)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    plan.computeQ_device(fd[:B64], Q64, B64, flags64)
+    torch.cuda.synchronize()
+    s64 = time.perf_counter() - t0
+    a = Qd[:B64].cpu().numpy()
+    b = Q64.cpu().numpy()
+    rel = max(float(np.linalg.norm(a[i] - b[i]) / np.linalg.norm(b[i])) for i in range(B64))
+    return {"fp32": {"value": B / ms32 * 1e3, "unit": UNIT, "ms_per_step": ms32,
+                     "batch": B, "steps": steps},
+            "fp64_plain": {"value": B64 / s64, "unit": UNIT, "batch": B64},
+            "rel_l2_fp32_vs_fp64_max": rel,
+            "note": ("Q(M,g) + Q(g,M) + Q(g,g) with M the Maxwellian of f, g = f - M, in one "
+                     "weight pass with two products per term (the reference runs three "
+                     "convolutions); conservation applied")}
+
+
 def load_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -672,6 +707,7 @@ def run_ours(args):
     a = Qd[:B64].double().cpu().numpy()
     b = Q64.cpu().numpy()
     rel = [float(np.linalg.norm(a[i] - b[i]) / np.linalg.norm(b[i])) for i in range(B64)]
+    maxp = None if args.no_maxpreserve else run_maxpreserve(plan, fd, Qd, B, B64, Q64)
     status = plan.status()
     fma_rate = sb.fp32_fma_rate()  # measured on this GPU, after the timed region
     peaks, peak_src = load_peaks()
@@ -777,6 +813,7 @@ def run_ours(args):
                 "h2d_bytes_per_step": 8 * B * n3, "d2h_bytes_per_step": 8 * B * n3},
         "gpu_launches": launches,
         "clocks": clk,
+        "maxpreserve": maxp,
         "fp64_plain": {"value": fp64_rate, "unit": UNIT, "batch": B64,
                        "speedup_fp32_vs_fp64": value / world / fp64_rate},
         "accuracy": {"fp32_vs_fp64_rel_l2_max": max(rel), "tolerance": 1e-3},
@@ -821,6 +858,8 @@ def main():
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--tuning", default="",
                     help="variant,bg,zs,stages,flush of the FP32 convolution (default: autotune)")
+    ap.add_argument("--no-maxpreserve", action="store_true",
+                    help="skip the maxPreserve measurement of the main line")
     ap.add_argument("--no-sym", action="store_true",
                     help="run every xi-row of the FP32 convolution (no row-pair form)")
     args = ap.parse_args()
