@@ -81,6 +81,7 @@ def run_maxpreserve(plan, fd, Qd, B, B64, Q64, steps=3):
     the same instances: the FP32 batched path on all B (CUDA events, after one
     warm-up) and the plain FP64 path on the first B64, with their rel-L2."""
     import torch
+    import spectralbte_gb300 as sb
     flags32 = sb.FP32 | sb.MAXPRESERVE | sb.CONSERVE
     flags64 = sb.FP64 | sb.MAXPRESERVE | sb.CONSERVE
     plan.computeQ_device(fd, Qd, B, flags32)
