@@ -61,7 +61,7 @@ NCU_TRAFFIC_SYM = {
         "kernel": "conv_ws_kernel (row-pair form)"},
 }
 KERNEL_NAME = {1: "conv_f32_kernel", 2: "conv_ws_kernel", 3: "conv_ws_kernel",
-               4: "conv_x4_kernel"}
+               4: "conv_x4_kernel", 5: "conv_ws_kernel"}
 
 
 def scaled_traffic(variant: int, N: int, B: int, bg: int, sym: bool = False):
@@ -644,7 +644,7 @@ def run_ours(args):
         tuned = (variant, bg, zs, stages, flush)
     else:
         tuned = plan.autotune(B, sb.FP32)
-    sym = (not args.no_sym) and tuned[0] in (2, 3)
+    sym = (not args.no_sym) and tuned[0] in (2, 3, 5)
 
     for _ in range(args.warmup):
         plan.computeQ_device(fd, Qd, B, flags)

@@ -226,13 +226,17 @@ int spectral_graph_capture(spectral_plan *plan, int kind, double *f_dev, int B,
                            double dt, double Kn, int order, int flags);
 int spectral_graph_launch(spectral_plan *plan, void *stream);
 
-/* FP32 convolution tuning.  variant 1 = block-barrier kernel, 2 = warp-
-   specialised kernel with packed FP32x2 math; bg = instances per CTA (32,
-   64, 128); zs = zeta_z values per thread (variant 2: 8 or 16); stages =
-   copy pipeline depth (variant 1: 2 or 3; variant 2 chooses its own);
-   flush = xi-rows per FP64 flush.  The autotuner times the supported
-   shapes on B instances and keeps the fastest; *chosen (optional, 5 ints:
-   variant, bg, zs, stages, flush) receives it. */
+/* FP32 convolution tuning.  variant 1 = block-barrier kernel; 2 = warp-
+   specialised kernel with packed FP32x2 math; 3 = warp-specialised, scalar
+   math; 4 = warp-specialised, FP32x2 on pre-expanded operands; 5 = as 3 with
+   the registers capped so that three CTAs share an SM (one-pair form only:
+   maxPreserve calls run variant 3's shape instead).  bg = instances per
+   CTA (32, 64, 128); zs = zeta_z values per thread (variants 2-5: 8 or 16);
+   stages = copy pipeline depth; flush = xi-rows per FP64 flush.  Shapes
+   that are not instantiated return SPECTRAL_ERR_UNSUPPORTED.  The
+   autotuner times the supported shapes on B instances and keeps the
+   fastest; *chosen (optional, 5 ints: variant, bg, zs, stages, flush)
+   receives it. */
 int spectral_plan_set_tuning(spectral_plan *plan, int variant, int bg, int zs,
                              int stages, int flush);
 int spectral_plan_autotune(spectral_plan *plan, int B, int flags,

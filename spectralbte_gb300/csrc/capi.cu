@@ -770,7 +770,7 @@ static int resolve_f32(spectral_plan_s *p, bool maxpreserve, ConvF32Config &cfg,
             return kErrUnsupported;
         }
     }
-    cfg.sym = (p->sym && (cfg.variant == 2 || cfg.variant == 3)) ? 1 : 0;
+    cfg.sym = (p->sym && (cfg.variant == 2 || cfg.variant == 3 || cfg.variant == 5)) ? 1 : 0;
     Wt = nullptr;
     if (cfg.variant == 4) {
         SBTE_TRY(ensure_w32x2(p->W, st));
@@ -1352,7 +1352,7 @@ int spectral_plan_autotune(spectral_plan *p, int B, int flags, int *chosen)
     const ConvF32Config cands[] = {
         {32, 2, 16},       {64, 2, 16},       {64, 3, 16},       {128, 2, 16},
         {32, 2, 16, 2, 8}, {64, 2, 16, 2, 8}, {32, 3, 16, 3, 8}, {64, 2, 16, 3, 8},
-        {64, 3, 16, 3, 8}, {64, 2, 16, 3, 16}, {64, 3, 16, 3, 16},
+        {64, 3, 16, 3, 8}, {64, 2, 16, 3, 16}, {64, 3, 16, 3, 16}, {64, 2, 16, 5, 8},
         {32, 2, 16, 4, 8}, {64, 2, 16, 4, 8}, {32, 3, 16, 4, 8}};
     cudaEvent_t e0, e1;
     SBTE_CUDA(cudaEventCreate(&e0));
@@ -1362,7 +1362,7 @@ int spectral_plan_autotune(spectral_plan *p, int B, int flags, int *chosen)
     for (ConvF32Config c : cands) {
         if (!conv_f32_supported(p->N, c, two)) continue;
         // time each variant in the form the plan would run it
-        c.sym = (p->sym && (c.variant == 2 || c.variant == 3)) ? 1 : 0;
+        c.sym = (p->sym && (c.variant == 2 || c.variant == 3 || c.variant == 5)) ? 1 : 0;
         const float *Wt = nullptr;
         if (c.sym) {
             SBTE_TRY(ensure_wsym(p->W, p->stream));

@@ -62,8 +62,8 @@ struct WsLayout {
 
 __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
 
-template <int N, int BG, int ZS, bool TWO, bool PACKED, int STG>
-__global__ void __launch_bounds__(WsLayout<N, BG, ZS, TWO, PACKED, STG>::kThreads)
+template <int N, int BG, int ZS, bool TWO, bool PACKED, int STG, int MINB>
+__global__ void __launch_bounds__(WsLayout<N, BG, ZS, TWO, PACKED, STG>::kThreads, MINB)
 conv_ws_kernel(const float *__restrict__ Wblk, const float2 *__restrict__ P,
                const float2 *__restrict__ R, const float2 *__restrict__ S,
                const float2 *__restrict__ T, double2 *__restrict__ qacc, int flush, int sym,
@@ -295,14 +295,14 @@ conv_ws_kernel(const float *__restrict__ Wblk, const float2 *__restrict__ P,
     if (since || first_flush) do_flush();
 }
 
-template <int N, int BG, int ZS, bool TWO, bool PACKED, int ST>
+template <int N, int BG, int ZS, bool TWO, bool PACKED, int ST, int MINB>
 cudaError_t launch_ws(const float *Wblk, const float2 *P, const float2 *R, const float2 *S,
                       const float2 *T, double2 *qacc, int B, int flush, int sym, unsigned *status,
                       cudaStream_t st)
 {
     using L = WsLayout<N, BG, ZS, TWO, PACKED, ST>;
     const size_t smem = (size_t)L::kStages * L::kStageBytes;
-    auto kern = conv_ws_kernel<N, BG, ZS, TWO, PACKED, ST>;
+    auto kern = conv_ws_kernel<N, BG, ZS, TWO, PACKED, ST, MINB>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
@@ -321,18 +321,24 @@ size_t ws_smem()
 }  // namespace
 
 // Shapes instantiated for the warp-specialised kernel:
-// (N, bg, zs, packed, stages); variant 2 = packed FP32x2, 3 = scalar.
-#define SBTE_WS_SHAPES(X)                                                     \
-    X(8, 32, 8, 1, 2) X(8, 32, 8, 0, 3) X(8, 64, 8, 0, 3)                     \
-    X(16, 32, 8, 1, 2) X(16, 32, 8, 0, 3) X(16, 64, 8, 0, 3) X(16, 64, 16, 0, 3) \
-    X(24, 32, 8, 1, 2) X(24, 32, 8, 0, 3) X(24, 64, 8, 0, 2) X(24, 64, 8, 0, 3)  \
-    X(32, 32, 8, 1, 2) X(32, 64, 8, 1, 2) X(32, 32, 8, 0, 3) X(32, 64, 8, 0, 2)  \
-    X(32, 64, 8, 0, 3) X(32, 64, 16, 0, 2) X(32, 64, 16, 0, 3)
+// (N, bg, zs, packed, stages, minb); variant 2 = packed FP32x2, 3 = scalar,
+// 5 = scalar with the registers capped so that minb = 3 CTAs fit on an SM
+// (65536 / (3 x 288 threads) -> 72 registers at N = 32, bg = 64).
+#define SBTE_WS_SHAPES(X)                                                                 \
+    X(8, 32, 8, 1, 2, 1) X(8, 32, 8, 0, 3, 1) X(8, 64, 8, 0, 3, 1)                        \
+    X(16, 32, 8, 1, 2, 1) X(16, 32, 8, 0, 3, 1) X(16, 64, 8, 0, 3, 1) X(16, 64, 16, 0, 3, 1) \
+    X(24, 32, 8, 1, 2, 1) X(24, 32, 8, 0, 3, 1) X(24, 64, 8, 0, 2, 1) X(24, 64, 8, 0, 3, 1)  \
+    X(32, 32, 8, 1, 2, 1) X(32, 64, 8, 1, 2, 1) X(32, 32, 8, 0, 3, 1) X(32, 64, 8, 0, 2, 1)  \
+    X(32, 64, 8, 0, 3, 1) X(32, 64, 16, 0, 2, 1) X(32, 64, 16, 0, 3, 1)                   \
+    X(32, 64, 8, 0, 2, 3)
 
-bool conv_ws_supported(int N, int bg, int zs, bool packed, int stages, bool two)
+bool conv_ws_supported(int N, int bg, int zs, bool packed, int stages, bool two, int minb)
 {
-#define SBTE_WS_Q(NN, BGV, ZSV, PK, STV)                                                 \
-    if (N == NN && bg == BGV && zs == ZSV && packed == (PK != 0) && stages == STV)      \
+    // the two-pair form does not fit the capped register budget (it spills)
+    if (two && minb != 1) return false;
+#define SBTE_WS_Q(NN, BGV, ZSV, PK, STV, MB)                                             \
+    if (N == NN && bg == BGV && zs == ZSV && packed == (PK != 0) && stages == STV &&    \
+        minb == MB)                                                                      \
         return (two ? ws_smem<NN, BGV, ZSV, true, PK != 0, STV>()                       \
                     : ws_smem<NN, BGV, ZSV, false, PK != 0, STV>()) <= 227 * 1024;
     SBTE_WS_SHAPES(SBTE_WS_Q)
@@ -342,16 +348,19 @@ bool conv_ws_supported(int N, int bg, int zs, bool packed, int stages, bool two)
 
 cudaError_t conv_ws(const float *Wblk, const float2 *P, const float2 *R, const float2 *S,
                     const float2 *T, double2 *qacc, int N, int B, int bg, int zs, bool packed,
-                    int stages, int flush, int sym, unsigned int *status, cudaStream_t st)
+                    int stages, int flush, int sym, int minb, unsigned int *status,
+                    cudaStream_t st)
 {
     const bool two = (S != nullptr);
-    if (!conv_ws_supported(N, bg, zs, packed, stages, two) || B < 1) return cudaErrorInvalidValue;
-#define SBTE_WS_L(NN, BGV, ZSV, PK, STV)                                                    \
-    if (N == NN && bg == BGV && zs == ZSV && packed == (PK != 0) && stages == STV)         \
-        return two ? launch_ws<NN, BGV, ZSV, true, PK != 0, STV>(Wblk, P, R, S, T, qacc, B,  \
-                                                                 flush, sym, status, st)  \
-                   : launch_ws<NN, BGV, ZSV, false, PK != 0, STV>(Wblk, P, R, S, T, qacc, B, \
-                                                                  flush, sym, status, st);
+    if (!conv_ws_supported(N, bg, zs, packed, stages, two, minb) || B < 1)
+        return cudaErrorInvalidValue;
+#define SBTE_WS_L(NN, BGV, ZSV, PK, STV, MB)                                                  \
+    if (N == NN && bg == BGV && zs == ZSV && packed == (PK != 0) && stages == STV &&         \
+        minb == MB)                                                                           \
+        return two ? launch_ws<NN, BGV, ZSV, true, PK != 0, STV, MB>(Wblk, P, R, S, T, qacc, B, \
+                                                                     flush, sym, status, st) \
+                   : launch_ws<NN, BGV, ZSV, false, PK != 0, STV, MB>(Wblk, P, R, S, T, qacc,  \
+                                                                      B, flush, sym, status, st);
     SBTE_WS_SHAPES(SBTE_WS_L)
 #undef SBTE_WS_L
     return cudaErrorInvalidValue;

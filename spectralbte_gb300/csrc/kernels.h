@@ -62,9 +62,10 @@ struct ConvF32Config {
     int flush;        // xi-rows between FP64 flushes of the FP32 partial sums
     int variant = 1;  // 1: block-barrier kernel; 2: warp-specialised with
                       // packed FP32x2 math; 3: warp-specialised, scalar math;
-                      // 4: warp-specialised, FP32x2 on expanded operands
+                      // 4: warp-specialised, FP32x2 on expanded operands;
+                      // 5: as 3, registers capped for 3 CTAs per SM
     int zs = 0;       // variants 2, 3: zeta_z values per thread (8 or 16)
-    int sym = 0;      // variants 2, 3: symmetric form over partner xi-rows
+    int sym = 0;      // variants 2, 3, 5: symmetric form over partner xi-rows
                       // (Wblk is then the table of weights_to_sym_f32)
 };
 cudaError_t conv_f32_batched(const float *Wblk, const float2 *P,
@@ -77,12 +78,14 @@ bool conv_f32_supported(int N, ConvF32Config cfg, bool two_pairs);
 
 // The warp-specialised FP32x2 variant (conv_ws.cu); writes qacc on its
 // first flush, so it needs no zeroed accumulator.
+// minb: CTAs per SM the kernel's register budget is sized for (1, or 3 for
+// variant 5).
 bool conv_ws_supported(int N, int bg, int zs, bool packed, int stages,
-                       bool two_pairs);
+                       bool two_pairs, int minb);
 cudaError_t conv_ws(const float *Wblk, const float2 *P, const float2 *R,
                     const float2 *S, const float2 *T, double2 *qacc, int N, int B,
                     int bg, int zs, bool packed, int stages, int flush, int sym,
-                    unsigned int *status, cudaStream_t st);
+                    int minb, unsigned int *status, cudaStream_t st);
 
 // Symmetric form of the convolution for g = f (both Q(f,f) and the
 // maxPreserve sum).  For zeta-row (zx, zy) the xi-row partner map is
