@@ -235,16 +235,34 @@ def main(argv=None):
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--init", default=None, help="start from this saved network")
+    ap.add_argument("--families", default=",".join(FAMILIES),
+                    help="comma-separated subset of " + ",".join(FAMILIES))
+    ap.add_argument("--check-batch", type=int, default=0,
+                    help="also score the network on this many instances of the 0D "
+                         "two-Maxwellian workload (workloads.two_maxwellian_batch)")
+    ap.add_argument("--check-seed", type=int, default=20261203)
     ap.add_argument("--out", required=True)
     a = ap.parse_args(argv)
+    fams = tuple(x for x in a.families.split(",") if x)
+    if not fams or any(x not in FAMILIES for x in fams):
+        ap.error(f"--families: choose from {','.join(FAMILIES)}")
     torch.cuda.set_device(0)
     v, zeta = grid_0d(a.n, a.lv)
     plan = Plan(a.n, a.lv, v, zeta, 512)
     plan.generate_weights_iso(a.lam)
     plan.autotune(512, FP32)
     t0 = time.time()
-    F, Q, _ = make_dataset(plan, a.pairs, seed=a.seed)
+    F, Q, _ = make_dataset(plan, a.pairs, seed=a.seed, families=fams)
+    # held out: every family, whichever ones the network trains on
     Fe, Qe, fam = make_dataset(plan, a.heldout, seed=a.seed + 10 ** 6, out_dtype=torch.float64)
+    Fc = Qc = None
+    if a.check_batch > 0:
+        from .workloads import two_maxwellian_batch
+        Fc = torch.from_numpy(two_maxwellian_batch(v, a.check_batch, a.check_seed)).cuda()
+        Qc = torch.empty_like(Fc)
+        for i in range(0, a.check_batch, 512):
+            b = min(512, a.check_batch - i)
+            plan.computeQ_device(Fc[i:i + b], Qc[i:i + b], b, FP32 | CONSERVE)
     t_data = time.time() - t0
     if a.init:
         net = FourierOperator.load(a.init)
@@ -254,11 +272,21 @@ def main(argv=None):
         net.output_scale = output_scale(F, Q)
     net.set_loss_floor(a.floor)
     e0 = evaluate(net, plan, Fe, Qe)
+    c0 = evaluate(net, plan, Fc, Qc) if Fc is not None else None
     log = train(net, F, Q, a.steps, batch=a.batch, lr=a.lr, seed=a.seed,
                 time_limit=60.0 * a.minutes)
     e1 = evaluate(net, plan, Fe, Qe)
+    c1 = evaluate(net, plan, Fc, Qc) if Fc is not None else None
     net.save(a.out)
+
+    def stats(e):
+        return None if e is None else {"mean": e.mean().item(), "median": e.median().item(),
+                                       "max": e.max().item()}
     print(json.dumps({
+        "families": list(fams),
+        "heldout_by_family_untrained": family_stats(e0, fam),
+        "workload_check_untrained": stats(c0),
+        "workload_check_trained": stats(c1),
         "pairs": a.pairs, "data_seconds": round(t_data, 1), "steps": log.steps,
         "train_seconds": round(log.seconds, 1), "samples_per_s": log.samples / log.seconds,
         "loss_first_last": [log.losses[0], log.losses[-1]],
