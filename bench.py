@@ -347,8 +347,8 @@ def run_learned(args, plan, fd, Qd, B, flags, peaks):
         (q for q in (os.path.join(ROOT, "spectralbte_gb300", "models", n)
                      for n in ("fno_n32_two_maxwellian.npz", "fno_n32.npz"))
          if os.path.exists(q)), "")
-    if not os.path.exists(path):
-        return {"status": f"no trained network at {os.path.relpath(path, ROOT)}"}
+    if not path or not os.path.exists(path):
+        return {"status": "no trained network in spectralbte_gb300/models"}
     net = sb.FourierOperator.load(path)
     if net.N != plan.N:
         return {"status": f"network trained for N={net.N}, workload N={plan.N}"}
