@@ -60,6 +60,9 @@ NCU_TRAFFIC_SYM = {
     3: {"bytes": 1.551603e9 + 45.4912e6, "N": 24, "B": 128, "bg": 32,
         "kernel": "conv_ws_kernel (row-pair form)"},
 }
+# DRAM bytes (read + write) of one channel-mix launch of the learned operator
+# at 256 instances (profiles/learned_layer0_n32_b256_ncu.md, capture 1).
+LEARNED_CM_TRAFFIC = {"bytes": 2.15e9 + 1.04e9, "B": 256}
 KERNEL_NAME = {1: "conv_f32_kernel", 2: "conv_ws_kernel", 3: "conv_ws_kernel",
                4: "conv_x4_kernel", 5: "conv_ws_kernel"}
 
@@ -321,19 +324,31 @@ def run_uneven(args):
 def learned_work(N: int, C: int, Km: int, L: int, Hd: int) -> dict:
     """Algorithmic flops and DRAM bytes of one learned-operator evaluation
     (one instance): every GEMM's real multiply-adds, and every tensor the
-    kernel sequence writes once and reads once (BF16 between GEMMs, FP32 for
-    the spectral sum S, FP64 for f and Q and the conservation projection)."""
+    kernel sequence writes once and reads once.  16-bit elements between the
+    GEMMs (activations H, the spectral sum S, the transform intermediates
+    T1, T2, X, Y, U1, U2), FP32 for the scaled input x and the readout y,
+    FP64 for f and Q.
+      per layer: forward axes read H, write T1 / read T1, write T2 / read T2,
+                 write X; mode mix reads X, writes Y; inverse axes read Y,
+                 write U1 / read U1, write U2 / read U2, write S; channel mix
+                 reads H and S, writes H'  ->  5 act + 4 (t1 + t2 + xm)
+      outside:   inst_max reads f; to_pb reads f, writes x; lift reads x,
+                 writes H0; readout reads H_L, writes y; output scaling reads
+                 y, writes Q; conservation reads Q (moments), reads and
+                 writes Q (projection)  ->  64 P + 2 act
+    The ncu capture of layer 0 at 256 instances moved 9.93 GB (38.8 MB per
+    instance) against 40.0 MB here."""
     P = N ** 3
     fl = (4 * Km * N ** 3 * C + 8 * Km ** 2 * N ** 2 * C + 8 * Km ** 3 * N * C   # forward axes
           + 4 * C * C * Km ** 3                                                 # mode mix
           + 8 * N * Km ** 3 * C + 8 * N ** 2 * Km ** 2 * C + 4 * N ** 3 * Km * C  # inverse axes
           + 2 * C * C * P)                                                      # channel mix
     flops = L * fl + 2 * Hd * C * P + 2 * Hd * P
-    act, s32 = 2 * P * C, 4 * P * C
+    act = 2 * P * C
     t1, t2, xm = 2 * N * N * 2 * Km * C, 2 * N * 2 * Km * Km * C, 2 * 2 * Km ** 3 * C
-    per_layer = 2 * act + 2 * (t1 + t2 + xm) * 2 + 2 * s32 + act
-    bytes_ = 8 * P + 4 * P * 2 + act + L * per_layer + 4 * P + 8 * P + 4 * 8 * P
-    return {"flops": float(flops), "bytes": float(bytes_)}
+    per_layer = 5 * act + 4 * (t1 + t2 + xm)
+    bytes_ = 64 * P + 2 * act + L * per_layer
+    return {"flops": float(flops), "bytes": float(bytes_), "channel_mix_bytes": float(3 * act)}
 
 
 def run_learned(args, plan, fd, Qd, B, flags, peaks):
@@ -361,6 +376,7 @@ def run_learned(args, plan, fd, Qd, B, flags, peaks):
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     steps = max(2, args.steps)
     k0 = sb.kernel_launches()
+    net.set_profiling(True)   # events around every channel-mix launch
     e0.record()
     for _ in range(steps):
         plan.computeQ_device(fd, Ql, B, lf)
@@ -368,6 +384,8 @@ def run_learned(args, plan, fd, Qd, B, flags, peaks):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / steps
     launches = (sb.kernel_launches() - k0) / steps
+    cm_ms, cm_n = net.kernel_time()
+    net.set_profiling(False)
     d = (Ql - Qd).pow(2).sum(dim=1) / Qd.pow(2).sum(dim=1)
     rel = d.sqrt()
     # the spot-checked path: one instance per call against the plain FP32 operator
@@ -410,6 +428,13 @@ def run_learned(args, plan, fd, Qd, B, flags, peaks):
     w = learned_work(net.N, net.width, net.modes, net.layers, net.hidden)
     tflops = w["flops"] * B / (ms / 1e3) / 1e12
     gbs = w["bytes"] * B / (ms / 1e3) / 1e9
+    # the dominant kernel: the channel mix (bias + spectral sum + GELU fused),
+    # 3 activation tensors of 16-bit elements per launch
+    Bp = -(-B // 8) * 8
+    cm_bytes = w["channel_mix_bytes"] * Bp
+    cm_avg = cm_ms / max(cm_n, 1) / 1e3
+    cm_gbs = cm_bytes / cm_avg / 1e9 if cm_n else None
+    cm_traffic = LEARNED_CM_TRAFFIC["bytes"] / LEARNED_CM_TRAFFIC["B"] * Bp
     return {
         "network": {"N": net.N, "width": net.width, "modes": net.modes, "layers": net.layers,
                     "hidden": net.hidden, "params": net.nparams,
@@ -429,11 +454,21 @@ def run_learned(args, plan, fd, Qd, B, flags, peaks):
                          "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 8 * B * net.n3,
                                  "d2h_bytes_per_step": 8 * B * net.n3,
                                  "fallbacks": st_e2e["fallbacks"], "calls": st_e2e["calls"]}},
-        "roofline": {"bound": "hbm", "achieved": gbs, "peak": float(peaks["hbm_gbs"]),
-                     "unit": "GB/s", "frac": gbs / float(peaks["hbm_gbs"]),
-                     "algorithmic_bytes_per_eval": w["bytes"], "traffic": None,
-                     "traffic_note": ("aggregate over the network's kernels; per-kernel shares "
-                                      "in profiles/learned_n32_b256_launches.md"),
+        "roofline": {"bound": "hbm", "kernel": "gemm_sa_kernel (channel mix, kEpiLayer)",
+                     "achieved": cm_gbs, "peak": float(peaks["hbm_gbs"]), "unit": "GB/s",
+                     "frac": (cm_gbs / float(peaks["hbm_gbs"])) if cm_gbs else None,
+                     "traffic": cm_traffic,
+                     "algorithmic": (f"3 activation tensors x {w['channel_mix_bytes']:.4e} B x "
+                                     f"{Bp} instances = {cm_bytes:.4e} B per launch (read H "
+                                     f"and S, write H')"),
+                     "launch_ms": cm_avg * 1e3, "launches_timed": cm_n,
+                     "traffic_note": (f"ncu dram bytes of the same kernel at "
+                                      f"{LEARNED_CM_TRAFFIC['B']} instances "
+                                      f"(profiles/learned_layer0_n32_b256_ncu.md), scaled by "
+                                      f"instances"),
+                     "aggregate": {"achieved": gbs, "frac": gbs / float(peaks["hbm_gbs"]),
+                                   "unit": "GB/s", "algorithmic_bytes_per_eval": w["bytes"],
+                                   "note": "all kernels of one evaluation over the step time"},
                      "tensor": {"achieved": tflops, "peak": float(peaks["bf16_tflops"]),
                                 "unit": "TFLOP/s",
                                 "frac": tflops / float(peaks["bf16_tflops"]),
@@ -844,12 +879,10 @@ def run_ours(args):
     if learned is not None:
         line["learned"] = learned
         if learned.get("accepted") and world == 1:
-            # the headline path's roofline is the network's (HBM-bound, all its kernels);
-            # the convolution's stays with the plain-operator figures
+            # the headline path's roofline is its dominant kernel's, the network's
+            # channel mix (HBM-bound); the convolution's stays with the plain figures
             line["fp32_plain"]["roofline"] = line["roofline"]
-            lr = dict(learned["roofline"])
-            lr["kernel"] = "learned operator, all kernels of one evaluation (aggregate)"
-            line["roofline"] = lr
+            line["roofline"] = dict(learned["roofline"])
     if cpu:
         line["cpu_baseline"] = cpu
     print(json.dumps(line), flush=True)

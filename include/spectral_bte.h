@@ -318,6 +318,12 @@ int spectral_fno_precision(spectral_fno *net);
    separate kernels; off by default).  Every other shape uses the separate
    kernels. */
 int spectral_fno_set_fused(spectral_fno *net, int on);
+/* Channel-mix timing: with profiling on, CUDA events are recorded on the
+   launching stream around every channel-mix launch (the separate-kernel
+   path, outside graph captures); spectral_fno_kernel_time returns their
+   summed duration and count since profiling was switched on. */
+int spectral_fno_set_profiling(spectral_fno *net, int on);
+int spectral_fno_kernel_time(spectral_fno *net, double *ms_total, int *launches);
 int spectral_fno_destroy(spectral_fno *net);
 long long spectral_fno_num_params(spectral_fno *net);
 int spectral_fno_num_classes(spectral_fno *net);

@@ -152,6 +152,8 @@ def lib() -> C.CDLL:
         "spectral_fno_create": (i, [pp, i, i, i, i, i, i, i, C.c_ulonglong]),
         "spectral_fno_precision": (i, [v]),
         "spectral_fno_set_fused": (i, [v, i]),
+        "spectral_fno_set_profiling": (i, [v, i]),
+        "spectral_fno_kernel_time": (i, [v, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
         "spectral_fno_destroy": (i, [v]),
         "spectral_fno_num_params": (C.c_longlong, [v]),
         "spectral_fno_num_classes": (i, [v]),
@@ -546,6 +548,17 @@ class FourierOperator:
 
     def set_fused(self, on: bool):
         _check(self.L.spectral_fno_set_fused(self.h, 1 if on else 0), "fno_set_fused")
+
+    def set_profiling(self, on: bool):
+        """Time every channel-mix launch with CUDA events on its stream."""
+        _check(self.L.spectral_fno_set_profiling(self.h, 1 if on else 0), "fno_set_profiling")
+
+    def kernel_time(self) -> tuple:
+        """(total ms, launches) of the channel-mix launches timed so far."""
+        ms, n = C.c_double(), C.c_int()
+        _check(self.L.spectral_fno_kernel_time(self.h, C.byref(ms), C.byref(n)),
+               "fno_kernel_time")
+        return ms.value, n.value
 
     def set_loss_floor(self, eps: float):
         _check(self.L.spectral_fno_set_loss_floor(self.h, float(eps)), "fno_set_loss_floor")

@@ -586,6 +586,10 @@ struct spectral_fno_s {
     uint16_t *dU = nullptr, *dZ = nullptr, *GY = nullptr, *GX = nullptr;
     double *d_loss = nullptr;
     std::vector<void *> owned;
+    // channel-mix timing (spectral_fno_set_profiling): an event pair per launch
+    bool prof = false;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pev;
+    size_t pev_used = 0;
 
     void free_acts()
     {
@@ -603,6 +607,10 @@ struct spectral_fno_s {
     ~spectral_fno_s()
     {
         cudaSetDevice(device);
+        for (auto &e : pev) {
+            cudaEventDestroy(e.first);
+            cudaEventDestroy(e.second);
+        }
         free_acts();
         for (float *q : {params, grads, am, av, F, G, Fu, gs}) cudaFree(q);
         cudaFree(cls);
@@ -852,6 +860,26 @@ int fused_layer(spectral_fno_s *n, int l, const uint16_t *hin, uint16_t *hout, f
     return kOk;
 }
 
+// The next event pair for a timed channel-mix launch, or null when profiling
+// is off or the stream is being captured into a graph.
+std::pair<cudaEvent_t, cudaEvent_t> *prof_pair(spectral_fno_s *n, cudaStream_t st)
+{
+    if (!n->prof) return nullptr;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone)
+        return nullptr;
+    if (n->pev_used == n->pev.size()) {
+        std::pair<cudaEvent_t, cudaEvent_t> e{};
+        if (cudaEventCreate(&e.first) != cudaSuccess) return nullptr;
+        if (cudaEventCreate(&e.second) != cudaSuccess) {
+            cudaEventDestroy(e.first);
+            return nullptr;
+        }
+        n->pev.push_back(e);
+    }
+    return &n->pev[n->pev_used++];
+}
+
 template <typename E, typename T>
 int forward(spectral_fno_s *n, const T *f, int B, int Bp, bool train, cudaStream_t st)
 {
@@ -894,7 +922,10 @@ int forward(spectral_fno_s *n, const T *f, int B, int Bp, bool train, cudaStream
         a.hout = hout;
         a.act = gelu ? 1 : 0;
         set_ext(a, ext.prm - n->oW[l], ext.act, ext.act);
+        auto *ev = prof_pair(n, st);
+        if (ev) cudaEventRecord(ev->first, st);
         FNO_LAUNCH((launch_sa<E, 64, 64, 2, 2, false, false, kEpiLayer>(a, st)));
+        if (ev) cudaEventRecord(ev->second, st);
     }
     SaArgs a = sa_base(prm + n->oQ1, C, 1, 0, (int)Hd, (int)C);
     a.B = sv(Hbuf(n, n->L, train), Bp, Bp, C * Bp);
@@ -1233,6 +1264,38 @@ int spectral_fno_set_fused(spectral_fno *n, int on)
         return kErrArg;
     }
     n->fused = on != 0;
+    return kOk;
+}
+
+int spectral_fno_set_profiling(spectral_fno *n, int on)
+{
+    if (!n) {
+        set_error(kErrArg, "spectral_fno_set_profiling: null handle");
+        return kErrArg;
+    }
+    n->prof = on != 0;
+    n->pev_used = 0;
+    return kOk;
+}
+
+int spectral_fno_kernel_time(spectral_fno *n, double *ms_total, int *launches)
+{
+    if (!n || !ms_total || !launches) {
+        set_error(kErrArg, "spectral_fno_kernel_time: null argument");
+        return kErrArg;
+    }
+    double tot = 0.0;
+    for (size_t i = 0; i < n->pev_used; i++) {
+        float ms = 0.f;
+        if (cudaEventSynchronize(n->pev[i].second) != cudaSuccess ||
+            cudaEventElapsedTime(&ms, n->pev[i].first, n->pev[i].second) != cudaSuccess) {
+            set_error(kErrCuda, "spectral_fno_kernel_time: event %zu", i);
+            return kErrCuda;
+        }
+        tot += ms;
+    }
+    *ms_total = tot;
+    *launches = (int)n->pev_used;
     return kOk;
 }
 

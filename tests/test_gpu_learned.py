@@ -234,3 +234,26 @@ def test_fused_layer_matches_unfused(gpu, prec):
     assert rel_l2(out[True][0], out[False][0]) < 2e-3
     assert abs(out[True][1] - out[False][1]) <= 1e-3 * out[False][1]
     assert rel_l2(out[True][2], out[False][2]) < 5e-3
+
+
+def test_channel_mix_profiling_counts_launches(gpu):
+    """spectral_fno_set_profiling: one event pair per channel-mix launch (one
+    per layer and forward pass); the timed output equals the untimed one."""
+    import torch
+    net, spec, _ = _net(gpu, shape="wide")
+    B = 6
+    f, _ = _data(B, 21, spec.N)
+    fd = torch.from_numpy(f.astype(np.float64)).cuda()
+    Q0, Q1 = torch.zeros_like(fd), torch.zeros_like(fd)
+    net.predict(fd, Q0, B)
+    net.set_profiling(True)
+    for _ in range(3):
+        net.predict(fd, Q1, B)
+    ms, n = net.kernel_time()
+    net.set_profiling(False)
+    assert n == 3 * spec.L
+    assert ms > 0.0
+    assert torch.equal(Q0, Q1)
+    net.set_profiling(True)   # switching on again starts a new count
+    assert net.kernel_time() == (0.0, 0)
+    net.set_profiling(False)
