@@ -226,6 +226,14 @@ def cpu_sample_rate(po, g, W_rows_fn, f, rows: int, reps: int, threads: int) -> 
             "seconds_per_eval": t}
 
 
+def headline_config(N: int, L_v: float, lam: float, B: int, world: int) -> dict:
+    """The workload of the headline line, shared by both arms."""
+    return {"workload": (f"0D hard spheres (lambda=1), N={N}, L_v={L_v}, discontinuous "
+                         f"two-Maxwellian +-5% jitter, {B} instances per GPU"),
+            "N": N, "L_v": L_v, "lambda": lam, "batch_per_gpu": B,
+            "parallelism": f"{world} independent GPU(s), instances sharded"}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -252,17 +260,16 @@ def run_reference(args):
             vals.append(r["seconds_per_eval"])
     t = float(np.mean(vals))
     value = 1.0 / t
-    sample = (f"{rows} of {g.n3} zeta rows of the convolution per step (W rows: {distinct} "
-              f"distinct quadrature rows, tiled) plus the full transforms and projection, "
-              f"extrapolated to one evaluation; N={N}, L_v={L_v}, lambda={lam}")
+    sample = (f"one instance of the batch per step: {rows} of {g.n3} zeta rows of the "
+              f"convolution (W rows: {distinct} distinct quadrature rows, tiled) plus the full "
+              f"transforms and projection, extrapolated to one evaluation; every instance and "
+              f"every zeta row costs the same; N={N}, L_v={L_v}, lambda={lam}")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * t, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"0D hard spheres, N={N}, L_v={L_v}, discontinuous "
-                               "two-Maxwellian, one instance", "N": N, "L_v": L_v,
-                   "lambda": lam},
+        "config": headline_config(N, L_v, lam, args.batch, args.gpus),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
@@ -828,10 +835,7 @@ def run_ours(args):
         "headline_path": headline, "fp32_plain": fp32_line,
         "dtype": "fp32 (FP64 moments and conservation)", "data": "synthetic",
         "config": {
-            "workload": (f"0D hard spheres (lambda=1), N={N}, L_v={L_v}, discontinuous "
-                         f"two-Maxwellian +-5% jitter, {B} instances per GPU"),
-            "N": N, "L_v": L_v, "lambda": lam, "batch_per_gpu": B,
-            "parallelism": f"{world} independent GPU(s), instances sharded",
+            **headline_config(N, L_v, lam, B, world),
             "l2": (f"inputs larger than L2 (weight table {w_bytes / 1e9:.2f} GB, f "
                    f"{8 * B * n3 / 1e6:.0f} MB)"),
             "tuning": {"variant": tuned[0], "bg": tuned[1], "zs": tuned[2],
