@@ -531,7 +531,7 @@ def run_bkw(args):
     """Config 1: 0D Maxwell molecules, N=16, L_v=5, one BKW instance (K=0.65),
     dt = 0.01, 200 RK2 steps of the plain FP64 operator with maxPreserve and
     conservation, one CUDA graph per step; the analytic BKW solution
-    (K(t) = 1 - exp(-t/6), initializer.c:121-135) judges the result."""
+    (K(t) = 1 - exp(-t/6), initializer.c:121-135) is the check on the result."""
     import math
     import torch
     import spectralbte_gb300 as sb

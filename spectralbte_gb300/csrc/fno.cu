@@ -1,7 +1,8 @@
 // fno.cu -- the learned collision operator: a Fourier neural operator that
 // maps f to Q(f) on the velocity grid, trained and evaluated on the device
-// with BF16 tensor-core GEMMs and FP32 accumulation.  The reference has no
-// counterpart; its judge is the plain operator of this library.
+// with 16-bit (FP16 or BF16) tensor-core GEMMs and FP32 accumulation.  The
+// reference has no counterpart; its accuracy is measured against the plain
+// operator of this library.
 //
 // Network, per instance (f on the N^3 grid, p a grid point, c, d channels):
 //   x(p)   = f(p) / s,  s = max_p f(p)                (Q is bilinear in f)
