@@ -445,6 +445,7 @@ def run_learned(args, plan, fd, Qd, B, flags, peaks):
     return {
         "network": {"N": net.N, "width": net.width, "modes": net.modes, "layers": net.layers,
                     "hidden": net.hidden, "params": net.nparams,
+                    "elements": "fp16" if net.precision == 1 else "bf16",
                     "checkpoint": os.path.relpath(path, ROOT)},
         "value": B / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
         "kernel_launches_per_step": launches,
@@ -822,7 +823,10 @@ def run_ours(args):
     headline = "plain FP32 operator (every instance within rel-L2 1e-3)"
     h_value, h_e2e, h_ms = value, e2e_value, ms_total / args.steps
     h_launches, h_clk = launches, clk
+    h_dtype = "fp32 (FP64 moments and conservation)"
     if learned and learned.get("accepted") and world == 1:
+        h_dtype = (f"{learned['network']['elements']} network GEMMs with fp32 accumulation, "
+                   f"fp32 spot check, fp64 conservation projection")
         sc = learned["spot_checked"]
         headline = ("FP32+learned: the network with a plain-FP32 spot check each batch "
                     "(fallback on failure); network rel-L2 <= 1e-3 on every instance here")
@@ -833,7 +837,7 @@ def run_ours(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": h_ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "headline_path": headline, "fp32_plain": fp32_line,
-        "dtype": "fp32 (FP64 moments and conservation)", "data": "synthetic",
+        "dtype": h_dtype, "data": "synthetic",
         "config": {
             **headline_config(N, L_v, lam, B, world),
             "l2": (f"inputs larger than L2 (weight table {w_bytes / 1e9:.2f} GB, f "
