@@ -66,6 +66,8 @@ def lib() -> C.CDLL:
             "oracle_ghat_integral": (d, [d, d, d, d, d]),
             "oracle_gauss_legendre": (None, [i, _dp, _dp]),
             "oracle_weights_iso": (None, [i, _dp, d, d, d, d, d, d, i, i, _dp, i]),
+            "oracle_weights_iso_closed": (None, [i, _dp, d, d, d, d, d, d, i, i, _dp, i]),
+            "oracle_ghat_closed": (d, [d, d, d, d, d]),
             "oracle_weights_landau": (None, [i, _dp, d, d, i, i, _dp]),
             "oracle_ghat3l": (d, [d, d, d, d, d, d, d, d]),
             "oracle_run_0d": (None, [i, d, _dp, _dp, d, d, i, i, i, _dp, i]),
@@ -199,13 +201,14 @@ def qhat_rows(g: Grid, W_rows: np.ndarray, row0: int, fhat: np.ndarray,
 
 
 def weights_iso(g: Grid, lam: float, rows=None, d_i=2.0, d_j=2.0, m_i=1.0,
-                m_j=1.0, nthreads: int = 0) -> np.ndarray:
-    """Rows of the isotropic weights (weights.c:265-281); default all."""
+                m_j=1.0, nthreads: int = 0, closed: bool = False) -> np.ndarray:
+    """Rows of the isotropic weights (weights.c:265-281); default all.
+    closed=True evaluates the radial integral in closed form (lambda 0, 1)."""
     n3 = g.n3
     r0, r1 = (0, n3) if rows is None else rows
     W = np.zeros((r1 - r0, n3))
-    lib().oracle_weights_iso(g.N, _p(g.zeta), g.L_v, float(lam), d_i, d_j,
-                             m_i, m_j, r0, r1, _p(W), nthreads)
+    fn = lib().oracle_weights_iso_closed if closed else lib().oracle_weights_iso
+    fn(g.N, _p(g.zeta), g.L_v, float(lam), d_i, d_j, m_i, m_j, r0, r1, _p(W), nthreads)
     return W
 
 

@@ -579,9 +579,73 @@ double oracle_ghat_integral(double a0, double a1, double a2, double lambda,
     return result;
 }
 
-void oracle_weights_iso(int N, const double *zeta, double L_v, double lambda,
-                        double d_i, double d_j, double m_i, double m_j,
-                        int row_begin, int row_end, double *W, int nthreads)
+/* Closed forms of the radial integral of ghat (weights.c:156-160) for
+   lambda = 0 and 1, derived here from the integrand (the reference
+   integrates it numerically, weights.c:203).  With s(x) = sin x / x and
+   q(x) = (1 - cos x) / x^2 = s(x/2)^2 / 2 (no cancellation at small x):
+     gain, lambda = 0:  int_0^L r^2 s(ra) s(rb) dr = L / (2ab) [s(Ld) - s(Le)]
+     gain, lambda = 1:  int_0^L r^3 s(ra) s(rb) dr
+                          = L^2 / (2ab) [s(Ld) - q(Ld) - s(Le) + q(Le)]
+       with d = a - b, e = a + b (from 2 sin A sin B = cos(A-B) - cos(A+B)
+       and int_0^L r cos(rk) dr = L^2 [s(Lk) - q(Lk)]);
+     loss, lambda = 0:  int_0^L r^2 s(rc) dr = (sin x - x cos x) / c^3
+     loss, lambda = 1:  int_0^L r^3 s(rc) dr = ((2 - x^2) cos x + 2x sin x - 2) / c^4
+       with x = Lc; below x = 1/2 the loss uses its series
+       L^(lambda+3) sum_k (-1)^k x^(2k) / ((2k+1)! (2k+lambda+3)).
+   A gain argument of exactly 0 turns the gain into the loss form of the
+   other argument (s = 1).  A gain argument that is nonzero but below 1/2 / L
+   would lose digits in 1/(ab): such entries (none on the grids of this
+   project) and every other lambda use the quadrature. */
+static double loss_closed(double c, int lam, double L)
+{
+    const double x = L * c;
+    const double Lp = lam == 0 ? L * L * L : L * L * L * L;
+    if (x < 0.5) {
+        double term = 1.0, sum = 0.0;  /* term = (-1)^k x^(2k) / (2k+1)! */
+        for (int k = 0; k < 12; k++) {
+            sum += term / (2.0 * k + lam + 3.0);
+            term *= -x * x / ((2.0 * k + 2.0) * (2.0 * k + 3.0));
+        }
+        return Lp * sum;
+    }
+    const double sx = sin(x), cx = cos(x);
+    if (lam == 0) return (sx - x * cx) / (c * c * c);
+    return ((2.0 - x * x) * cx + 2.0 * x * sx - 2.0) / (c * c * c * c);
+}
+
+static double q_stable(double x)
+{
+    const double h = sinc_ref(0.5 * x);
+    return 0.5 * h * h;
+}
+
+double oracle_ghat_closed(double a0, double a1, double a2, double lambda, double L_v)
+{
+    const int lam = (lambda == 0.0) ? 0 : (lambda == 1.0 ? 1 : -1);
+    const double small = 0.5 / L_v;
+    if (lam < 0 || (a0 != 0.0 && a0 < small) || (a2 != 0.0 && a2 < small))
+        return oracle_ghat_integral(a0, a1, a2, lambda, L_v);
+    double gain;
+    if (a0 == 0.0 && a2 == 0.0)
+        gain = (lam == 0 ? L_v * L_v * L_v / 3.0 : L_v * L_v * L_v * L_v / 4.0);
+    else if (a0 == 0.0)
+        gain = loss_closed(a2, lam, L_v);
+    else if (a2 == 0.0)
+        gain = loss_closed(a0, lam, L_v);
+    else {
+        const double d = L_v * (a0 - a2), e = L_v * (a0 + a2);
+        if (lam == 0)
+            gain = L_v / (2.0 * a0 * a2) * (sinc_ref(d) - sinc_ref(e));
+        else
+            gain = L_v * L_v / (2.0 * a0 * a2) *
+                   (sinc_ref(d) - q_stable(d) - sinc_ref(e) + q_stable(e));
+    }
+    return gain - loss_closed(a1, lam, L_v);
+}
+
+static void weights_iso_rows(int N, const double *zeta, double L_v, double lambda,
+                             double d_i, double d_j, double m_i, double m_j,
+                             int row_begin, int row_end, double *W, int nthreads, int closed)
 {
     /* initialize_weights (weights.c:41-49) and generate_conv_weights_iso
        (weights.c:265-281) with gHat3 (weights.c:181-262) */
@@ -613,12 +677,29 @@ void oracle_weights_iso(int N, const double *zeta, double L_v, double lambda,
             double a1 = sqrt(k1 * k1 + k2 * k2 + k3 * k3);
             double a2 = sqrt((k1 - mu * z1) * (k1 - mu * z1) + (k2 - mu * z2) * (k2 - mu * z2) +
                              (k3 - mu * z3) * (k3 - mu * z3));
-            double g = prefactor * oracle_ghat_integral(a0, a1, a2, lambda, L_v);
+            double g = prefactor * (closed ? oracle_ghat_closed(a0, a1, a2, lambda, L_v)
+                                           : oracle_ghat_integral(a0, a1, a2, lambda, L_v));
             W[(row - row_begin) * n3 + col] =
                 wtN[l] * wtN[m] * wtN[n] * 0.25 * pow(0.5 * (d_i + d_j), 2) * g;
         }
     }
     free(wtN);
+}
+
+void oracle_weights_iso(int N, const double *zeta, double L_v, double lambda,
+                        double d_i, double d_j, double m_i, double m_j,
+                        int row_begin, int row_end, double *W, int nthreads)
+{
+    weights_iso_rows(N, zeta, L_v, lambda, d_i, d_j, m_i, m_j, row_begin, row_end, W,
+                     nthreads, 0);
+}
+
+void oracle_weights_iso_closed(int N, const double *zeta, double L_v, double lambda,
+                               double d_i, double d_j, double m_i, double m_j,
+                               int row_begin, int row_end, double *W, int nthreads)
+{
+    weights_iso_rows(N, zeta, L_v, lambda, d_i, d_j, m_i, m_j, row_begin, row_end, W,
+                     nthreads, 1);
 }
 
 /* -------------------------------------------------------------- 0D driver */

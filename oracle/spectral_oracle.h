@@ -123,6 +123,13 @@ double oracle_ghat_integral(double a0, double a1, double a2, double lambda,
 void oracle_weights_iso(int N, const double *zeta, double L_v, double lambda,
                         double d_i, double d_j, double m_i, double m_j,
                         int row_begin, int row_end, double *W, int nthreads);
+/* The same integral in closed form for lambda = 0 and 1 (quadrature for
+   other lambda and for nonzero gain arguments below 1/(2 L_v)), and the
+   weights built from it. */
+double oracle_ghat_closed(double a0, double a1, double a2, double lambda, double L_v);
+void oracle_weights_iso_closed(int N, const double *zeta, double L_v, double lambda,
+                               double d_i, double d_j, double m_i, double m_j,
+                               int row_begin, int row_end, double *W, int nthreads);
 
 /* ---- 0D driver (exec/boltz.c:186-250, output.c:159-213) ---------------- */
 /* Runs nT steps of the homogeneous solver for one species with the

@@ -158,3 +158,44 @@ def test_landau_weights_ignore_glance_in_reference():
     assert np.array_equal(d["g4_W"], d["n4_W"])
     assert str(d["g4_file"]) == "Weights/N4_AnIso_L_v4_lambda0_glance0.3.wts"
     assert str(d["n4_file"]) == "Weights/N4_Aniso_L_v4_lambda0_Landau.wts"
+
+
+@pytest.mark.parametrize("tag,L_v,kind,lam", [("bkw8", 5.0, "0d", 0.0),
+                                              ("heat", 9.0, "1d", 1.0)])
+def test_closed_form_weights_match_reference_fixture(oracle, golden_w, tag, L_v, kind, lam):
+    """The radial integral of ghat (weights.c:156-160) in closed form for
+    lambda = 0 and 1 against the reference's own .wts fixtures (the same
+    bounds as the quadrature) and against the quadrature itself."""
+    g = oracle.Grid(8, L_v, kind)
+    W = oracle.weights_iso(g, lam, closed=True)
+    rows = golden_w[f"{tag}_row_index"]
+    assert rel_l2(W[rows], golden_w[f"{tag}_rows"]) < 1e-13
+    assert abs(W.sum() - golden_w[f"{tag}_sum"]) <= 1e-12 * golden_w[f"{tag}_abssum"]
+    assert abs((W * W).sum() / golden_w[f"{tag}_sumsq"] - 1) < 1e-13
+    assert rel_l2(W, oracle.weights_iso(g, lam)) < 1e-14
+
+
+@pytest.mark.parametrize("N,L_v,lam", [(16, 5.0, 0.0), (24, 6.0, 1.0), (32, 6.0, 1.0)])
+def test_closed_form_weights_match_quadrature_rows(oracle, N, L_v, lam):
+    """Sampled rows at the bench grids: closed form against the converged
+    composite Gauss-Legendre quadrature."""
+    g = oracle.Grid(N, L_v, "0d")
+    n3 = N ** 3
+    for r0 in (0, n3 // 2 + N // 3, n3 - 2):
+        a = oracle.weights_iso(g, lam, rows=(r0, r0 + 2), closed=True)
+        b = oracle.weights_iso(g, lam, rows=(r0, r0 + 2))
+        assert rel_l2(a, b) < 1e-13, r0
+
+
+def test_closed_form_limits():
+    """Exact zero arguments, the small-argument loss series, and a lambda
+    without a closed form (quadrature) against the quadrature."""
+    from oracle import pyoracle as po
+    L = po.lib()
+    cases = [(0.0, 0.0, 0.0), (0.0, 0.4, 0.9), (0.8, 0.0, 0.6), (0.4, 1.3, 0.0),
+             (0.55, 0.01, 0.55), (0.3, 0.7, 1.1), (2.0, 3.0, 1.7), (0.02, 0.3, 0.5)]
+    for lam in (0.0, 1.0, 0.5):
+        for a0, a1, a2 in cases:
+            q = L.oracle_ghat_integral(a0, a1, a2, lam, 6.0)
+            c = L.oracle_ghat_closed(a0, a1, a2, lam, 6.0)
+            assert abs(c - q) <= 1e-13 * max(abs(q), 1.0), (lam, a0, a1, a2, q, c)
