@@ -44,10 +44,10 @@ N_DEF, LV_DEF, LAM_DEF = 32, 6.0, 1.0
 # at the maximum SM clock.
 N_SM, FP32_LANES = 152, 128
 # DRAM bytes (read + write) of one convolution launch measured by ncu at
-# N=24, B=128, per kernel variant: the block-barrier kernel (variant 1, bg=64,
-# profiles/conv_f32_n24_b128_ncu.md) and the warp-specialised kernel
-# (variants 2-4, bg=32, profiles/conv_ws_n24_b128_ncu.md).  W streams once
-# per instance group, so traffic scales with N^6 times the number of groups.
+# N=24, B=128, per kernel variant: the block-barrier kernel (variant 1,
+# bg=64) and the warp-specialised kernel (variants 2-4, bg=32).  W streams
+# once per instance group, so traffic scales with N^6 times the number of
+# groups.
 NCU_TRAFFIC = {
     1: {"bytes": 1.691575e9 + 66.592768e6, "N": 24, "B": 128, "bg": 64,
         "kernel": "conv_f32_kernel"},
@@ -55,13 +55,13 @@ NCU_TRAFFIC = {
         "kernel": "conv_ws_kernel"},
 }
 # The same kernel in its symmetric (row-pair) form streams the partner-summed
-# table, N^2 (N^4 + N^2)/2 FP32 values (profiles/conv_ws_sym_n24_b128_ncu.md).
+# table, N^2 (N^4 + N^2)/2 FP32 values (ncu at N=24, B=128, bg=32).
 NCU_TRAFFIC_SYM = {
     3: {"bytes": 1.551603e9 + 45.4912e6, "N": 24, "B": 128, "bg": 32,
         "kernel": "conv_ws_kernel (row-pair form)"},
 }
 # DRAM bytes (read + write) of one channel-mix launch of the learned operator
-# at 256 instances (profiles/learned_layer0_n32_b256_ncu.md, capture 1).
+# at 256 instances, measured by ncu on the network alone at N=32.
 LEARNED_CM_TRAFFIC = {"bytes": 2.15e9 + 1.04e9, "B": 256}
 KERNEL_NAME = {1: "conv_f32_kernel", 2: "conv_ws_kernel", 3: "conv_ws_kernel",
                4: "conv_x4_kernel", 5: "conv_ws_kernel"}
@@ -472,7 +472,7 @@ def run_learned(args, plan, fd, Qd, B, flags, peaks):
                      "launch_ms": cm_avg * 1e3, "launches_timed": cm_n,
                      "traffic_note": (f"ncu dram bytes of the same kernel at "
                                       f"{LEARNED_CM_TRAFFIC['B']} instances "
-                                      f"(profiles/learned_layer0_n32_b256_ncu.md), scaled by "
+                                      f"(ncu capture of the network alone at N=32), scaled by "
                                       f"instances"),
                      "aggregate": {"achieved": gbs, "frac": gbs / float(peaks["hbm_gbs"]),
                                    "unit": "GB/s", "algorithmic_bytes_per_eval": w["bytes"],

@@ -250,9 +250,21 @@ int spectral_plan_autotune(spectral_plan *plan, int B, int flags,
    every row with the plain tiled weights. */
 int spectral_plan_set_symmetric(spectral_plan *plan, int on);
 
-/* Device status word of the last call: bit 0 = a bounded device wait gave
-   up, bit 1 = non-finite output.  Cleared by the read. */
+/* Device status word of the calls since the last read: bit 0 = a bounded
+   device wait gave up (the kernel then left early and its output is not
+   valid), bit 1 = a non-finite moment sum (NaN or infinity in f or Q; set by
+   the conservation, Maxwellian-split and moment kernels).  Cleared by the
+   read.  No counterpart in the reference, which neither bounds its waits nor
+   checks for NaN. */
 int spectral_plan_status(spectral_plan *plan, unsigned int *status);
+/* Test hook of the bounded waits, no counterpart in the reference.  The next
+   FP32 convolution launch of the plan (warp-specialised variants 2, 3, 5)
+   skips the copies of pipeline slot `slot` in its first CTA, whose waits then
+   give up after limit_clocks (1e3 .. 2^31): that CTA's consumers wait on a
+   barrier that nothing completes, set bit 0 of the status word and leave,
+   and every other CTA runs normally.  One shot.  The call's result is not
+   valid; the plan stays usable. */
+int spectral_plan_inject_stall(spectral_plan *plan, int slot, long long limit_clocks);
 
 /* Convolution-kernel timing: with profiling on, every convolution launch
    is bracketed by CUDA events on its own stream; spectral_plan_conv_time
@@ -275,7 +287,11 @@ int spectral_plan_sync(spectral_plan *plan);
    the library holds until exit; N^2 + B*N^3 must not exceed 2,097,152
    complex values (N = 32: B <= 63), larger sizes return SPECTRAL_ERR_ARG.
    The first call on a device looks up the array's device address, so make
-   it before any stream capture.  All calls share the array and nothing in
+   it before any stream capture.  Under CUDA's lazy module loading (the
+   default since CUDA 12.2) the array comes into being when the library's
+   device code first loads on that device, which may be at that first call:
+   the call then takes the 32 MiB from device memory, so a host that pools
+   all device memory makes its first call before the pool takes it.  All calls share the array and nothing in
    it needs to start at zero; calls that overlap on the GPU race.  in_dev
    may equal out_dev.  Asynchronous on stream (NULL: default stream). */
 int spectral_fft3d_noalloc(int N, double L_v, const double *v,
@@ -364,11 +380,6 @@ int spectral_plan_set_learned(spectral_plan *plan, spectral_fno *net,
 int spectral_plan_learned_stats(spectral_plan *plan, long long *calls,
                                 long long *checks, long long *fallbacks,
                                 double *last_err);
-
-/* Roofline calibration: the FP32 FMA rate (TFLOP/s, FMA = 2 flop) that the
-   current GPU sustains on independent register FMA chains; the FP32
-   convolution's fraction of peak is reported against it. */
-int spectral_fp32_fma_rate(double *tflops, void *stream);
 
 /* Number of kernels the library launched since load (monotonic). */
 long long spectral_kernel_launches(void);

@@ -27,9 +27,10 @@ def build(quiet: bool = True) -> str:
     return os.path.join(HERE, "liboracle.so")
 
 
-def build_ref(ref_dir: str = "/root/reference") -> bool:
-    """Compile _ref/ from the reference sources if they are present."""
-    if not os.path.isdir(os.path.join(ref_dir, "src")):
+def build_ref(ref_dir: str) -> bool:
+    """Compile _ref/ from the reference sources in ref_dir, if they are
+    present there."""
+    if not ref_dir or not os.path.isdir(os.path.join(ref_dir, "src")):
         return False
     out = subprocess.run(["make", "-C", HERE, "ref", f"REF={ref_dir}"],
                          capture_output=True, text=True)

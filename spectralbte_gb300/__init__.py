@@ -136,6 +136,7 @@ def lib() -> C.CDLL:
         "spectral_plan_set_tuning": (i, [v, i, i, i, i, i]),
         "spectral_plan_autotune": (i, [v, i, i, C.POINTER(C.c_int)]),
         "spectral_plan_set_symmetric": (i, [v, i]),
+        "spectral_plan_inject_stall": (i, [v, i, C.c_longlong]),
         "spectral_plan_status": (i, [v, C.POINTER(C.c_uint)]),
         "spectral_plan_sync": (i, [v]),
         "spectral_plan_set_profiling": (i, [v, i]),
@@ -144,7 +145,6 @@ def lib() -> C.CDLL:
         "spectral_1d_advect": (i, [v, v, v, v]),
         "spectral_graph_capture": (i, [v, i, v, i, d, d, i, i]),
         "spectral_graph_launch": (i, [v, v]),
-        "spectral_fp32_fma_rate": (i, [_dp, v]),
         "spectral_group_computeQ": (i, [C.POINTER(C.c_void_p), i, C.POINTER(C.c_void_p),
                                         C.POINTER(C.c_void_p), C.POINTER(C.c_int), i, v]),
         "spectral_plan_conv_time": (i, [v, _dp, C.POINTER(C.c_int)]),
@@ -430,6 +430,13 @@ class Plan:
         _check(self.L.spectral_plan_autotune(self.h, B, flags, out), "autotune")
         return tuple(out)
 
+    def inject_stall(self, slot: int, limit_clocks: int):
+        """Test hook: the next FP32 convolution launch skips the copies of
+        pipeline slot `slot` in its first CTA, whose waits give up after
+        limit_clocks (spectral_plan_inject_stall)."""
+        _check(self.L.spectral_plan_inject_stall(self.h, int(slot), int(limit_clocks)),
+               "inject_stall")
+
     def status(self) -> int:
         s = C.c_uint()
         _check(self.L.spectral_plan_status(self.h, C.byref(s)), "status")
@@ -615,9 +622,20 @@ def group_computeQ(plans, fs, Qs, flags: int = FP32 | CONSERVE, stream: int = 0)
 
 
 def fp32_fma_rate() -> float:
-    """Sustained FP32 FMA rate of the current GPU in TFLOP/s (probe kernel)."""
+    """Sustained FP32 FMA rate of the current GPU in TFLOP/s, measured by the
+    benchmark's calibration library (libspectral_calib.so, a probe kernel of
+    independent register FMA chains); the collision library does not
+    contain it."""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libspectral_calib.so")
+    if not os.path.exists(path):
+        raise SpectralError(f"calibration library missing: {path} (run the build)")
+    cal = C.CDLL(path)
+    cal.spectral_calib_fp32_fma_rate.restype = C.c_int
+    cal.spectral_calib_fp32_fma_rate.argtypes = [_dp, C.c_void_p]
     out = C.c_double()
-    _check(lib().spectral_fp32_fma_rate(C.byref(out), _stream(0)), "spectral_fp32_fma_rate")
+    rc = cal.spectral_calib_fp32_fma_rate(C.byref(out), _stream(0))
+    if rc != 0:
+        raise SpectralError(f"spectral_calib_fp32_fma_rate: CUDA error {rc}")
     return out.value
 
 

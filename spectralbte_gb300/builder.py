@@ -1,8 +1,10 @@
 """Build libspectral_gb300.so in place with nvcc for sm_103a.
 
 Each translation unit compiles in parallel to an object under _build/; the
-objects then link into spectralbte_gb300/libspectral_gb300.so.  No CMake is
-involved, and building needs no GPU.
+objects then link into spectralbte_gb300/libspectral_gb300.so.  The
+benchmark's FP32 FMA-rate probe (calib/fma_probe.cu) links into a library of
+its own, libspectral_calib.so, so the collision library carries no
+calibration code.  No CMake is involved, and building needs no GPU.
 """
 from __future__ import annotations
 
@@ -18,7 +20,9 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libspectral_gb300.so")
 
 SOURCES = ["fft3d.cu", "conv.cu", "conv_ws.cu", "conserve.cu", "weights.cu", "transport.cu",
-           "capi.cu", "noalloc.cu", "probe.cu", "fno.cu"]
+           "capi.cu", "noalloc.cu", "fno.cu"]
+CALIB_SRC = os.path.join(HERE, "calib", "fma_probe.cu")
+CALIB_LIB = os.path.join(HERE, "libspectral_calib.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
          "-Xcompiler", "-fvisibility=default"]
@@ -33,8 +37,9 @@ def nvcc() -> str:
 
 
 def _compile(src: str, extra: list[str]) -> str:
-    obj = os.path.join(OUT, os.path.splitext(src)[0] + ".o")
-    cmd = [nvcc(), *ARCH, *FLAGS, *extra, "-c", os.path.join(CSRC, src), "-o", obj]
+    path = src if os.path.isabs(src) else os.path.join(CSRC, src)
+    obj = os.path.join(OUT, os.path.splitext(os.path.basename(src))[0] + ".o")
+    cmd = [nvcc(), *ARCH, *FLAGS, *extra, "-c", path, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
@@ -42,7 +47,9 @@ def _compile(src: str, extra: list[str]) -> str:
 
 
 def _stale(objs: list[str]) -> bool:
-    if not os.path.exists(LIB):
+    if not os.path.exists(LIB) or not os.path.exists(CALIB_LIB):
+        return True
+    if os.path.getmtime(CALIB_SRC) > os.path.getmtime(CALIB_LIB):
         return True
     t = os.path.getmtime(LIB)
     deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
@@ -56,14 +63,15 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
     os.makedirs(OUT, exist_ok=True)
     if not force and not _stale([]):
         return LIB
-    with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        objs = list(ex.map(lambda s: _compile(s, extra), SOURCES))
-    tmp = LIB + ".tmp"
-    cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
+    with cf.ThreadPoolExecutor(max_workers=len(SOURCES) + 1) as ex:
+        objs = list(ex.map(lambda s: _compile(s, extra), SOURCES + [CALIB_SRC]))
+    for lib, parts in ((LIB, objs[:-1]), (CALIB_LIB, objs[-1:])):
+        tmp = lib + ".tmp"
+        cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *parts, "-lcudart"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+        os.replace(tmp, lib)
     if verbose:
         print("built", LIB)
     return LIB

@@ -220,7 +220,11 @@ static int build_conservation(ConsParams &cp, int N, double dv, const double *v,
             }
         }
         cp.pivot[k] = i0;
-        if (cc[k] == 0.0) {
+        // conserve.c:130-135 exits when the best scaled pivot is 0.  A zero
+        // row scale (e.g. mass 0) makes it 0/0 = NaN, which that test lets
+        // through; NaN is singular here too.  For any regular matrix the two
+        // tests agree, so the factors are the reference's.
+        if (!(cc[k] > 0.0)) {
             set_error(kErrSingular, "conservation matrix CC^T is singular");
             return kErrSingular;
         }
@@ -482,6 +486,10 @@ struct spectral_plan_s {
     ConvF32Config tune{64, 3, 16};
     int sym = 1;  // symmetric convolution form for variants 2, 3 (g = f)
     unsigned int *d_status = nullptr;
+    // bounded-wait test hook for the next FP32 convolution launch
+    // (spectral_plan_inject_stall); one shot
+    int stall_slot = -1;
+    long long stall_limit = 0;
     // FP64 scratch: capacity cap64 instances
     int cap64 = 0;
     double2 *c64[6] = {};  // fhat, ghat, R, S(=Mhat), T, qhat
@@ -719,9 +727,9 @@ static int q_fp64(spectral_plan_s *p, const WeightsDev &W, const double *fdev,
         double *Mi = p->r64[0], *gi = p->r64[1], *Mj = p->r64[2], *gj = p->r64[3];
         // find_maxwellians (collisions.c:181-182): both g's subtract M_i
         SBTE_LAUNCH(maxwellian_split(fdev, Mi, gi, nullptr, B, N, p->d_v, p->mom_mass,
-                                     p->mom_KB, nullptr, st), 1);
+                                     p->mom_KB, nullptr, st, p->d_status), 1);
         SBTE_LAUNCH(maxwellian_split(gdev, Mj, gj, Mi, B, N, p->d_v, p->mom_mass,
-                                     p->mom_KB, nullptr, st), 1);
+                                     p->mom_KB, nullptr, st, p->d_status), 1);
         // Q(M_i,g_j) + Q(g_i,M_j) + Q(g_i,g_j) in one W pass:
         //   sum W [ghat_j (Mhat_i + ghat_i)[idx] + Mhat_j ghat_i[idx]]
         SBTE_LAUNCH(dft3_f64(Mi, DftIn::kRealF64, 1, p->tmp64, A, DftOut::kComplexF64, 1,
@@ -792,6 +800,16 @@ static int q_fp32(spectral_plan_s *p, const double *fdev, double *Qdev, int B,
     ConvF32Config cfg;
     const float *Wt = nullptr;
     SBTE_TRY(resolve_f32(p, maxpreserve, cfg, Wt, st));
+    if (p->stall_slot >= 0) {
+        if (cfg.variant != 2 && cfg.variant != 3 && cfg.variant != 5) {
+            p->stall_slot = -1;
+            set_error(kErrUnsupported, "stall test hook: needs convolution variant 2, 3 or 5");
+            return kErrUnsupported;
+        }
+        cfg.stall_slot = p->stall_slot;
+        cfg.stall_limit = p->stall_limit;
+        p->stall_slot = -1;
+    }
     const int bg = cfg.bg;
     const int groups = (B + bg - 1) / bg;
     const float pf_f = (float)p->pf_fwd, pf_i = (float)p->pf_inv;
@@ -803,7 +821,7 @@ static int q_fp32(spectral_plan_s *p, const double *fdev, double *Qdev, int B,
         if (maxpreserve) {
             double *M = p->r32[0], *g = p->r32[1];
             SBTE_LAUNCH(maxwellian_split(fdev, M, g, nullptr, B, N, p->d_v, p->mom_mass,
-                                         p->mom_KB, nullptr, st), 1);
+                                         p->mom_KB, nullptr, st, p->d_status), 1);
             SBTE_LAUNCH(dft3_f32(M, DftIn::kRealF64, 1, p->tmp32, S4, DftOut::kG4, bg,
                                  p->Dfwd32, pf_f, N, B, st), 2);
             gsrc = g;
@@ -840,7 +858,7 @@ static int q_fp32(spectral_plan_s *p, const double *fdev, double *Qdev, int B,
     } else {
         double *M = p->r32[0], *g = p->r32[1];
         SBTE_LAUNCH(maxwellian_split(fdev, M, g, nullptr, B, N, p->d_v, p->mom_mass,
-                                     p->mom_KB, nullptr, st), 1);
+                                     p->mom_KB, nullptr, st, p->d_status), 1);
         // P = ghat, R = fhat (= Mhat + ghat), S = Mhat, T = ghat
         SBTE_LAUNCH(dft3_f32(g, DftIn::kRealF64, 1, p->tmp32, P, DftOut::kComplexF32, bg,
                              p->Dfwd32, pf_f, N, B, st), 2);
@@ -887,7 +905,7 @@ static int learned_q(spectral_plan_s *p, const double *f, double *Q, int B, int 
         return computeQ_dev(p, f, Q, B, plain, st);
     }
     SBTE_TRY(fno_predict(p->fno, f, Q, B, st));
-    SBTE_LAUNCH(conserve_batch(Q, B, p->d_v, p->cons, st), 1);
+    SBTE_LAUNCH(conserve_batch(Q, B, p->d_v, p->cons, st, p->d_status), 1);
     if (!check) return kOk;
     if (!p->lq) {
         SBTE_TRY(dalloc(&p->lq, n3));
@@ -895,7 +913,7 @@ static int learned_q(spectral_plan_s *p, const double *f, double *Q, int B, int 
     }
     const int b = (int)((p->lchecks++) % B);
     SBTE_TRY(q_fp32(p, f + (long long)b * n3, p->lq, 1, false, st));
-    SBTE_LAUNCH(conserve_batch(p->lq, 1, p->d_v, p->cons, st), 1);
+    SBTE_LAUNCH(conserve_batch(p->lq, 1, p->d_v, p->cons, st, p->d_status), 1);
     SBTE_TRY(rel_l2_device(Q + (long long)b * n3, p->lq, n3, p->d_lerr, st));
     SBTE_CUDA(cudaMemcpyAsync(&p->lerr, p->d_lerr, sizeof(double), cudaMemcpyDeviceToHost, st));
     SBTE_CUDA(cudaStreamSynchronize(st));
@@ -923,7 +941,7 @@ static int computeQ_dev(spectral_plan_s *p, const double *f, double *Q, int B,
         SBTE_TRY(q_fp32(p, f, Q, B, mp, st));
     else
         SBTE_TRY(q_fp64(p, p->W, f, f, Q, B, mp, st));
-    if (flags & SPECTRAL_CONSERVE) SBTE_LAUNCH(conserve_batch(Q, B, p->d_v, p->cons, st), 1);
+    if (flags & SPECTRAL_CONSERVE) SBTE_LAUNCH(conserve_batch(Q, B, p->d_v, p->cons, st, p->d_status), 1);
     return kOk;
 }
 
@@ -1107,31 +1125,45 @@ int spectral_computeQ_host(spectral_plan *p, const double *f_host, double *Q_hos
         p->host_events.push_back(e);
     }
     const long long n3 = p->n3;
-    for (int c = 0; c < nch; c++) {
-        const long long b0 = (long long)c * chunk;
-        const int nb = (int)std::min<long long>(chunk, B - b0);
-        const size_t bytes = sizeof(double) * (size_t)nb * n3;
-        cudaEvent_t in = p->host_events[2 * c], done = p->host_events[2 * c + 1];
-        SBTE_CUDA(cudaMemcpyAsync(p->d_fh + b0 * n3, f_host + b0 * n3, bytes,
-                                  cudaMemcpyHostToDevice, p->copy_in));
-        SBTE_CUDA(cudaEventRecord(in, p->copy_in));
-        SBTE_CUDA(cudaStreamWaitEvent(p->stream, in, 0));
-        SBTE_TRY(computeQ_dev(p, p->d_fh + b0 * n3, p->d_Qh + b0 * n3, nb, flags, p->stream));
-        SBTE_CUDA(cudaEventRecord(done, p->stream));
-        SBTE_CUDA(cudaStreamWaitEvent(p->copy_out, done, 0));
-        SBTE_CUDA(cudaMemcpyAsync(Q_host + b0 * n3, p->d_Qh + b0 * n3, bytes,
-                                  cudaMemcpyDeviceToHost, p->copy_out));
+    auto run_chunks = [&]() -> int {
+        for (int c = 0; c < nch; c++) {
+            const long long b0 = (long long)c * chunk;
+            const int nb = (int)std::min<long long>(chunk, B - b0);
+            const size_t bytes = sizeof(double) * (size_t)nb * n3;
+            cudaEvent_t in = p->host_events[2 * c], done = p->host_events[2 * c + 1];
+            SBTE_CUDA(cudaMemcpyAsync(p->d_fh + b0 * n3, f_host + b0 * n3, bytes,
+                                      cudaMemcpyHostToDevice, p->copy_in));
+            SBTE_CUDA(cudaEventRecord(in, p->copy_in));
+            SBTE_CUDA(cudaStreamWaitEvent(p->stream, in, 0));
+            SBTE_TRY(computeQ_dev(p, p->d_fh + b0 * n3, p->d_Qh + b0 * n3, nb, flags,
+                                  p->stream));
+            SBTE_CUDA(cudaEventRecord(done, p->stream));
+            SBTE_CUDA(cudaStreamWaitEvent(p->copy_out, done, 0));
+            SBTE_CUDA(cudaMemcpyAsync(Q_host + b0 * n3, p->d_Qh + b0 * n3, bytes,
+                                      cudaMemcpyDeviceToHost, p->copy_out));
+        }
+        SBTE_CUDA(cudaStreamSynchronize(p->copy_out));
+        SBTE_CUDA(cudaStreamSynchronize(p->stream));
+        return kOk;
+    };
+    const int rc = run_chunks();
+    if (rc != kOk) {
+        // Copies into and out of the caller's host buffers may still be
+        // queued: finish them before returning, so the caller may free the
+        // buffers as soon as the call returns (their errors are not the
+        // first one and are not reported).
+        cudaStreamSynchronize(p->copy_in);
+        cudaStreamSynchronize(p->stream);
+        cudaStreamSynchronize(p->copy_out);
     }
-    SBTE_CUDA(cudaStreamSynchronize(p->copy_out));
-    SBTE_CUDA(cudaStreamSynchronize(p->stream));
-    return kOk;
+    return rc;
 }
 
 int spectral_conserve_device(spectral_plan *p, double *Q_dev, int B, void *stream)
 {
     if (!p || !Q_dev || B < 1) return set_error(kErrArg, "bad arguments"), kErrArg;
     cudaStream_t st = (cudaStream_t)stream;  // NULL: the default stream
-    SBTE_LAUNCH(conserve_batch(Q_dev, B, p->d_v, p->cons, st), 1);
+    SBTE_LAUNCH(conserve_batch(Q_dev, B, p->d_v, p->cons, st, p->d_status), 1);
     return kOk;
 }
 
@@ -1342,6 +1374,16 @@ int spectral_plan_set_symmetric(spectral_plan *p, int on)
     return kOk;
 }
 
+int spectral_plan_inject_stall(spectral_plan *p, int slot, long long limit_clocks)
+{
+    if (!p || slot < 0 || limit_clocks < 1000 || limit_clocks > (1LL << 31))
+        return set_error(kErrArg, "inject_stall: slot >= 0, limit in [1e3, 2^31] clocks"),
+               kErrArg;
+    p->stall_slot = slot;
+    p->stall_limit = limit_clocks;
+    return kOk;
+}
+
 int spectral_plan_autotune(spectral_plan *p, int B, int flags, int *chosen)
 {
     if (!p || B < 1) return set_error(kErrArg, "bad arguments"), kErrArg;
@@ -1464,7 +1506,7 @@ int spectral_moments_device(spectral_plan *p, const double *f_dev, int B, double
     }
     SBTE_CUDA(cudaSetDevice(p->device));
     SBTE_LAUNCH(moments_batch(f_dev, B, p->N, p->d_v, p->mom_mass, p->mom_KB, out_dev,
-                              (cudaStream_t)stream), 1);
+                              (cudaStream_t)stream, p->d_status), 1);
     return kOk;
 }
 
@@ -1526,6 +1568,7 @@ struct LegacyCons {
     double *d_v = nullptr;
     double *d_Q = nullptr;
     double **d_ptrs = nullptr;
+    unsigned int *d_status = nullptr;  // kStatusNonFinite from the projection
     size_t capQ = 0;
 };
 struct LegacyWeights {
@@ -1752,6 +1795,7 @@ void dealloc_conservation(void)
     dfree(g_cons.d_v);
     dfree(g_cons.d_Q);
     dfree(g_cons.d_ptrs);
+    dfree(g_cons.d_status);
     g_cons.capQ = 0;
 }
 
@@ -1806,6 +1850,11 @@ void conserveAllMoments(double **Q)
             (rc = dalloc(&g_cons.d_ptrs, (size_t)Ns * Ns)) == kOk)
             g_cons.capQ = need;
     }
+    if (rc == kOk && !g_cons.d_status) {
+        rc = dalloc(&g_cons.d_status, 1);
+        if (rc == kOk && cudaMemset(g_cons.d_status, 0, sizeof(unsigned)) != cudaSuccess)
+            rc = kErrCuda;
+    }
     std::vector<double *> ptrs(Ns * Ns);
     for (int a = 0; a < Ns * Ns && rc == kOk; a++) {
         ptrs[a] = g_cons.d_Q + a * n3;
@@ -1816,11 +1865,12 @@ void conserveAllMoments(double **Q)
     if (rc == kOk) {
         cudaError_t e;
         if (Ns == 1) {
-            e = conserve_batch(g_cons.d_Q, 1, g_cons.d_v, g_cons.cp, st);
+            e = conserve_batch(g_cons.d_Q, 1, g_cons.d_v, g_cons.cp, st, g_cons.d_status);
         } else {
             e = cudaMemcpyAsync(g_cons.d_ptrs, ptrs.data(), sizeof(double *) * Ns * Ns,
                                 cudaMemcpyHostToDevice, st);
-            if (e == cudaSuccess) e = conserve_species(g_cons.d_ptrs, g_cons.d_v, g_cons.cp, st);
+            if (e == cudaSuccess)
+                e = conserve_species(g_cons.d_ptrs, g_cons.d_v, g_cons.cp, st, g_cons.d_status);
         }
         if (e != cudaSuccess) rc = kErrCuda;
         else count(1);
@@ -1830,6 +1880,18 @@ void conserveAllMoments(double **Q)
             cudaSuccess)
             rc = kErrCuda;
     if (rc == kOk && cudaStreamSynchronize(st) != cudaSuccess) rc = kErrCuda;
+    unsigned int flags = 0;
+    if (rc == kOk &&
+        cudaMemcpy(&flags, g_cons.d_status, sizeof(unsigned), cudaMemcpyDeviceToHost) ==
+            cudaSuccess &&
+        flags != 0) {
+        // Q held a NaN or an infinity: the projection cannot conserve it.
+        // The reference would carry on with NaN; here the caller is told.
+        cudaMemset(g_cons.d_status, 0, sizeof(unsigned));
+        set_error(kErrNonFinite, "conserveAllMoments: non-finite moments of Q");
+        report("conserveAllMoments");
+        return;
+    }
     if (rc != kOk) {
         if (last_error() == kOk || rc == kErrCuda)
             set_error(rc, "conserveAllMoments: %s", cudaGetErrorString(cudaGetLastError()));

@@ -65,7 +65,7 @@ __device__ void solve_cct(const ConsParams &cp, double *b)
 // One species, one CTA per instance.
 __global__ void __launch_bounds__(kThreads)
 conserve_batch_kernel(double *__restrict__ Q, const double *__restrict__ v,
-                      ConsParams cp)
+                      ConsParams cp, unsigned int *__restrict__ status)
 {
     __shared__ double red[32 * 5];
     __shared__ double lam[8];
@@ -89,7 +89,13 @@ conserve_batch_kernel(double *__restrict__ Q, const double *__restrict__ v,
         double b[8];
         for (int t = 0; t < 5; t++) b[t] = m[t];
         solve_cct(cp, b);
-        for (int t = 0; t < 5; t++) lam[t] = b[t];
+        bool finite = true;
+        for (int t = 0; t < 5; t++) {
+            lam[t] = b[t];
+            finite = finite && isfinite(m[t]) && isfinite(b[t]);
+        }
+        // A NaN or infinity anywhere in Q reaches its moment sums.
+        if (!finite && status) atomicOr(status, kStatusNonFinite);
     }
     __syncthreads();
     const double l0 = lam[0], l1 = lam[1], l2 = lam[2], l3 = lam[3], l4 = lam[4];
@@ -106,7 +112,7 @@ conserve_batch_kernel(double *__restrict__ Q, const double *__restrict__ v,
 // Ns species (Ns <= 4), a single instance; Qp[n*Ns+m] are N^3 arrays.
 __global__ void __launch_bounds__(kThreads)
 conserve_species_kernel(double **__restrict__ Qp, const double *__restrict__ v,
-                        ConsParams cp)
+                        ConsParams cp, unsigned int *__restrict__ status)
 {
     __shared__ double red[32 * 8];
     __shared__ double lam[8];
@@ -136,7 +142,12 @@ conserve_species_kernel(double **__restrict__ Qp, const double *__restrict__ v,
         double b[8];
         for (int t = 0; t < 8; t++) b[t] = m[t];
         solve_cct(cp, b);
-        for (int t = 0; t < 8; t++) lam[t] = b[t];
+        bool finite = true;
+        for (int t = 0; t < 8; t++) {
+            lam[t] = b[t];
+            if (t < Ns + 4) finite = finite && isfinite(m[t]) && isfinite(b[t]);
+        }
+        if (!finite && status) atomicOr(status, kStatusNonFinite);
     }
     __syncthreads();
     for (int x = threadIdx.x; x < (int)n3; x += blockDim.x) {
@@ -159,7 +170,7 @@ __global__ void __launch_bounds__(kThreads)
 maxwellian_kernel(const double *__restrict__ f, double *__restrict__ M,
                   double *__restrict__ g, const double *__restrict__ Mref,
                   int N, const double *__restrict__ v, double mass, double KB,
-                  double *__restrict__ mom)
+                  double *__restrict__ mom, unsigned int *__restrict__ status)
 {
     __shared__ double red[32 * 4];
     const long long n3 = (long long)N * N * N;
@@ -192,6 +203,9 @@ maxwellian_kernel(const double *__restrict__ f, double *__restrict__ M,
     block_sum<1>(tt, red);
     const double T = (mass * mass / KB) * (tt[0] / (3.0 * rho));
     const double pre = rho * pow(0.5 / (M_PI * T), 1.5);
+    if (threadIdx.x == 0 && status &&
+        !(isfinite(rho) && isfinite(u0) && isfinite(u1) && isfinite(u2) && isfinite(T)))
+        atomicOr(status, kStatusNonFinite);
     for (int x = threadIdx.x; x < (int)n3; x += blockDim.x) {
         const int i = x / (N * N), j = (x / N) % N, k = x % N;
         const double Mx = pre * exp(-(0.5 / T) * ((v[i] - u0) * (v[i] - u0) +
@@ -216,7 +230,7 @@ maxwellian_kernel(const double *__restrict__ f, double *__restrict__ M,
 // {rho, u_x, u_y, u_z, T, rho T, E+, E-}.  One CTA per instance, FP64.
 __global__ void __launch_bounds__(kThreads)
 moments_kernel(const double *__restrict__ f, int N, const double *__restrict__ v, double mass,
-               double KB, double *__restrict__ out)
+               double KB, double *__restrict__ out, unsigned int *__restrict__ status)
 {
     __shared__ double red[32 * 4];
     const long long n3 = (long long)N * N * N;
@@ -252,6 +266,9 @@ moments_kernel(const double *__restrict__ f, int N, const double *__restrict__ v
         double *o = out + 8 * (long long)blockIdx.x;
         o[0] = rho; o[1] = u0; o[2] = u1; o[3] = u2; o[4] = T; o[5] = rho * T;
         o[6] = t[1]; o[7] = t[2];
+        bool finite = true;
+        for (int q = 0; q < 8; q++) finite = finite && isfinite(o[q]);
+        if (!finite && status) atomicOr(status, kStatusNonFinite);
     }
 }
 
@@ -271,36 +288,36 @@ __global__ void axpy_kernel(double *__restrict__ y, const double *__restrict__ x
 }  // namespace
 
 cudaError_t conserve_batch(double *Q, int B, const double *v,
-                           const ConsParams &cp, cudaStream_t st)
+                           const ConsParams &cp, cudaStream_t st, unsigned int *status)
 {
     if (B < 1) return cudaSuccess;
-    conserve_batch_kernel<<<B, kThreads, 0, st>>>(Q, v, cp);
+    conserve_batch_kernel<<<B, kThreads, 0, st>>>(Q, v, cp, status);
     return cudaGetLastError();
 }
 
 cudaError_t conserve_species(double **Qptrs_dev, const double *v,
-                             const ConsParams &cp, cudaStream_t st)
+                             const ConsParams &cp, cudaStream_t st, unsigned int *status)
 {
-    conserve_species_kernel<<<1, kThreads, 0, st>>>(Qptrs_dev, v, cp);
+    conserve_species_kernel<<<1, kThreads, 0, st>>>(Qptrs_dev, v, cp, status);
     return cudaGetLastError();
 }
 
 cudaError_t maxwellian_split(const double *f, double *M, double *g,
                              const double *Mref, int B, int N, const double *v,
                              double mass, double KB, double *moments_out,
-                             cudaStream_t st)
+                             cudaStream_t st, unsigned int *status)
 {
     if (B < 1) return cudaSuccess;
     maxwellian_kernel<<<B, kThreads, 0, st>>>(f, M, g, Mref, N, v, mass, KB,
-                                              moments_out);
+                                              moments_out, status);
     return cudaGetLastError();
 }
 
 cudaError_t moments_batch(const double *f, int B, int N, const double *v, double mass,
-                          double KB, double *out, cudaStream_t st)
+                          double KB, double *out, cudaStream_t st, unsigned int *status)
 {
     if (B < 1) return cudaSuccess;
-    moments_kernel<<<B, kThreads, 0, st>>>(f, N, v, mass, KB, out);
+    moments_kernel<<<B, kThreads, 0, st>>>(f, N, v, mass, KB, out, status);
     return cudaGetLastError();
 }
 

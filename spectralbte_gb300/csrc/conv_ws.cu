@@ -35,6 +35,14 @@
 //    CTA runs (N^2 + F)/2 slots instead of N^2, where F (0 or 4) counts the
 //    rows that are their own partner.  Wblk is then the pre-summed table of
 //    weights_to_sym_f32.
+//  * Bounded waits.  Every mbarrier wait gives up after a clock limit, sets
+//    kStatusTimeout in the status word and leaves; before leaving, the
+//    producer and the consumers wait (again bounded) for the copies already
+//    issued into the ring, so no copy lands in the shared memory of a CTA
+//    that has exited.  A test hook (stall_slot >= 0) makes the producer of
+//    CTA (0, 0) skip that slot's copies, and that CTA's waits use stall_limit
+//    clocks: its consumers then wait on a barrier that nothing completes,
+//    which is how the timeout path is tested without a fault.
 #include "common.cuh"
 #include "kernels.h"
 #include "mbarrier.cuh"
@@ -67,7 +75,7 @@ __global__ void __launch_bounds__(WsLayout<N, BG, ZS, TWO, PACKED, STG>::kThread
 conv_ws_kernel(const float *__restrict__ Wblk, const float2 *__restrict__ P,
                const float2 *__restrict__ R, const float2 *__restrict__ S,
                const float2 *__restrict__ T, double2 *__restrict__ qacc, int flush, int sym,
-               unsigned int *__restrict__ status)
+               unsigned int *__restrict__ status, int stall_slot, long long stall_limit)
 {
     using L = WsLayout<N, BG, ZS, TWO, PACKED, STG>;
     constexpr int NN = N * N;
@@ -89,6 +97,11 @@ conv_ws_kernel(const float *__restrict__ Wblk, const float2 *__restrict__ P,
     const long long grp = blockIdx.y;
     // slots this CTA runs: every xi-row, or one per partner pair
     const int nslot = sym ? sym_slots(N, zx, zy) : NN;
+    // the stall test hook acts on CTA (0, 0) only; every other CTA keeps the
+    // default limit and skips nothing
+    const bool stall_cta = stall_slot >= 0 && blockIdx.x == 0 && blockIdx.y == 0;
+    const int skip = stall_cta ? stall_slot : -1;
+    const long long limit = stall_cta ? stall_limit : kWaitLimitClocks;
 
     if (tid == 0) {
         for (int s = 0; s < ST; s++) {
@@ -117,10 +130,20 @@ conv_ws_kernel(const float *__restrict__ Wblk, const float2 *__restrict__ P,
             if (sym && fx * N + fy < it) continue;  // covered by its partner row
             const int s = slot % ST;
             if (slot >= ST) {
-                if (!mbar_wait_bounded(&empty[s], (uint32_t)(((slot / ST) - 1) & 1))) {
+                if (!mbar_wait_bounded(&empty[s], (uint32_t)(((slot / ST) - 1) & 1), limit)) {
                     atomicOr(status, kStatusTimeout);
+                    // let the copies of the slots issued since land before
+                    // this thread, and with it the CTA, leaves
+                    for (int j = slot - ST + 1; j < slot; j++)
+                        if (j != skip)
+                            (void)mbar_wait_bounded(&full[j % ST], (uint32_t)((j / ST) & 1),
+                                                    limit);
                     return;
                 }
+            }
+            if (slot == skip) {  // test hook: this slot's barrier never completes
+                slot++;
+                continue;
             }
             unsigned char *base = smem + s * L::kStageBytes;
             const long long prow = (long long)it * N * BG;
@@ -182,10 +205,14 @@ conv_ws_kernel(const float *__restrict__ Wblk, const float2 *__restrict__ P,
 
     for (int it = 0; it < nslot; it++) {
         const int s = it % ST;
-        if (!mbar_wait_bounded(&full[s], (uint32_t)((it / ST) & 1))) {
+        if (!mbar_wait_bounded(&full[s], (uint32_t)((it / ST) & 1), limit)) {
             atomicOr(status, kStatusTimeout);
-            // give a copy still in flight one more bounded chance to land
-            (void)mbar_wait_bounded(&full[s], (uint32_t)((it / ST) & 1));
+            // The producer may have issued slots it + 1 .. it + ST - 1 (their
+            // stages were released); give each copy a bounded chance to land
+            // before leaving.  Slot `it` itself gets one more wait.
+            for (int j = it; j < it + ST && j < nslot; j++)
+                if (j != skip)
+                    (void)mbar_wait_bounded(&full[j % ST], (uint32_t)((j / ST) & 1), limit);
             return;
         }
         const unsigned char *base = smem + s * L::kStageBytes;
@@ -298,7 +325,7 @@ conv_ws_kernel(const float *__restrict__ Wblk, const float2 *__restrict__ P,
 template <int N, int BG, int ZS, bool TWO, bool PACKED, int ST, int MINB>
 cudaError_t launch_ws(const float *Wblk, const float2 *P, const float2 *R, const float2 *S,
                       const float2 *T, double2 *qacc, int B, int flush, int sym, unsigned *status,
-                      cudaStream_t st)
+                      cudaStream_t st, int stall_slot, long long stall_limit)
 {
     using L = WsLayout<N, BG, ZS, TWO, PACKED, ST>;
     const size_t smem = (size_t)L::kStages * L::kStageBytes;
@@ -307,7 +334,8 @@ cudaError_t launch_ws(const float *Wblk, const float2 *P, const float2 *R, const
                                          (int)smem);
     if (e != cudaSuccess) return e;
     dim3 grid(N * N, (B + BG - 1) / BG);
-    kern<<<grid, L::kThreads, smem, st>>>(Wblk, P, R, S, T, qacc, flush, sym, status);
+    kern<<<grid, L::kThreads, smem, st>>>(Wblk, P, R, S, T, qacc, flush, sym, status,
+                                          stall_slot, stall_limit);
     return cudaGetLastError();
 }
 
@@ -349,18 +377,21 @@ bool conv_ws_supported(int N, int bg, int zs, bool packed, int stages, bool two,
 cudaError_t conv_ws(const float *Wblk, const float2 *P, const float2 *R, const float2 *S,
                     const float2 *T, double2 *qacc, int N, int B, int bg, int zs, bool packed,
                     int stages, int flush, int sym, int minb, unsigned int *status,
-                    cudaStream_t st)
+                    cudaStream_t st, int stall_slot, long long stall_limit)
 {
     const bool two = (S != nullptr);
     if (!conv_ws_supported(N, bg, zs, packed, stages, two, minb) || B < 1)
         return cudaErrorInvalidValue;
+    if (stall_slot >= 0 && stall_limit <= 0) return cudaErrorInvalidValue;
 #define SBTE_WS_L(NN, BGV, ZSV, PK, STV, MB)                                                  \
     if (N == NN && bg == BGV && zs == ZSV && packed == (PK != 0) && stages == STV &&         \
         minb == MB)                                                                           \
-        return two ? launch_ws<NN, BGV, ZSV, true, PK != 0, STV, MB>(Wblk, P, R, S, T, qacc, B, \
-                                                                     flush, sym, status, st) \
-                   : launch_ws<NN, BGV, ZSV, false, PK != 0, STV, MB>(Wblk, P, R, S, T, qacc,  \
-                                                                      B, flush, sym, status, st);
+        return two ? launch_ws<NN, BGV, ZSV, true, PK != 0, STV, MB>(                       \
+                         Wblk, P, R, S, T, qacc, B, flush, sym, status, st, stall_slot,         \
+                         stall_limit)                                                           \
+                   : launch_ws<NN, BGV, ZSV, false, PK != 0, STV, MB>(                      \
+                         Wblk, P, R, S, T, qacc, B, flush, sym, status, st, stall_slot,         \
+                         stall_limit);
     SBTE_WS_SHAPES(SBTE_WS_L)
 #undef SBTE_WS_L
     return cudaErrorInvalidValue;

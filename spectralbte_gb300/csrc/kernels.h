@@ -67,6 +67,11 @@ struct ConvF32Config {
     int zs = 0;       // variants 2, 3: zeta_z values per thread (8 or 16)
     int sym = 0;      // variants 2, 3, 5: symmetric form over partner xi-rows
                       // (Wblk is then the table of weights_to_sym_f32)
+    // Test hook of the bounded waits (variants 2, 3, 5): with stall_slot >= 0
+    // the first CTA's producer skips that slot's copies and the CTA's waits
+    // give up after stall_limit clocks (conv_ws.cu).
+    int stall_slot = -1;
+    long long stall_limit = 0;
 };
 cudaError_t conv_f32_batched(const float *Wblk, const float2 *P,
                              const float2 *R, const float2 *S,
@@ -85,7 +90,8 @@ bool conv_ws_supported(int N, int bg, int zs, bool packed, int stages,
 cudaError_t conv_ws(const float *Wblk, const float2 *P, const float2 *R,
                     const float2 *S, const float2 *T, double2 *qacc, int N, int B,
                     int bg, int zs, bool packed, int stages, int flush, int sym,
-                    int minb, unsigned int *status, cudaStream_t st);
+                    int minb, unsigned int *status, cudaStream_t st,
+                    int stall_slot = -1, long long stall_limit = 0);
 
 // Symmetric form of the convolution for g = f (both Q(f,f) and the
 // maxPreserve sum).  For zeta-row (zx, zy) the xi-row partner map is
@@ -130,12 +136,16 @@ struct ConsParams {
     int pivot[8];
 };
 // Conservation projection (conserve.c:207-264) for one species on B
-// independent instances Q[b][pos] (plain layout), in place, FP64.
+// independent instances Q[b][pos] (plain layout), in place, FP64.  A
+// non-finite moment sum or multiplier sets kStatusNonFinite in *status
+// (when status is not null).
 cudaError_t conserve_batch(double *Q, int B, const double *v,
-                           const ConsParams &cp, cudaStream_t st);
+                           const ConsParams &cp, cudaStream_t st,
+                           unsigned int *status = nullptr);
 // Multi-species form: Qptrs[n*Ns+m] point at N^3 arrays (one instance).
 cudaError_t conserve_species(double **Qptrs_dev, const double *v,
-                             const ConsParams &cp, cudaStream_t st);
+                             const ConsParams &cp, cudaStream_t st,
+                             unsigned int *status = nullptr);
 
 // Maxwellian split of find_maxwellians (collisions.c:91-106) for B
 // instances: M = Maxwellian with the (rho, u, T) of f, computed with the
@@ -145,13 +155,15 @@ cudaError_t conserve_species(double **Qptrs_dev, const double *v,
 cudaError_t maxwellian_split(const double *f, double *M, double *g,
                              const double *Mref, int B, int N,
                              const double *v, double mass, double KB,
-                             double *moments_out, cudaStream_t st);
+                             double *moments_out, cudaStream_t st,
+                             unsigned int *status = nullptr);
 
 // Output moments of B instances, 8 doubles each: rho, u_x, u_y, u_z, T,
 // rho T, and the positive and negative parts of getEnergy
 // (output.c:156-213, momentRoutines.c:58-190).
 cudaError_t moments_batch(const double *f, int B, int N, const double *v, double mass,
-                          double KB, double *out, cudaStream_t st);
+                          double KB, double *out, cudaStream_t st,
+                          unsigned int *status = nullptr);
 
 // Euler / RK2 combinations of boltz.c:206-241 on B*N^3 values.
 cudaError_t axpy_update(double *y, const double *x, const double *q,

@@ -39,14 +39,18 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
     return done != 0;
 }
 
-// Bounded wait: gives up after ~2^31 clocks (about a second) and returns
-// false so the caller can record the failure and leave cleanly.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity)
+// Default limit of a bounded wait: 2^31 clocks, about a second.
+constexpr long long kWaitLimitClocks = 1LL << 31;
+
+// Bounded wait: gives up after `limit` clocks and returns false so the
+// caller can record the failure and leave cleanly.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity,
+                                                  long long limit = kWaitLimitClocks)
 {
     if (mbar_try_wait(bar, parity)) return true;
     const long long t0 = clock64();
     while (!mbar_try_wait(bar, parity)) {
-        if (clock64() - t0 > (1LL << 31)) return false;
+        if (clock64() - t0 > limit) return false;
     }
     return true;
 }

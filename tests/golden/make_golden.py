@@ -1,8 +1,9 @@
 """Generate the golden fixtures in tests/golden/ from the reference itself.
 
-Run where the reference checkout exists (default /root/reference):
+Run where the reference checkout exists, naming it by argument or by the
+SPECTRAL_REFERENCE_DIR environment variable:
 
-    python tests/golden/make_golden.py [REF_DIR]
+    python tests/golden/make_golden.py REF_DIR
 
 It builds oracle/_ref/libspectral_ref.so from the reference's own
 collisions.c, conserve.c, momentRoutines.c and weights.c, compiled with the
@@ -141,7 +142,7 @@ def two_maxwellian(g: po.Grid, rng, jitter=0.05):
     return np.ascontiguousarray(f.reshape(-1))
 
 
-def landau(ref_dir="/root/reference"):
+def landau(ref_dir):
     """golden_landau.npz: the reference's initialize_weights_AnIso, run in a
     scratch directory (it writes Weights/N*_Aniso_*_Landau.wts there)."""
     import tempfile
@@ -174,7 +175,7 @@ def landau(ref_dir="/root/reference"):
     np.savez_compressed(os.path.join(HERE, "golden_landau.npz"), **out)
 
 
-def main(ref_dir="/root/reference"):
+def main(ref_dir):
     assert po.build_ref(ref_dir), "reference sources not found"
     po.build()
     ref = RefLib(os.path.join(ROOT, "oracle", "_ref", "libspectral_ref.so"))
@@ -236,8 +237,11 @@ def main(ref_dir="/root/reference"):
 
 if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    ref = args[0] if args else os.environ.get("SPECTRAL_REFERENCE_DIR", "")
+    if not ref:
+        sys.exit("usage: make_golden.py REF_DIR (or set SPECTRAL_REFERENCE_DIR)")
     if "--landau" in sys.argv:
-        landau(*args)
+        landau(ref)
     else:
-        main(*args)
-        landau(*args)
+        main(ref)
+        landau(ref)

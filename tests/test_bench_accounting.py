@@ -52,7 +52,7 @@ def test_learned_bytes_match_the_pass_list(N, C, Km, L, Hd):
 
 
 def test_learned_layer_bytes_match_ncu():
-    """ncu, layer 0 at 256 instances (profiles/learned_layer0_n32_b256_ncu.md):
+    """ncu, layer 0 at 256 instances:
     9.93 GB over the eight GEMMs of the layer."""
     layer = sum(b for name, b in _passes(32, 64, 12, 4) if name.startswith("0:"))
     measured = 9.93e9 / 256

@@ -10,7 +10,10 @@ its only intermediate in a fixed static device array.
 This file checks it through the C ABI against the existing fft3D entry point.
 It makes several calls in a row that share the same static array, and the
 tolerance is the transform parity bar of the other tests: rel-L2 <= 1e-12.
-It also checks that a size beyond the array's limit is refused with an error.
+It also checks that the calls leave the device's free memory unchanged (after
+a first call, which may load the library's device module and with it the
+array), that N = 64 (its largest grid, 7 instances) and a non-default stream
+work, and that a size beyond the array's limit is refused with an error.
 pytest collects this file last, so a run that stops at the first failure has
 already run every other test.
 """
@@ -100,3 +103,56 @@ def test_noalloc_rejects_sizes_beyond_the_static_scratch(gpu):
             small.data_ptr(), 64, 0, None)
     assert rc == sb.lib().spectral_last_error() == 2
     assert b"32 MiB static scratch" in sb.lib().spectral_last_error_message()
+
+
+def test_noalloc_calls_leave_free_device_memory_unchanged(gpu):
+    """After one warm-up call (which may load the device module that holds the
+    static array), further calls change the device's free memory by nothing:
+    the entry point allocates no device memory."""
+    import torch
+    sb = gpu
+    N, L_v, B = 32, 6.0, 4
+    v, zeta = sb.grid_0d(N, L_v)
+    vp, zp = v.ctypes.data_as(DP), zeta.ctypes.data_as(DP)
+    fn = _entry(sb)
+    src = torch.randn(B, 2 * N ** 3, dtype=torch.float64, device="cuda")
+    out = torch.empty_like(src)
+    assert fn(N, L_v, vp, zp, src.data_ptr(), out.data_ptr(), B, 0, None) == 0
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for invert in (0, 1, 0, 1, 0):
+        assert fn(N, L_v, vp, zp, src.data_ptr(), out.data_ptr(), B, invert, None) == 0
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
+
+
+def test_noalloc_n64_on_a_side_stream(gpu):
+    """The largest grid (N = 64, 7 instances: 64^2 + 7 * 64^3 values of the
+    2^21 the array holds) on a non-default stream, against the oracle's
+    fft3D restatement (the existing fft3D entry point serves N <= 32 plans
+    the same way; the oracle is the common checker)."""
+    import torch
+    from oracle import pyoracle as po
+    sb = gpu
+    N, L_v, B = 64, 8.0, 7
+    v, zeta = sb.grid_0d(N, L_v)
+    g = po.Grid(N, L_v, "0d")
+    assert np.array_equal(g.v, v) and np.array_equal(g.zeta, zeta)
+    vp, zp = v.ctypes.data_as(DP), zeta.ctypes.data_as(DP)
+    fn = _entry(sb)
+    rng = np.random.default_rng(64)
+    x = rng.standard_normal((B, N ** 3)) + 1j * rng.standard_normal((B, N ** 3))
+    src = torch.from_numpy(np.ascontiguousarray(x).view(np.float64).copy()).cuda()
+    out = torch.empty_like(src)
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    for invert in (0, 1):
+        rc = fn(N, L_v, vp, zp, src.data_ptr(), out.data_ptr(), B, invert,
+                C.c_void_p(side.cuda_stream))
+        assert rc == 0, sb.lib().spectral_last_error_message()
+        side.synchronize()
+        got = out.cpu().numpy().view(np.complex128).reshape(B, -1)
+        for b in (0, B - 1):
+            want = po.fft3d(g, x[b], invert)
+            assert _rel(got[b], want) <= TOL, (invert, b, _rel(got[b], want))
