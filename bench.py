@@ -63,6 +63,11 @@ NCU_TRAFFIC_SYM = {
 # DRAM bytes (read + write) of one channel-mix launch of the learned operator
 # at 256 instances, measured by ncu on the network alone at N=32.
 LEARNED_CM_TRAFFIC = {"bytes": 2.15e9 + 1.04e9, "B": 256}
+# Floor of the learned operator's spot check and acceptance: the distance
+# |Q_net - Q| / sqrt(|Q|^2 + eps mean_b |Q_b|^2), with the eps of the training
+# loss.  Near equilibrium Q -> 0, and the floor measures the error against the
+# batch's collision-term scale instead.
+LEARNED_FLOOR = 0.1
 KERNEL_NAME = {1: "conv_f32_kernel", 2: "conv_ws_kernel", 3: "conv_ws_kernel",
                4: "conv_x4_kernel", 5: "conv_ws_kernel"}
 
@@ -357,12 +362,9 @@ def run_learned(args, plan, fd, Qd, B, flags, peaks):
     workload, next to the plain FP32 operator's Q (already in Qd)."""
     import torch
     import spectralbte_gb300 as sb
-    # the 0D two-Maxwellian workload runs the network fine-tuned on that family
-    # when it is present, otherwise the general network
-    path = args.learned or next(
-        (q for q in (os.path.join(ROOT, "spectralbte_gb300", "models", n)
-                     for n in ("fno_n32_two_maxwellian.npz", "fno_n32.npz"))
-         if os.path.exists(q)), "")
+    # the general network (trained on every family, never scored on this
+    # workload's seed); --learned selects another
+    path = args.learned or os.path.join(ROOT, "spectralbte_gb300", "models", "fno_n32.npz")
     if not path or not os.path.exists(path):
         return {"status": "no trained network in spectralbte_gb300/models"}
     net = sb.FourierOperator.load(path)
@@ -371,6 +373,7 @@ def run_learned(args, plan, fd, Qd, B, flags, peaks):
     Ql = torch.empty_like(Qd)
     lf = flags | sb.LEARNED
     plan.set_learned(net, tol=1e-3, check_every=0)   # network + FP64 projection only
+    plan.set_learned_floor(LEARNED_FLOOR)
     for _ in range(max(1, args.warmup)):
         plan.computeQ_device(fd, Ql, B, lf)
     torch.cuda.synchronize()
@@ -387,8 +390,14 @@ def run_learned(args, plan, fd, Qd, B, flags, peaks):
     launches = (sb.kernel_launches() - k0) / steps
     cm_ms, cm_n = net.kernel_time()
     net.set_profiling(False)
-    d = (Ql - Qd).pow(2).sum(dim=1) / Qd.pow(2).sum(dim=1)
-    rel = d.sqrt()
+    num = (Ql - Qd).pow(2).sum(dim=1)
+    q2 = Qd.pow(2).sum(dim=1)
+    rel = (num / q2).sqrt()
+    # the floored distance of the spot check and the training loss:
+    # |dQ| / sqrt(|Q|^2 + eps mean_b |Q_b|^2)
+    rel_f = (num / (q2 + LEARNED_FLOOR * q2.mean())).sqrt()
+    from spectralbte_gb300.workloads import moment_residual
+    mom_res = moment_residual(plan.v, Ql)
     # the spot-checked path: one instance per call against the plain FP32 operator
     plan.set_learned(net, tol=1e-3, check_every=1)
     for _ in range(max(3, args.warmup)):
@@ -446,8 +455,13 @@ def run_learned(args, plan, fd, Qd, B, flags, peaks):
         "speedup_vs_fp32_plain": None,
         "rel_l2_vs_plain_fp32": {"mean": float(rel.mean()), "median": float(rel.median()),
                                  "max": float(rel.max())},
+        "rel_l2_floored_vs_plain_fp32": {"mean": float(rel_f.mean()),
+                                         "max": float(rel_f.max()), "floor": LEARNED_FLOOR},
+        "moments_after_projection": mom_res,
         "tolerance": 1e-3,
-        "accepted": bool(float(rel.max()) <= 1e-3),
+        "accepted": bool(float(rel_f.max()) <= 1e-3),
+        "acceptance": ("every instance of this workload within rel-L2 1e-3 of the plain FP32 "
+                       "operator, with the floor of the spot check"),
         "spot_checked": {"value": B / (ms_checked / 1e3), "unit": UNIT,
                          "ms_per_step": ms_checked, "steps": steps,
                          "gpu_launches": launches_checked, "clocks": clk_checked,
@@ -460,9 +474,9 @@ def run_learned(args, plan, fd, Qd, B, flags, peaks):
                      "achieved": cm_gbs, "peak": float(peaks["hbm_gbs"]), "unit": "GB/s",
                      "frac": (cm_gbs / float(peaks["hbm_gbs"])) if cm_gbs else None,
                      "traffic": cm_traffic,
-                     "algorithmic": (f"3 activation tensors x {w['channel_mix_bytes']:.4e} B x "
-                                     f"{Bp} instances = {cm_bytes:.4e} B per launch (read H "
-                                     f"and S, write H')"),
+                     "algorithmic": (f"{w['channel_mix_bytes']:.4e} B per instance (read H and "
+                                     f"S, write H': 3 tensors of 64 channels x N^3 points x 2 "
+                                     f"B) x {Bp} instances = {cm_bytes:.4e} B per launch"),
                      "launch_ms": cm_avg * 1e3, "launches_timed": cm_n,
                      "traffic_note": (f"ncu dram bytes of the same kernel at "
                                       f"{LEARNED_CM_TRAFFIC['B']} instances "
@@ -638,12 +652,14 @@ def run_1d(args):
         if os.path.exists(path):
             net = sb.FourierOperator.load(path)
             plan.set_learned(net, tol=1e-3, check_every=0)
+            plan.set_learned_floor(LEARNED_FLOOR)
             fl, msl, moml, _ = run(sb.FP32 | sb.LEARNED, steps)
             dev = {k: float(np.abs(moml[:, i] - mom[:, i]).max() / np.abs(mom[:, i]).max())
                    for k, i in (("rho", 0), ("T", 4))}
             dev["u_x_abs"] = float(np.abs(moml[:, 1] - mom[:, 1]).max())
             # the spot-checked policy on a short run (a check reads back, so no graph)
             plan.set_learned(net, tol=1e-3, check_every=1)
+            plan.set_learned_floor(LEARNED_FLOOR)
             fc = torch.from_numpy(f0).cuda()
             nchk = min(steps, 50)
             torch.cuda.synchronize()
@@ -662,7 +678,7 @@ def run_1d(args):
                                             "steps": nchk, "calls": st["calls"],
                                             "fallbacks": st["fallbacks"],
                                             "last_check_rel_l2": st["last_err"],
-                                            "tolerance": 1e-3},
+                                            "tolerance": 1e-3, "floor": LEARNED_FLOOR},
             }
     print(json.dumps(line), flush=True)
     return 0
@@ -910,7 +926,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--batch", type=int, default=1024)
     ap.add_argument("--n", type=int, default=N_DEF)
-    ap.add_argument("--seed", type=int, default=20261203)
+    # the workload seed: no network was trained or selected on its instances
+    ap.add_argument("--seed", type=int, default=52001)
     ap.add_argument("--fp64-batch", type=int, default=8)
     ap.add_argument("--cpu-evals", type=int, default=3,
                     help="full CPU evaluations timed for cpu_baseline")

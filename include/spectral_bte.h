@@ -108,6 +108,16 @@ void initialize_weights_AnIso(int nodes, double *zeta, double Lv, double lam,
                               int weightFlag, double **conv_weights,
                               double glance);
 void dealloc_weights(int N, double **conv_weights);
+/* exec/MPIWeightGenerator.c (the `weights_ N glance beta lambda L_v`
+   executable, main :37-127): on its own grid (:63-74), Landau weights for
+   glance = 0 or grazing-collision weights otherwise, written to
+   Weights/N%d_Aniso_L_v%g_lambda%g_Landau.wts or
+   Weights/N%d_AnIso_L_v%g_lambda%g_glance%g.wts (:79-83) unless the file
+   exists; initialize_weights_AnIso with the same arguments then loads it.
+   One GPU replaces the MPI ranks; beta is unused, as in the reference.
+   Returns a status (the reference exits). */
+int spectral_weights_generator(int N, double glance, double beta, double lambda,
+                               double L_v);
 /* weights.h:43 (weights.c:265): GPU quadrature into conv_weights rows */
 void generate_conv_weights_iso(double **conv_weights);
 /* weights.h:47 (weights.c:156): the integrand, on the host */
@@ -169,6 +179,14 @@ int spectral_plan_get_weights(spectral_plan *plan, double *W_host,
    double integral of gHat3L, no trapezoid factors) for the plan's grid. */
 int spectral_plan_generate_weights_landau(spectral_plan *plan, double lambda);
 int spectral_plan_set_conservation(spectral_plan *plan, double mass);
+/* Grazing-collision weights: gHat3 of the stand-alone generator
+   (MPIcollisionRoutines.c:33-205, eps-linear cross section with the
+   Coulomb-case Taylor term below theta = sqrt(glance)), no trapezoid
+   factors, for the plan's grid; 0 < glance < pi^2/4, N <= 16.  The
+   reference's GSL QAG/CQUAD (tolerance 1e-6) is replaced by composite
+   Gauss-Legendre rules converged to ~1e-13. */
+int spectral_plan_generate_weights_grazing(spectral_plan *plan, double lambda,
+                                           double glance);
 
 /* Q for B instances.  f and Q are [B][N^3] FP64 in device memory; for
    flag SPECTRAL_FP32 the transforms and the convolution run in FP32 and
@@ -358,6 +376,16 @@ int spectral_fno_predict(spectral_fno *net, const double *f_dev, double *Q_dev,
    |y - Q~|^2 / (|Q~|^2 + eps * mean over the batch of |Q~|^2), so that
    near-equilibrium instances with |Q~| -> 0 do not dominate. */
 int spectral_fno_set_loss_floor(spectral_fno *net, float eps);
+/* Equilibrium-exact form (on = 1): the operator becomes
+   Q(f) = s_f^2 sigma y(f / s_f) - s_M^2 sigma y(M_f / s_M), where M_f is the
+   Maxwellian with the density, bulk velocity and temperature of f
+   (momentRoutines.c:58-185 with unit mass and KB), so Q(M) = 0 holds
+   identically.  v holds the N velocity nodes of the grid (needed for M_f).
+   f and M_f run as one batch of 2B instances, so an evaluation costs twice
+   the plain network.  Training (loss_grad, train_step) then fits the
+   difference. */
+int spectral_fno_set_equilibrium(spectral_fno *net, int on, const double *v);
+int spectral_fno_equilibrium(spectral_fno *net);
 /* Mean over instances of |y - Q~|^2 / |Q~|^2 (Q~ = Q / (s^2 sigma), with the
    loss floor above) and its gradient (host, nparams floats) for FP32 device
    data f, Q [B][N^3]. */
@@ -377,6 +405,13 @@ int spectral_fno_train_step(spectral_fno *net, const float *f_dev,
    checks.  net = NULL detaches. */
 int spectral_plan_set_learned(spectral_plan *plan, spectral_fno *net,
                               double tol, int check_every);
+/* Floor of the spot check (default 0): with eps > 0 the check's distance is
+   |Q_net - Q| / sqrt(|Q|^2 + eps * mean over the batch of |Q_net,b|^2), the
+   normalisation of the training loss with the same eps.  Near equilibrium
+   Q -> 0 for every method, and the plain FP32 operator itself then differs
+   from FP64 by more than 1e-3 of |Q|; the floor measures the error against
+   the collision term's scale in the batch instead. */
+int spectral_plan_set_learned_floor(spectral_plan *plan, double eps);
 int spectral_plan_learned_stats(spectral_plan *plan, long long *calls,
                                 long long *checks, long long *fallbacks,
                                 double *last_err);

@@ -212,15 +212,32 @@ class Net:
         y, c = self.forward(f)
         return y * (c["s"] ** 2 * self.sigma)[:, None, None, None]
 
-    def loss_grad(self, f, Q, floor: float = 0.0):
+    def predict_eq(self, f, M):
+        """Equilibrium-exact form: predict(f) - predict(M), M the Maxwellian
+        of each f (fno.cu header)."""
+        return self.predict(f) - self.predict(M)
+
+    def loss_grad(self, f, Q, floor: float = 0.0, M=None):
         """Mean over instances of |y - t|^2/(|t|^2 + floor mean_b |t_b|^2),
         t = Q / (s^2 sigma), and its gradient as a dict of arrays shaped like
-        the parameters."""
+        the parameters.  With M (the Maxwellian of each f) the equilibrium-
+        exact form: y is replaced by y(f) - (s_M / s_f)^2 y(M), both halves
+        run as one batch [f; M], and the M half receives the output gradient
+        times -(s_M / s_f)^2."""
         p, sp = self.p, self.spec
         B = f.shape[0]
-        y, c = self.forward(f)
+        if M is None:
+            y, c = self.forward(f)
+            sf = c["s"]
+        else:
+            f = np.asarray(f, dtype=np.float64).reshape(B, sp.N, sp.N, sp.N)
+            M = np.asarray(M, dtype=np.float64).reshape(B, sp.N, sp.N, sp.N)
+            y2, c = self.forward(np.concatenate([f, M]))
+            sf, sM = c["s"][:B], c["s"][B:]
+            rho = (sM / sf) ** 2
+            y = y2[:B] - rho[:, None, None, None] * y2[B:]
         t = np.asarray(Q, dtype=np.float64).reshape(y.shape) / \
-            (c["s"] ** 2 * self.sigma)[:, None, None, None]
+            (sf ** 2 * self.sigma)[:, None, None, None]
         den = (t.reshape(B, -1) ** 2).sum(axis=1)
         den = den + floor * den.mean()
         r = y - t
@@ -228,6 +245,14 @@ class Net:
         # the device carries gradients times the loss scale gs = B mean(den) / 2
         gs = 0.5 * den.sum()
         dy = 2.0 * r / (den * B)[:, None, None, None] * gs
+        if M is not None:
+            dy = np.concatenate([dy, -rho[:, None, None, None] * dy])
+        return loss, self._backward(c, dy, gs)
+
+    def _backward(self, c, dy, gs):
+        """Parameter gradients (divided by the loss scale gs) of the cached
+        forward pass c for the output gradient dy."""
+        p, sp = self.p, self.spec
         g = {k: np.zeros_like(v) for k, v in p.items()}
         g["c2"][0] = dy.sum()
         u = c["u"]
@@ -267,4 +292,28 @@ class Net:
         x = c["x"]
         g["P"] = np.einsum("bijkc,bijk->c", dh, x)
         g["bP"] = dh.sum(axis=(0, 1, 2, 3))
-        return loss, {k: val / gs for k, val in g.items()}
+        return {k: val / gs for k, val in g.items()}
+
+
+def maxwellian_of(f: np.ndarray, v: np.ndarray) -> np.ndarray:
+    """The Maxwellian with the density, bulk velocity and temperature of each
+    f (B, N^3), with unit mass and Boltzmann constant and the trapezoid
+    weights of momentRoutines.c:58-185 (getDensity, getBulkVelocity,
+    getTemperature), as the device builds it for the equilibrium form."""
+    v = np.asarray(v, dtype=np.float64)
+    N = v.size
+    f = np.asarray(f, dtype=np.float64).reshape(-1, N, N, N)
+    wt = np.ones(N)
+    wt[0] = wt[-1] = 0.5
+    dv = v[1] - v[0]
+    w = wt[:, None, None] * wt[None, :, None] * wt[None, None, :] * dv ** 3
+    vx, vy, vz = v[:, None, None], v[None, :, None], v[None, None, :]
+    out = np.empty_like(f)
+    for b in range(f.shape[0]):
+        fb = f[b]
+        rho = (w * fb).sum()
+        u = [(w * vx * fb).sum() / rho, (w * vy * fb).sum() / rho, (w * vz * fb).sum() / rho]
+        d2 = (vx - u[0]) ** 2 + (vy - u[1]) ** 2 + (vz - u[2]) ** 2
+        T = (w * d2 * fb).sum() / (3.0 * rho)
+        out[b] = rho * (0.5 / (np.pi * T)) ** 1.5 * np.exp(-(0.5 / T) * d2)
+    return out.reshape(f.shape[0], -1)

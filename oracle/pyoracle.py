@@ -71,6 +71,9 @@ def lib() -> C.CDLL:
             "oracle_ghat_closed": (d, [d, d, d, d, d]),
             "oracle_weights_landau": (None, [i, _dp, d, d, i, i, _dp]),
             "oracle_ghat3l": (d, [d, d, d, d, d, d, d, d]),
+            "oracle_graze_panels": (i, [d, d]),
+            "oracle_ghat3_graze": (d, [d, d, d, d, d, d, d, d, d, i]),
+            "oracle_ghat3_graze_pairs": (None, [i, _dp, d, d, d, i, _dp]),
             "oracle_run_0d": (None, [i, d, _dp, _dp, d, d, i, i, i, _dp, i]),
             "oracle_init_bkw": (None, [i, _dp, d, _dp]),
             "oracle_conserve_batch1": (None, [C.c_void_p, _dp, i]),
@@ -221,6 +224,47 @@ def weights_landau(N: int, zeta: np.ndarray, L_v: float, lam: float, rows=None) 
     W = np.zeros((r1 - r0, n3))
     lib().oracle_weights_landau(N, _p(zeta), float(L_v), float(lam), r0, r1 - r0, _p(W))
     return W
+
+
+def graze_unique(N: int, eta: np.ndarray):
+    """Group the N^6 (zeta, xi) pairs of a weight table by the exact integer
+    key (|2k|^2, 2k.2l, |2l|^2) of their offsets from the grid centre
+    (2 k_a = 2 i_a - N), on which gHat3 depends alone (through |zeta|,
+    xi.zeta and |xi|).  Returns (pairs [U][6] of one representative each,
+    inverse [N^3 * N^3] index of each table entry into them)."""
+    eta = np.asarray(eta, dtype=np.float64)
+    k = 2 * np.arange(N) - N
+    Kx = np.stack(np.meshgrid(k, k, k, indexing="ij"), -1).reshape(-1, 3)
+    a = (Kx * Kx).sum(1)
+    d = Kx @ Kx.T
+    n3 = N ** 3
+    key = (a[:, None].astype(np.int64) * (1 << 40) + (d.astype(np.int64) + (1 << 20)) * (1 << 20)
+           + a[None, :].astype(np.int64)).reshape(-1)
+    uniq, first, inverse = np.unique(key, return_index=True, return_inverse=True)
+    z, x = first // n3, first % n3
+    idx = np.stack(np.meshgrid(np.arange(N), np.arange(N), np.arange(N), indexing="ij"),
+                   -1).reshape(-1, 3)
+    pairs = np.concatenate([eta[idx[z]], eta[idx[x]]], 1)
+    return np.ascontiguousarray(pairs), inverse.astype(np.int64)
+
+
+def weights_graze(N: int, eta: np.ndarray, L_v: float, lam: float, glance: float,
+                  pairs_only=None):
+    """Grazing-collision weights of the stand-alone generator
+    (MPIcollisionRoutines.c:154-274) on the grid eta: the whole table, or,
+    with pairs_only = (pairs, npan), gHat3 of those pairs."""
+    L = lib()
+    if pairs_only is not None:
+        pairs, npan = pairs_only
+        pairs = np.ascontiguousarray(pairs, dtype=np.float64)
+        out = np.zeros(pairs.shape[0])
+        L.oracle_ghat3_graze_pairs(pairs.shape[0], _p(pairs), float(L_v), float(lam),
+                                   float(glance), int(npan), _p(out))
+        return out
+    npan = L.oracle_graze_panels(float(np.abs(eta).max()), float(L_v))
+    pairs, inverse = graze_unique(N, eta)
+    vals = weights_graze(N, eta, L_v, lam, glance, (pairs, npan))
+    return vals[inverse].reshape(N ** 3, N ** 3)
 
 
 def gauss_legendre(n: int):

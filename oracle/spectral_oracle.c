@@ -1196,3 +1196,109 @@ void oracle_weights_landau(int N, const double *eta, double L_v, double lambda, 
                         oracle_ghat3l(eta[i], eta[j], eta[k], eta[l], eta[m], eta[n], L_v, lambda);
     }
 }
+
+/* ------------------------------------------------- grazing-collision weights
+   gHat3 of the reference's stand-alone generator (MPIcollisionRoutines.c:
+   33-205): for zeta and xi, with zl = |zeta|, xz = xi.zeta / zl and
+   xp = |xi - xz zeta / zl| (both 0 when zl = 0),
+     W = 4 pi^2 int_0^{L_v} r^{lambda+2} int_0^pi sin(phi) J0(r sin(phi) xp)
+           [ I1(r, phi) + C(r, phi) (2/pi) log(g) / log(sin(g/2)) ] dphi dr
+     I1 = int_{sqrt g}^{pi} (8/pi) (g / theta^2) theta^-2
+            [cos(a7 (1 - cos theta) - a6) J0(a8 sin theta) - cos(a6)] dtheta
+     a6 = r cos(phi) xz, a7 = r cos(phi) zl / 2, a8 = r sin(phi) zl / 2,
+     C  = -a8^2 cos(a6) / 4 + a7 sin(a6) / 2
+   (:33-52 ghat_theta, :83-121 ghat_phi with the Coulomb-case Taylor term of
+   :112-119, :124-143 ghat_r, :154-205 gHat3).  The reference integrates with
+   GSL QAG (61 points, 1e-6) in r and phi and CQUAD (1e-6) in theta.  Here
+   every level is composite 16-point Gauss-Legendre, converged to ~1e-13:
+   npan equal panels in r and in phi, and in theta panels graded
+   geometrically from sqrt(g) by a factor 2 (the integrand grows like
+   theta^-2 towards sqrt(g)).  Parity with GSL's 1e-6 answers is not pinned:
+   no GSL CQUAD exists here. */
+int oracle_graze_theta_edges(double glance, double *edges /* >= 64 */)
+{
+    int n = 0;
+    double t = sqrt(glance);
+    edges[n++] = t;
+    while (2.0 * t < M_PI && n < 62) {
+        t *= 2.0;
+        edges[n++] = t;
+    }
+    edges[n++] = M_PI;
+    return n - 1; /* panels */
+}
+
+int oracle_graze_panels(double L_eta, double L_v)
+{
+    /* the integrands' phase in r and phi stays below |zeta| + |xi| <=
+       2 sqrt(3) L_eta per unit r; 16-point panels spanning <= 8 rad of it */
+    int K = (int)ceil(2.0 * sqrt(3.0) * L_eta * L_v / 8.0);
+    return K < 2 ? 2 : K;
+}
+
+double oracle_ghat3_graze(double zeta1, double zeta2, double zeta3, double xi1, double xi2,
+                          double xi3, double L_v, double lambda, double glance, int npan)
+{
+    static double gx[16], gw[16];
+    static int init = 0;
+    if (!init) {
+#pragma omp critical(oracle_gl16)
+        {
+            if (!init) { oracle_gauss_legendre(16, gx, gw); init = 1; }
+        }
+    }
+    double zetalen2 = zeta1 * zeta1 + zeta2 * zeta2 + zeta3 * zeta3;
+    double xilen2 = xi1 * xi1 + xi2 * xi2 + xi3 * xi3;
+    double xizeta = xi1 * zeta1 + xi2 * zeta2 + xi3 * zeta3;
+    double zl = sqrt(zetalen2), xp;
+    if (((xilen2 - xizeta * xizeta / zetalen2) < 0) || (zetalen2 == 0))
+        xp = 0;
+    else
+        xp = sqrt(xilen2 - xizeta * xizeta / zetalen2);
+    double xz = zl != 0 ? xizeta / zl : 0.0;
+    double te[64];
+    int nte = oracle_graze_theta_edges(glance, te);
+    double taylor = (2.0 / M_PI) * log(glance) / log(sin(0.5 * glance));
+    double hr = L_v / npan, hp = M_PI / npan;
+    double total = 0.0;
+    for (int pr = 0; pr < npan; pr++)
+        for (int qr = 0; qr < 16; qr++) {
+            double r = hr * pr + 0.5 * hr * (gx[qr] + 1.0);
+            double phisum = 0.0;
+            for (int pp = 0; pp < npan; pp++)
+                for (int qp = 0; qp < 16; qp++) {
+                    double phi = hp * pp + 0.5 * hp * (gx[qp] + 1.0);
+                    double cph = cos(phi), sph = sin(phi);
+                    double a6 = r * cph * xz, a7 = 0.5 * r * cph * zl, a8 = 0.5 * r * sph * zl;
+                    double a9 = cos(a6);
+                    double i1 = 0.0;
+                    for (int pt = 0; pt < nte; pt++) {
+                        double t0 = te[pt], ht = te[pt + 1] - te[pt], s = 0.0;
+                        for (int qt = 0; qt < 16; qt++) {
+                            double th = t0 + 0.5 * ht * (gx[qt] + 1.0);
+                            double bcos = (8.0 / M_PI) * (glance / (th * th)) / (th * th);
+                            s += gw[qt] * bcos *
+                                 (cos(a7 * (1.0 - cos(th)) - a6) * j0(a8 * sin(th)) - a9);
+                        }
+                        i1 += 0.5 * ht * s;
+                    }
+                    double C = -0.25 * a8 * a8 * cos(a6) + 0.5 * a7 * sin(a6);
+                    phisum += 0.5 * hp * gw[qp] * sph * j0(r * sph * xp) * (i1 + C * taylor);
+                }
+            total += 0.5 * hr * gw[qr] * pow(r, lambda + 2) * phisum;
+        }
+    return 4.0 * M_PI * M_PI * total;
+}
+
+/* gHat3 of the grazing generator for npairs (zeta, xi) pairs, pairs[6 p ..
+   6 p + 5] = zeta1..3, xi1..3, OpenMP over pairs. */
+void oracle_ghat3_graze_pairs(int npairs, const double *pairs, double L_v, double lambda,
+                              double glance, int npan, double *out)
+{
+#pragma omp parallel for schedule(dynamic)
+    for (int p = 0; p < npairs; p++) {
+        const double *q = pairs + 6L * p;
+        out[p] = oracle_ghat3_graze(q[0], q[1], q[2], q[3], q[4], q[5], L_v, lambda, glance,
+                                    npan);
+    }
+}

@@ -109,6 +109,17 @@ double oracle_ghat3l(double zeta1, double zeta2, double zeta3, double xi1, doubl
                      double xi3, double L_v, double lambda);
 void oracle_weights_landau(int N, const double *eta, double L_v, double lambda, int row0,
                            int nrows, double *W);
+/* Grazing-collision weights of the stand-alone generator
+   (MPIcollisionRoutines.c:33-205), composite Gauss-Legendre at every level
+   (spectral_oracle.c): theta panel edges (returns the panel count), the r and
+   phi panel count for a grid with max |eta| = L_eta, one weight, and a list
+   of (zeta, xi) pairs. */
+int oracle_graze_theta_edges(double glance, double *edges);
+int oracle_graze_panels(double L_eta, double L_v);
+double oracle_ghat3_graze(double zeta1, double zeta2, double zeta3, double xi1, double xi2,
+                          double xi3, double L_v, double lambda, double glance, int npan);
+void oracle_ghat3_graze_pairs(int npairs, const double *pairs, double L_v, double lambda,
+                              double glance, int npan, double *out);
 /* Number of 16-point Gauss-Legendre panels the oracle uses on [0, L_v] for an
    integrand whose highest angular frequency is omega. */
 int oracle_quad_panels(double L_v, double omega);

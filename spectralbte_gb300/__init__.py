@@ -126,6 +126,8 @@ def lib() -> C.CDLL:
         "spectral_plan_set_weights": (i, [v, v, i]),
         "spectral_plan_generate_weights_iso": (i, [v, d, d, d, d, d]),
         "spectral_plan_generate_weights_landau": (i, [v, d]),
+        "spectral_plan_generate_weights_grazing": (i, [v, d, d]),
+        "spectral_weights_generator": (i, [i, d, d, d, d]),
         "initialize_weights_AnIso": (None, [i, _dp, d, d, i, C.POINTER(_dp), d]),
         "spectral_plan_get_weights": (i, [v, _dp, C.c_longlong, C.c_longlong]),
         "spectral_plan_set_conservation": (i, [v, d]),
@@ -162,6 +164,9 @@ def lib() -> C.CDLL:
         "spectral_fno_set_output_scale": (i, [v, C.c_float]),
         "spectral_fno_output_scale": (C.c_float, [v]),
         "spectral_fno_set_loss_floor": (i, [v, C.c_float]),
+        "spectral_fno_set_equilibrium": (i, [v, i, _dp]),
+        "spectral_fno_equilibrium": (i, [v]),
+        "spectral_plan_set_learned_floor": (i, [v, d]),
         "spectral_fno_predict": (i, [v, v, v, i, v]),
         "spectral_fno_loss_grad": (i, [v, v, v, i, _dp, C.POINTER(C.c_float)]),
         "spectral_fno_train_step": (i, [v, v, v, i, C.c_float, _dp, v]),
@@ -381,6 +386,11 @@ class Plan:
         _check(self.L.spectral_plan_generate_weights_iso(self.h, float(lam), d_i, d_j, m_i, m_j),
                "generate_weights_iso")
 
+    def generate_weights_grazing(self, lam: float, glance: float):
+        """Grazing-collision weights (gHat3 of the stand-alone generator)."""
+        _check(self.L.spectral_plan_generate_weights_grazing(self.h, float(lam), float(glance)),
+               "generate_weights_grazing")
+
     def generate_weights_landau(self, lam: float):
         """Landau-kernel weights (aniso_weights.c:370-425) on the device."""
         _check(self.L.spectral_plan_generate_weights_landau(self.h, float(lam)),
@@ -483,6 +493,10 @@ class Plan:
         _check(self.L.spectral_plan_set_learned(self.h, net.h if net else None, float(tol),
                                                 int(check_every)), "set_learned")
 
+    def set_learned_floor(self, eps: float):
+        """Floor of the spot check's relative distance (spectral_plan_set_learned_floor)."""
+        _check(self.L.spectral_plan_set_learned_floor(self.h, float(eps)), "set_learned_floor")
+
     def learned_stats(self) -> dict:
         c, k, fb = C.c_longlong(), C.c_longlong(), C.c_longlong()
         e = C.c_double()
@@ -570,6 +584,23 @@ class FourierOperator:
     def set_loss_floor(self, eps: float):
         _check(self.L.spectral_fno_set_loss_floor(self.h, float(eps)), "fno_set_loss_floor")
 
+    def set_equilibrium(self, on: bool, v=None):
+        """Equilibrium-exact form Q(f) = P(f) - P(M_f) (spectral_fno_set_equilibrium);
+        v: the N velocity nodes of the grid."""
+        vv = None
+        if on:
+            vv = np.ascontiguousarray(v, dtype=np.float64)
+            if vv.size != self.N:
+                raise SpectralError(f"expected {self.N} velocity nodes, got {vv.size}")
+            self._v = vv
+        _check(self.L.spectral_fno_set_equilibrium(self.h, 1 if on else 0,
+                                                   _p(vv) if on else None),
+               "fno_set_equilibrium")
+
+    @property
+    def equilibrium(self) -> bool:
+        return bool(self.L.spectral_fno_equilibrium(self.h) == 1)
+
     def predict(self, f, Q, B: int, stream: int = 0):
         """Network output (FP64 device) for f (FP64 device), no projection."""
         _check(self.L.spectral_fno_predict(self.h, _ptr(f), _ptr(Q), B, _stream(stream)),
@@ -593,9 +624,13 @@ class FourierOperator:
         return loss.value if want_loss else None
 
     def save(self, path: str):
+        extra = {}
+        if self.equilibrium:
+            extra["v"] = self._v
         np.savez(path, theta=self.get_params(), sigma=self.output_scale,
                  shape=np.array([self.N, self.width, self.modes, self.layers, self.hidden,
-                                 self.kind, self.precision]))
+                                 self.kind, self.precision]),
+                 equilibrium=np.array(int(self.equilibrium)), **extra)
 
     @classmethod
     def load(cls, path: str) -> "FourierOperator":
@@ -606,6 +641,8 @@ class FourierOperator:
         net = cls(N, width, modes, layers, hidden, kind=kind, precision=precision)
         net.set_params(d["theta"])
         net.output_scale = float(d["sigma"])
+        if "equilibrium" in d.files and int(d["equilibrium"]) == 1:
+            net.set_equilibrium(True, d["v"])
         return net
 
 

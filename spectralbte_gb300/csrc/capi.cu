@@ -21,6 +21,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 namespace sbte {
@@ -401,6 +402,152 @@ static int generate_landau_device(WeightsDev &wd, int N, double L_v, double lamb
     return rc;
 }
 
+// Grazing-collision weights of the stand-alone generator
+// (MPIcollisionRoutines.c:154-274) into wd.  gHat3(zeta, xi) depends on the
+// pair only through |zeta|, xi.zeta and |xi|, so the table is evaluated once
+// per distinct value of those three and scattered: on a uniform grid
+// zeta_i = zeta_0 + i h the sums of the index vectors, of their squares and
+// their dot product fix the three exactly (with zeta_0 = -N h / 2, the
+// generator's own grid, the centred offsets 2 i - N alone do).  The
+// quadrature rules are those of graze_kernel (weights.cu).
+static int graze_theta_edges(double glance, double *edges)
+{
+    int n = 0;
+    double t = sqrt(glance);
+    edges[n++] = t;
+    while (2.0 * t < M_PI && n < 62) {
+        t *= 2.0;
+        edges[n++] = t;
+    }
+    edges[n++] = M_PI;
+    return n - 1;
+}
+
+static int graze_panels(double L_eta, double L_v)
+{
+    const int K = (int)ceil(2.0 * sqrt(3.0) * L_eta * L_v / 8.0);
+    return K < 2 ? 2 : K;
+}
+
+static int generate_graze_device(WeightsDev &wd, int N, double L_v, double lambda, double glance,
+                                 const double *zeta, cudaStream_t st)
+{
+    if (!(glance > 0.0) || !(sqrt(glance) < 0.5 * M_PI) || N < 2 || N > 16 || !(L_v > 0.0)) {
+        set_error(kErrArg, "grazing weights: need 0 < glance < pi^2/4, 2 <= N <= 16, L_v > 0");
+        return kErrArg;
+    }
+    const long long n3 = (long long)N * N * N, n6 = n3 * n3;
+    const double h = zeta[1] - zeta[0];
+    bool uniform = h > 0.0;
+    double zmax = 0.0;
+    for (int i = 0; i < N; i++) {
+        uniform = uniform && fabs(zeta[i] - (zeta[0] + i * h)) <= 1e-12 * fabs(h) * N;
+        zmax = std::max(zmax, fabs(zeta[i]));
+    }
+    const bool centred = uniform && fabs(zeta[0] / h + 0.5 * N) < 1e-9;
+    // distinct keys in order of first appearance, and each entry's key index
+    std::vector<int> map((size_t)n6);
+    std::vector<double> pairs;
+    std::unordered_map<unsigned long long, int> seen;
+    seen.reserve((size_t)std::min<long long>(n6, 1 << 22));
+    for (long long z = 0; z < n3; z++) {
+        const int zi[3] = {(int)(z / (N * N)), (int)((z / N) % N), (int)(z % N)};
+        for (long long x = 0; x < n3; x++) {
+            const int xi[3] = {(int)(x / (N * N)), (int)((x / N) % N), (int)(x % N)};
+            unsigned long long key;
+            if (centred) {
+                long long a = 0, d = 0, c = 0;
+                for (int q = 0; q < 3; q++) {
+                    const long long kz = 2 * zi[q] - N, kx = 2 * xi[q] - N;
+                    a += kz * kz;
+                    d += kz * kx;
+                    c += kx * kx;
+                }
+                key = ((unsigned long long)a << 42) | ((unsigned long long)(d + (1 << 20)) << 21) |
+                      (unsigned long long)c;
+            } else if (uniform) {
+                unsigned long long sz = 0, qz = 0, sx = 0, qx = 0, d = 0;
+                for (int q = 0; q < 3; q++) {
+                    sz += zi[q];
+                    qz += zi[q] * zi[q];
+                    sx += xi[q];
+                    qx += xi[q] * xi[q];
+                    d += zi[q] * xi[q];
+                }
+                key = (sz << 58) | (qz << 48) | (sx << 42) | (qx << 32) | d;
+            } else {
+                key = (unsigned long long)(z * n3 + x);
+            }
+            auto it = seen.find(key);
+            int id;
+            if (it == seen.end()) {
+                id = (int)seen.size();
+                seen.emplace(key, id);
+                const double pz[6] = {zeta[zi[0]], zeta[zi[1]], zeta[zi[2]],
+                                      zeta[xi[0]], zeta[xi[1]], zeta[xi[2]]};
+                pairs.insert(pairs.end(), pz, pz + 6);
+            } else {
+                id = it->second;
+            }
+            map[(size_t)(z * n3 + x)] = id;
+        }
+    }
+    const int npairs = (int)(pairs.size() / 6);
+    if (wd.N != N || !wd.w64) {
+        wd.release();
+        SBTE_TRY(dalloc(&wd.w64, (size_t)n6));
+        wd.N = N;
+    }
+    dfree(wd.w32);
+    dfree(wd.w32x2);
+    dfree(wd.wsym);
+    std::vector<double> gx, gw;
+    gl_nodes(16, gx, gw);
+    double te[64];
+    const int nte = graze_theta_edges(glance, te);
+    const int npan = graze_panels(zmax, L_v);
+    double *d_pairs = nullptr, *d_vals = nullptr, *d_te = nullptr, *d_gx = nullptr,
+           *d_gw = nullptr;
+    int *d_map = nullptr;
+    int rc = kOk;
+    auto cleanup = [&]() {
+        dfree(d_pairs); dfree(d_vals); dfree(d_te); dfree(d_gx); dfree(d_gw); dfree(d_map);
+    };
+    if ((rc = dalloc(&d_pairs, pairs.size())) || (rc = dalloc(&d_vals, (size_t)npairs)) ||
+        (rc = dalloc(&d_te, 64)) || (rc = dalloc(&d_gx, 16)) || (rc = dalloc(&d_gw, 16)) ||
+        (rc = dalloc(&d_map, (size_t)n6))) {
+        cleanup();
+        return rc;
+    }
+    cudaError_t e = cudaMemcpyAsync(d_pairs, pairs.data(), sizeof(double) * pairs.size(),
+                                    cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_map, map.data(), sizeof(int) * (size_t)n6, cudaMemcpyHostToDevice,
+                            st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_te, te, sizeof(double) * (nte + 1), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_gx, gx.data(), sizeof(double) * 16, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_gw, gw.data(), sizeof(double) * 16, cudaMemcpyHostToDevice, st);
+    // chunks of distinct pairs keep each launch short
+    for (int u0 = 0; u0 < npairs && e == cudaSuccess; u0 += 8192) {
+        const int nu = std::min(8192, npairs - u0);
+        e = weights_graze(d_vals + u0, d_pairs + 6LL * u0, nu, L_v, lambda, glance, npan, d_te,
+                          nte, d_gx, d_gw, st);
+        if (e == cudaSuccess) count(1);
+    }
+    if (e == cudaSuccess) e = weights_scatter(wd.w64, d_vals, d_map, n6, st);
+    if (e == cudaSuccess) count(1);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cleanup();
+    if (e != cudaSuccess) {
+        set_error(kErrCuda, "grazing weights: %s", cudaGetErrorString(e));
+        return kErrCuda;
+    }
+    return kOk;
+}
+
 static int generate_iso_device(WeightsDev &wd, const IsoWeightSpec &s,
                                cudaStream_t st)
 {
@@ -531,7 +678,8 @@ struct spectral_plan_s {
     long long lcalls = 0, lchecks = 0, lfallbacks = 0;
     double lerr = -1.0;
     bool lok = true;
-    double *lq = nullptr, *d_lerr = nullptr;
+    double lfloor = 0.0;  // spectral_plan_set_learned_floor
+    double *lq = nullptr, *d_lerr = nullptr, *d_lmsq = nullptr;
 
     ~spectral_plan_s()
     {
@@ -551,7 +699,7 @@ struct spectral_plan_s {
         for (cudaEvent_t e : host_events) cudaEventDestroy(e);
         if (copy_in) cudaStreamDestroy(copy_in);
         if (copy_out) cudaStreamDestroy(copy_out);
-        dfree(lq); dfree(d_lerr);
+        dfree(lq); dfree(d_lerr); dfree(d_lmsq);
         dfree(d_x); dfree(d_dx); dfree(fconv); dfree(f1); dfree(ftmp); dfree(f_l); dfree(f_r);
         if (graph_exec) cudaGraphExecDestroy(graph_exec);
         if (graph) cudaGraphDestroy(graph);
@@ -884,10 +1032,13 @@ static int computeQ_dev(spectral_plan_s *p, const double *f, double *Q, int B,
 
 // The learned operator with its periodic spot check.  Every levery-th call
 // one instance (rotating) is recomputed with the plain FP32 operator and
-// conservation; a rel-L2 distance above ltol switches the plan to the plain
-// operator (flags without SPECTRAL_LEARNED) for this call and for every call
-// up to the next check that passes.  The network output is always projected
-// by the FP64 conservation step.
+// conservation; a relative distance above ltol switches the plan to the
+// plain operator (flags without SPECTRAL_LEARNED) for this call and for every
+// call up to the next check that passes.  The distance is |Q_net - Q| / |Q|,
+// or with a floor eps > 0 |Q_net - Q| / sqrt(|Q|^2 + eps * mean_b |Q_net,b|^2)
+// (the batch's mean squared norm of the network output), the normalisation
+// of the training loss.  The network output is always projected by the FP64
+// conservation step.
 static int learned_q(spectral_plan_s *p, const double *f, double *Q, int B, int flags,
                      cudaStream_t st)
 {
@@ -910,11 +1061,18 @@ static int learned_q(spectral_plan_s *p, const double *f, double *Q, int B, int 
     if (!p->lq) {
         SBTE_TRY(dalloc(&p->lq, n3));
         SBTE_TRY(dalloc(&p->d_lerr, 1));
+        SBTE_TRY(dalloc(&p->d_lmsq, 1));
     }
     const int b = (int)((p->lchecks++) % B);
     SBTE_TRY(q_fp32(p, f + (long long)b * n3, p->lq, 1, false, st));
     SBTE_LAUNCH(conserve_batch(p->lq, 1, p->d_v, p->cons, st, p->d_status), 1);
-    SBTE_TRY(rel_l2_device(Q + (long long)b * n3, p->lq, n3, p->d_lerr, st));
+    if (p->lfloor > 0.0) {
+        SBTE_TRY(batch_sumsq(Q, (long long)B * n3, p->d_lmsq, st));
+        SBTE_TRY(rel_l2_floor_device(Q + (long long)b * n3, p->lq, n3, p->d_lmsq, p->lfloor, B,
+                                     p->d_lerr, st));
+    } else {
+        SBTE_TRY(rel_l2_device(Q + (long long)b * n3, p->lq, n3, p->d_lerr, st));
+    }
     SBTE_CUDA(cudaMemcpyAsync(&p->lerr, p->d_lerr, sizeof(double), cudaMemcpyDeviceToHost, st));
     SBTE_CUDA(cudaStreamSynchronize(st));
     p->lok = std::isfinite(p->lerr) && p->lerr <= p->ltol;
@@ -1054,6 +1212,16 @@ int spectral_plan_generate_weights_iso(spectral_plan *p, double lambda, double d
     s.m_j = m_j;
     s.zeta = p->zeta;
     return generate_iso_device(p->W, s, p->stream);
+}
+
+int spectral_plan_generate_weights_grazing(spectral_plan *p, double lambda, double glance)
+{
+    if (!p) {
+        set_error(kErrArg, "spectral_plan_generate_weights_grazing: null plan");
+        return kErrArg;
+    }
+    SBTE_CUDA(cudaSetDevice(p->device));
+    return generate_graze_device(p->W, p->N, p->L_v, lambda, glance, p->zeta.data(), p->stream);
 }
 
 int spectral_plan_generate_weights_landau(spectral_plan *p, double lambda)
@@ -1523,6 +1691,16 @@ int spectral_plan_set_learned(spectral_plan *p, spectral_fno *net, double tol, i
     p->lcalls = p->lchecks = p->lfallbacks = 0;
     p->lerr = -1.0;
     p->lok = true;
+    return kOk;
+}
+
+int spectral_plan_set_learned_floor(spectral_plan *p, double eps)
+{
+    if (!p || !(eps >= 0.0)) {
+        set_error(kErrArg, "spectral_plan_set_learned_floor: need a plan and eps >= 0");
+        return kErrArg;
+    }
+    p->lfloor = eps;
     return kOk;
 }
 
@@ -2043,6 +2221,67 @@ void initialize_weights_AnIso(int nodes, double *zeta, double Lv, double lam, in
         report("initialize_weights_AnIso");
     }
     fclose(fid);
+}
+
+// The stand-alone weight generator (exec/MPIWeightGenerator.c, the `weights_`
+// executable: `weights_ N glance beta lambda L_v`) on one GPU: the grid of
+// MPIWeightGenerator.c:63-74 (h_v = 2 L_v / (N - 1), h_eta = 2 pi / (N h_v),
+// eta_i = -N h_eta / 2 + i h_eta), then Landau weights (glance = 0,
+// gHat3L) or grazing-collision weights (gHat3), written to the file name of
+// :79-83 unless that file exists (:92-95).  beta is accepted and unused, as
+// in the reference.  initialize_weights_AnIso then loads the file.
+int spectral_weights_generator(int N, double glance, double beta, double lambda, double L_v)
+{
+    (void)beta;
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (N < 2 || !(L_v > 0.0) || glance < 0.0) {
+        set_error(kErrArg, "spectral_weights_generator: need N >= 2, L_v > 0, glance >= 0");
+        return kErrArg;
+    }
+    char name[256];
+    if (glance == 0.0)
+        snprintf(name, sizeof(name), "Weights/N%d_Aniso_L_v%g_lambda%g_Landau.wts", N, L_v, lambda);
+    else
+        snprintf(name, sizeof(name), "Weights/N%d_AnIso_L_v%g_lambda%g_glance%g.wts", N, L_v,
+                 lambda, glance);
+    if (FILE *fid = fopen(name, "r")) {
+        fclose(fid);
+        return kOk;  // "Stored weights already computed!"
+    }
+    std::vector<double> eta(N);
+    const double h_v = 2.0 * L_v / (double)(N - 1), h_eta = (2.0 * M_PI / N) / h_v;
+    const double L_eta = 0.5 * N * h_eta;
+    for (int i = 0; i < N; i++) eta[i] = -L_eta + (double)i * h_eta;
+    SBTE_TRY(ensure_device());
+    cudaStream_t st = g_coll.plan ? g_coll.plan->stream : nullptr;
+    WeightsDev wd;
+    int rc = glance == 0.0 ? generate_landau_device(wd, N, L_v, lambda, eta.data(), st)
+                           : generate_graze_device(wd, N, L_v, lambda, glance, eta.data(), st);
+    const long long n3 = (long long)N * N * N;
+    std::vector<double> host;
+    if (rc == kOk) {
+        host.resize((size_t)(n3 * n3));
+        if (cudaMemcpy(host.data(), wd.w64, sizeof(double) * n3 * n3, cudaMemcpyDeviceToHost) !=
+            cudaSuccess) {
+            set_error(kErrCuda, "spectral_weights_generator: weights D2H failed");
+            rc = kErrCuda;
+        }
+    }
+    wd.release();
+    if (rc != kOk) return rc;
+    FILE *fid = fopen(name, "w");
+    if (!fid) {
+        set_error(kErrWeights, "cannot open %s for writing", name);
+        return kErrWeights;
+    }
+    const size_t wrote = fwrite(host.data(), sizeof(double), host.size(), fid);
+    const bool ok = wrote == host.size() && fflush(fid) == 0;
+    fclose(fid);
+    if (!ok) {
+        set_error(kErrWeights, "storing the weights in %s failed", name);
+        return kErrWeights;
+    }
+    return kOk;
 }
 
 void dealloc_weights(int N, double **conv_weights)

@@ -212,7 +212,7 @@ maxwellian_kernel(const double *__restrict__ f, double *__restrict__ M,
                                                  (v[j] - u1) * (v[j] - u1) +
                                                  (v[k] - u2) * (v[k] - u2)));
         M[off + x] = Mx;
-        g[off + x] = f[off + x] - (Mref ? Mref[off + x] : Mx);
+        if (g) g[off + x] = f[off + x] - (Mref ? Mref[off + x] : Mx);
     }
     if (mom && threadIdx.x == 0) {
         mom[5 * blockIdx.x + 0] = rho;

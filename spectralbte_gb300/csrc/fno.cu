@@ -15,6 +15,14 @@
 // + e % 8, r(e) = l(e) + 8: y is then a quadratic form in x, as Q is in f,
 // with the form sum_e (K_e * f)(v) (K'_e * f)(v) of a separable
 // approximation of the collision kernel in Fourier space.
+// Equilibrium-exact form (spectral_fno_set_equilibrium): the operator is
+//   Q(f) = s_f^2 sigma y(f / s_f) - s_M^2 sigma y(M_f / s_M),
+// with M_f the Maxwellian that has the density, velocity and temperature of
+// f (momentRoutines.c formulas, unit mass).  Q then vanishes identically at
+// equilibrium (f = M_f), as the collision operator does.  Both terms run as
+// one batch of 2B instances [f; M_f] through the same kernels, and training
+// minimises the same loss on the difference (the M half of the batch gets
+// the output gradient times -(s_M / s_f)^2).
 // theta(m, p) = 2 pi m.p / N over the lowest Km^3 modes m in [-Km/2, Km/2)^3.
 // The spectral weights are shared by all modes of equal |m|^2 (the collision
 // operator is isotropic) and are real.  Training minimises the mean over
@@ -37,6 +45,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <type_traits>
 #include <vector>
 
 using sbte::fno::bf16;
@@ -115,6 +124,44 @@ __global__ void from_pb_kernel(const float *__restrict__ y, const float *__restr
             Q[(long long)b * P + p] = sb * sb * (double)sigma * (double)tile[threadIdx.x][r];
         }
     }
+}
+
+// Equilibrium form: Q[b][p] = sigma (s[b]^2 y[p][b] - s[B+b]^2 y[p][B+b])
+// (FP64) for the B instances whose Maxwellians sit at B..2B-1.
+__global__ void from_pb_diff_kernel(const float *__restrict__ y, const float *__restrict__ s,
+                                    float sigma, int B, int Bp, long long P,
+                                    double *__restrict__ Q)
+{
+    __shared__ float tf[32][33], tm[32][33];
+    const long long p0 = (long long)blockIdx.x * 32;
+    const int b0 = blockIdx.y * 32;
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+        const long long p = p0 + r;
+        const int b = b0 + threadIdx.x;
+        const bool in = p < P && b < B;
+        tf[r][threadIdx.x] = in ? y[p * Bp + b] : 0.f;
+        tm[r][threadIdx.x] = in ? y[p * Bp + B + b] : 0.f;
+    }
+    __syncthreads();
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+        const int b = b0 + r;
+        const long long p = p0 + threadIdx.x;
+        if (b < B && p < P) {
+            const double sf = s[b], sm = s[B + b];
+            Q[(long long)b * P + p] =
+                (double)sigma * (sf * sf * (double)tf[threadIdx.x][r] -
+                                 sm * sm * (double)tm[threadIdx.x][r]);
+        }
+    }
+}
+
+// out[b][p] = (double) in[b][p] for n values.
+__global__ void f32_to_f64_kernel(const float *__restrict__ in, double *__restrict__ out,
+                                  long long n)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        out[i] = (double)in[i];
 }
 
 template <typename E> __device__ __forceinline__ void st_e8(E *dst, const float (&v)[8])
@@ -384,6 +431,60 @@ __global__ void loss_kernel(const float *__restrict__ y, const float *__restrict
     }
 }
 
+// Equilibrium form of loss_kernel.  y holds the outputs of f (b < B) and of
+// its Maxwellian (b + B), both in their own scale s^2 sigma; the residual of
+// instance b is r = y_b - rho_b y_{B+b} - t_b with rho_b = (s_{B+b} / s_b)^2.
+// dy_b = 2 r / (den_b B) gs, dy_{B+b} = -rho_b dy_b, 0 for padding;
+// loss += r^2 / (den_b B); dc2 += sum dy.
+__global__ void loss_diff_kernel(const float *__restrict__ y, const float *__restrict__ t,
+                                 const float *__restrict__ den, const float *__restrict__ gs,
+                                 const float *__restrict__ s, float *__restrict__ dy,
+                                 double *loss, float *dc2, long long P, int B, int Bp)
+{
+    const float scale = gs[0];
+    __shared__ double r1[32];
+    __shared__ float r2[32];
+    double l = 0.0;
+    float g = 0.f;
+    const long long n = P * Bp;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int b = (int)(i % Bp);
+        if (b < B) {
+            const float q = s[B + b] / s[b];
+            const float rho = q * q;
+            const float r = y[i] - rho * y[i + B] - t[i];
+            const float inv = 1.f / (den[b] * (float)B);
+            const float d = 2.f * r * inv * scale;
+            dy[i] = d;
+            dy[i + B] = -rho * d;
+            l += (double)r * r * inv;
+            g += d - rho * d;
+        } else if (b >= 2 * B) {
+            dy[i] = 0.f;
+        }
+    }
+    for (int o = 16; o; o >>= 1) {
+        l += __shfl_xor_sync(0xffffffffu, l, o);
+        g += __shfl_xor_sync(0xffffffffu, g, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        r1[threadIdx.x >> 5] = l;
+        r2[threadIdx.x >> 5] = g;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0;
+        float b2 = 0.f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+            a += r1[w];
+            b2 += r2[w];
+        }
+        atomicAdd(loss, a);
+        atomicAdd(dc2, b2);
+    }
+}
+
 __global__ void adam_kernel(float *__restrict__ p, const float *__restrict__ g,
                             const float *__restrict__ gs, float *__restrict__ m,
                             float *__restrict__ v, long long n, float lr, float b1, float b2,
@@ -428,6 +529,59 @@ __global__ void rel_l2_kernel(const double *__restrict__ A, const double *__rest
             y += s2[w];
         }
         out[0] = y > 0.0 ? sqrt(x / y) : sqrt(x);
+    }
+}
+
+// out[0] += sum of A[i]^2 over n values (FP64; out zeroed by the caller).
+__global__ void sumsq_kernel(const double *__restrict__ A, long long n, double *out)
+{
+    __shared__ double red[32];
+    double a = 0.0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        a += A[i] * A[i];
+    for (int o = 16; o; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = a;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w];
+        atomicAdd(out, t);
+    }
+}
+
+// out[0] = |A - R| / sqrt(|R|^2 + eps * msq[0] / B) for one instance (the
+// floored relative distance of the spot check: msq is the batch's summed
+// squared norm of the network output, so eps * msq / B is eps times its
+// mean squared instance norm).
+__global__ void rel_l2_floor_kernel(const double *__restrict__ A, const double *__restrict__ R,
+                                    long long n, const double *__restrict__ msq, double eps,
+                                    int B, double *out)
+{
+    __shared__ double s1[32], s2[32];
+    double a = 0.0, b = 0.0;
+    for (long long i = threadIdx.x; i < n; i += blockDim.x) {
+        const double d = A[i] - R[i];
+        a += d * d;
+        b += R[i] * R[i];
+    }
+    for (int o = 16; o; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        s1[threadIdx.x >> 5] = a;
+        s2[threadIdx.x >> 5] = b;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double x = 0.0, y = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+            x += s1[w];
+            y += s2[w];
+        }
+        const double den = y + eps * msq[0] / (double)B;
+        out[0] = den > 0.0 ? sqrt(x / den) : sqrt(x);
     }
 }
 
@@ -567,6 +721,12 @@ struct spectral_fno_s {
               oc2 = 0;
     float sigma = 1.f;
     float floor_eps = 0.f;  // loss: |y - t|^2 / (|t|^2 + floor_eps * mean_b |t_b|^2)
+    // equilibrium-exact form (spectral_fno_set_equilibrium): the velocity
+    // nodes for the Maxwellian of f, and the FP64 input batch [f; M_f]
+    int eq = 0;
+    double *d_v = nullptr;
+    double *fM = nullptr;
+    int capM = 0;
     float *params = nullptr, *grads = nullptr, *am = nullptr, *av = nullptr;
     long long adam_t = 0;
     int prec = 0;                      // 0: BF16 elements, 1: FP16 elements
@@ -615,6 +775,8 @@ struct spectral_fno_s {
         free_acts();
         for (float *q : {params, grads, am, av, F, G, Fu, gs}) cudaFree(q);
         cudaFree(cls);
+        cudaFree(d_v);
+        cudaFree(fM);
     }
 };
 
@@ -958,8 +1120,12 @@ int backward(spectral_fno_s *n, int B, int Bp, cudaStream_t st)
     const Ext ext(n, Bp);
     FNO_LAUNCH(cudaMemsetAsync(gr, 0, sizeof(float) * n->nparams, st));
     FNO_LAUNCH(cudaMemsetAsync(n->d_loss, 0, sizeof(double), st));
-    loss_kernel<<<ew_grid(P * Bp / 8), kEw, 0, st>>>(n->y, n->t, n->den, n->gs, n->dy,
-                                                      n->d_loss, gr + n->oc2, P * Bp, B, Bp);
+    if (n->eq)  // B real instances at 0..B-1, their Maxwellians at B..2B-1
+        loss_diff_kernel<<<ew_grid(P * Bp / 8), kEw, 0, st>>>(
+            n->y, n->t, n->den, n->gs, n->s, n->dy, n->d_loss, gr + n->oc2, P, B, Bp);
+    else
+        loss_kernel<<<ew_grid(P * Bp / 8), kEw, 0, st>>>(n->y, n->t, n->den, n->gs, n->dy,
+                                                          n->d_loss, gr + n->oc2, P * Bp, B, Bp);
     E *dU = reinterpret_cast<E *>(n->dU);
     if (n->kind == 1)
         proj_bwd_bil_kernel<E><<<ew_grid(P * Hd * Bp / 8), kEw, 0, st>>>(
@@ -1038,12 +1204,57 @@ int backward(spectral_fno_s *n, int B, int Bp, cudaStream_t st)
     return kOk;
 }
 
+// The equilibrium form's input batch: fM[0..B) = f, fM[B..2B) = the
+// Maxwellian of each f (unit mass and Boltzmann constant), FP64.
+template <typename T>
+int eq_inputs(spectral_fno_s *n, const T *f, int B, cudaStream_t st)
+{
+    if (!n->d_v) {
+        set_error(kErrNotInit, "equilibrium form: the network has no velocity grid");
+        return kErrNotInit;
+    }
+    const long long P = n->P;
+    if (2 * B > n->capM) {
+        cudaFree(n->fM);
+        n->fM = nullptr;
+        n->capM = 0;
+        cudaError_t e = cudaMalloc((void **)&n->fM, sizeof(double) * (size_t)(2 * B) * P);
+        if (e != cudaSuccess) {
+            n->fM = nullptr;
+            set_error(kErrNoMem, "cudaMalloc of the equilibrium input batch failed: %s",
+                      cudaGetErrorString(e));
+            return kErrNoMem;
+        }
+        n->capM = 2 * B;
+    }
+    if constexpr (std::is_same<T, double>::value) {
+        FNO_LAUNCH(cudaMemcpyAsync(n->fM, f, sizeof(double) * (size_t)B * P,
+                                   cudaMemcpyDeviceToDevice, st));
+    } else {
+        f32_to_f64_kernel<<<ew_grid((long long)B * P / 8), kEw, 0, st>>>(f, n->fM,
+                                                                         (long long)B * P);
+        add_launches(1);
+        FNO_LAUNCH(cudaGetLastError());
+    }
+    FNO_LAUNCH(maxwellian_split(n->fM, n->fM + (long long)B * P, nullptr, nullptr, B, n->N,
+                                n->d_v, 1.0, 1.0, nullptr, st));
+    add_launches(1);
+    return kOk;
+}
+
 template <typename E, typename T>
 int loss_and_grad(spectral_fno_s *n, const T *f, const T *Q, int B, cudaStream_t st)
 {
-    const int Bp = (B + 7) / 8 * 8;
+    // the equilibrium form runs [f; M_f], 2B instances, through the network
+    const int Bt = n->eq ? 2 * B : B;
+    const int Bp = (Bt + 7) / 8 * 8;
     FNO_TRY(ensure(n, Bp, true));
-    FNO_TRY((forward<E, T>(n, f, B, Bp, true, st)));
+    if (n->eq) {
+        FNO_TRY(eq_inputs<T>(n, f, B, st));
+        FNO_TRY((forward<E, double>(n, n->fM, Bt, Bp, true, st)));
+    } else {
+        FNO_TRY((forward<E, T>(n, f, B, Bp, true, st)));
+    }
     const long long P = n->P;
     to_pb_kernel<T><<<dim3((unsigned)((P + 31) / 32), (unsigned)((Bp + 31) / 32)), dim3(32, 8),
                       0, st>>>(Q, n->s, 2, 1.f / n->sigma, B, Bp, P, n->t);
@@ -1078,15 +1289,24 @@ int fno_predict(spectral_fno_s *n, const double *f, double *Q, int B, cudaStream
 {
     if (B < 1) return kOk;
     if (cudaSetDevice(n->device) != cudaSuccess) return kErrCuda;
-    const int Bp = (B + 7) / 8 * 8;
+    const int Bt = n->eq ? 2 * B : B;
+    const int Bp = (Bt + 7) / 8 * 8;
     FNO_TRY(ensure(n, Bp, n->cap_train));
+    const double *in = f;
+    if (n->eq) {
+        FNO_TRY(eq_inputs<double>(n, f, B, st));
+        in = n->fM;
+    }
     if (n->prec == 1)
-        FNO_TRY((forward<f16, double>(n, f, B, Bp, n->cap_train, st)));
+        FNO_TRY((forward<f16, double>(n, in, Bt, Bp, n->cap_train, st)));
     else
-        FNO_TRY((forward<bf16, double>(n, f, B, Bp, n->cap_train, st)));
+        FNO_TRY((forward<bf16, double>(n, in, Bt, Bp, n->cap_train, st)));
     const long long P = n->P;
-    from_pb_kernel<<<dim3((unsigned)((P + 31) / 32), (unsigned)((Bp + 31) / 32)), dim3(32, 8), 0,
-                     st>>>(n->y, n->s, n->sigma, B, Bp, P, Q);
+    const dim3 grid((unsigned)((P + 31) / 32), (unsigned)((Bp + 31) / 32));
+    if (n->eq)
+        from_pb_diff_kernel<<<grid, dim3(32, 8), 0, st>>>(n->y, n->s, n->sigma, B, Bp, P, Q);
+    else
+        from_pb_kernel<<<grid, dim3(32, 8), 0, st>>>(n->y, n->s, n->sigma, B, Bp, P, Q);
     add_launches(1);
     FNO_LAUNCH(cudaGetLastError());
     return kOk;
@@ -1097,7 +1317,40 @@ int fno_grid_n(const spectral_fno_s *n) { return n->N; }
 int fno_reserve(spectral_fno_s *n, int B)
 {
     if (cudaSetDevice(n->device) != cudaSuccess) return kErrCuda;
-    return ensure(n, (B + 7) / 8 * 8, n->cap_train);
+    const int Bt = n->eq ? 2 * B : B;
+    FNO_TRY(ensure(n, (Bt + 7) / 8 * 8, n->cap_train));
+    if (n->eq && 2 * B > n->capM) {
+        cudaFree(n->fM);
+        n->fM = nullptr;
+        n->capM = 0;
+        if (cudaMalloc((void **)&n->fM, sizeof(double) * (size_t)(2 * B) * n->P) != cudaSuccess) {
+            n->fM = nullptr;
+            set_error(kErrNoMem, "cudaMalloc of the equilibrium input batch failed");
+            return kErrNoMem;
+        }
+        n->capM = 2 * B;
+    }
+    return kOk;
+}
+
+int fno_equilibrium(const spectral_fno_s *n) { return n->eq; }
+
+int batch_sumsq(const double *A, long long n, double *out, cudaStream_t st)
+{
+    FNO_LAUNCH(cudaMemsetAsync(out, 0, sizeof(double), st));
+    fno::sumsq_kernel<<<fno::ew_grid(n / 8), fno::kEw, 0, st>>>(A, n, out);
+    add_launches(1);
+    FNO_LAUNCH(cudaGetLastError());
+    return kOk;
+}
+
+int rel_l2_floor_device(const double *A, const double *R, long long n3, const double *msq,
+                        double eps, int B, double *out, cudaStream_t st)
+{
+    fno::rel_l2_floor_kernel<<<1, 512, 0, st>>>(A, R, n3, msq, eps, B, out);
+    add_launches(1);
+    FNO_LAUNCH(cudaGetLastError());
+    return kOk;
 }
 
 int rel_l2_device(const double *A, const double *R, long long n3, double *out, cudaStream_t st)
@@ -1334,6 +1587,36 @@ int spectral_fno_set_output_scale(spectral_fno *n, float sigma)
 }
 
 float spectral_fno_output_scale(spectral_fno *n) { return n ? n->sigma : 0.f; }
+
+int spectral_fno_set_equilibrium(spectral_fno *n, int on, const double *v)
+{
+    if (!n || (on && !v)) {
+        set_error(kErrArg, "spectral_fno_set_equilibrium: need a handle and, to switch on, "
+                           "the N velocity nodes");
+        return kErrArg;
+    }
+    if (cudaSetDevice(n->device) != cudaSuccess) return kErrCuda;
+    if (on) {
+        for (int i = 1; i < n->N; i++)
+            if (!(v[i] > v[i - 1])) {
+                set_error(kErrArg, "spectral_fno_set_equilibrium: nodes must increase");
+                return kErrArg;
+            }
+        if (!n->d_v) {
+            cudaError_t e = cudaMalloc((void **)&n->d_v, sizeof(double) * n->N);
+            if (e != cudaSuccess) {
+                n->d_v = nullptr;
+                set_error(kErrNoMem, "cudaMalloc: %s", cudaGetErrorString(e));
+                return kErrNoMem;
+            }
+        }
+        FNO_LAUNCH(cudaMemcpy(n->d_v, v, sizeof(double) * n->N, cudaMemcpyHostToDevice));
+    }
+    n->eq = on ? 1 : 0;
+    return kOk;
+}
+
+int spectral_fno_equilibrium(spectral_fno *n) { return n ? n->eq : -1; }
 
 int spectral_fno_set_loss_floor(spectral_fno *n, float eps)
 {

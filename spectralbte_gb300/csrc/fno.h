@@ -20,5 +20,14 @@ int rel_l2_device(const double *A, const double *Bref, long long n3, double *out
                   cudaStream_t st);
 // Add n kernel launches to the library's launch counter.
 void add_launches(int n);
+// 1 when the network runs in its equilibrium-exact form (fno.cu header).
+int fno_equilibrium(const spectral_fno_s *net);
+// out[0] = sum of the squares of n FP64 device values (device double).
+int batch_sumsq(const double *A, long long n, double *out, cudaStream_t st);
+// out[0] = |A - R| / sqrt(|R|^2 + eps * msq[0] / B) for one instance of n3
+// values: the spot check's relative distance with a floor of eps times the
+// batch's mean squared instance norm (msq from batch_sumsq over B instances).
+int rel_l2_floor_device(const double *A, const double *R, long long n3, const double *msq,
+                        double eps, int B, double *out, cudaStream_t st);
 
 }  // namespace sbte

@@ -151,7 +151,7 @@ cudaError_t conserve_species(double **Qptrs_dev, const double *v,
 // instances: M = Maxwellian with the (rho, u, T) of f, computed with the
 // momentRoutines.c formulas (mass, KB); g = f - Mref where Mref = M of the
 // instance's "first" argument (the reference always subtracts M_i).
-// When Mref == nullptr, g = f - M.
+// When Mref == nullptr, g = f - M; when g == nullptr, only M is written.
 cudaError_t maxwellian_split(const double *f, double *M, double *g,
                              const double *Mref, int B, int N,
                              const double *v, double mass, double KB,
@@ -209,6 +209,15 @@ cudaError_t weights_iso(double *W, int row0, int nrows, const double *zeta,
 // Landau weights (aniso_weights.c:370-425) for rows [row0, row0 + nrows)
 // into W[row - row0][N^3] (FP64); glx, glw: the 64-point Gauss-Legendre rule
 // on [-1, 1] (device).
+// Grazing-collision weights (MPIcollisionRoutines.c:33-205), one value per
+// (zeta, xi) pair of pairs[6 u ..]: npan 16-point panels in r and phi, the
+// nte theta panels between te[0..nte]; glx, glw the 16-point rule.
+cudaError_t weights_graze(double *vals, const double *pairs, int npairs, double L_v,
+                          double lambda, double glance, int npan, const double *te, int nte,
+                          const double *glx, const double *glw, cudaStream_t st);
+// W[e] = vals[map[e]], e < n.
+cudaError_t weights_scatter(double *W, const double *vals, const int *map, long long n,
+                            cudaStream_t st);
 cudaError_t weights_landau(double *W, int row0, int nrows, const double *zeta, int N,
                            double L_v, double lambda, const double *glx, const double *glw,
                            cudaStream_t st);

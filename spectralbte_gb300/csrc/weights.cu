@@ -195,7 +195,118 @@ landau_kernel(double *__restrict__ W, int row0, int nrows, const double *__restr
     W[e] = 2.0 * M_PI * (rhalf * outer);
 }
 
+// gHat3 of the grazing-collision generator (MPIcollisionRoutines.c:33-205)
+// for one (zeta, xi) pair per CTA: pairs[6 u .. 6 u + 5] = zeta1..3, xi1..3.
+//   W = 4 pi^2 int_0^{L_v} r^{lambda+2} int_0^pi sin(phi) J0(r sin(phi) xp)
+//         [I1(r, phi) + C(r, phi) taylor] dphi dr,
+//   I1 = int_{sqrt g}^pi (8/pi) g theta^-4 [cos(a7 (1 - cos th) - a6)
+//         J0(a8 sin th) - cos a6] dth,
+// a6 = r cos(phi) xz, a7 = r cos(phi) zl / 2, a8 = r sin(phi) zl / 2,
+// C = -a8^2 cos(a6) / 4 + a7 sin(a6) / 2, taylor = (2/pi) log g / log sin(g/2)
+// (the reference's analytic Coulomb-case term for theta < sqrt g).  Every
+// level is composite 16-point Gauss-Legendre: npan equal panels in r and phi,
+// and the nte panels between the edges te[] in theta (graded geometrically
+// from sqrt g, where the integrand grows like theta^-2).  The reference
+// integrates with GSL QAG / CQUAD to 1e-6; these rules converge to ~1e-13.
+// The threads of a CTA share the npan^2 * 256 (r, phi) nodes; each node's
+// theta integral runs in one thread, and a block sum finishes the weight.
+__global__ void __launch_bounds__(256)
+graze_kernel(double *__restrict__ out, const double *__restrict__ pairs, double L_v,
+             double lambda, double glance, double taylor, int npan,
+             const double *__restrict__ te, int nte, const double *__restrict__ glx,
+             const double *__restrict__ glw)
+{
+    __shared__ double sx[16], sw[16], se[64], red[8];
+    if (threadIdx.x < 16) {
+        sx[threadIdx.x] = glx[threadIdx.x];
+        sw[threadIdx.x] = glw[threadIdx.x];
+    }
+    for (int q = threadIdx.x; q <= nte; q += blockDim.x) se[q] = te[q];
+    __syncthreads();
+    const double *q = pairs + 6LL * blockIdx.x;
+    const double z1 = q[0], z2 = q[1], z3 = q[2], x1 = q[3], x2 = q[4], x3 = q[5];
+    const double zetalen2 = z1 * z1 + z2 * z2 + z3 * z3;
+    const double xilen2 = x1 * x1 + x2 * x2 + x3 * x3;
+    const double xizeta = x1 * z1 + x2 * z2 + x3 * z3;
+    const double zl = sqrt(zetalen2);
+    double xp;
+    if (((xilen2 - xizeta * xizeta / zetalen2) < 0) || (zetalen2 == 0))
+        xp = 0;
+    else
+        xp = sqrt(xilen2 - xizeta * xizeta / zetalen2);
+    const double xz = zl != 0 ? xizeta / zl : 0.0;
+    const double hr = L_v / npan, hp = M_PI / npan;
+    const int nn = npan * 16;
+    double acc = 0.0;
+    for (int t = threadIdx.x; t < nn * nn; t += blockDim.x) {
+        const int ir = t / nn, ip = t - ir * nn;
+        const double r = hr * (ir >> 4) + 0.5 * hr * (sx[ir & 15] + 1.0);
+        const double wr = 0.5 * hr * sw[ir & 15];
+        const double phi = hp * (ip >> 4) + 0.5 * hp * (sx[ip & 15] + 1.0);
+        const double wp = 0.5 * hp * sw[ip & 15];
+        double sph, cph;
+        sincos(phi, &sph, &cph);
+        const double a6 = r * cph * xz, a7 = 0.5 * r * cph * zl, a8 = 0.5 * r * sph * zl;
+        double s6, c6;
+        sincos(a6, &s6, &c6);
+        double i1 = 0.0;
+        for (int pt = 0; pt < nte; pt++) {
+            const double t0 = se[pt], ht = se[pt + 1] - se[pt];
+            double s = 0.0;
+            for (int qt = 0; qt < 16; qt++) {
+                const double th = t0 + 0.5 * ht * (sx[qt] + 1.0);
+                double sth, cth;
+                sincos(th, &sth, &cth);
+                const double bcos = (8.0 / M_PI) * (glance / (th * th)) / (th * th);
+                s += sw[qt] * bcos * (cos(a7 * (1.0 - cth) - a6) * j0(a8 * sth) - c6);
+            }
+            i1 += 0.5 * ht * s;
+        }
+        const double C = -0.25 * a8 * a8 * c6 + 0.5 * a7 * s6;
+        acc += wr * pow(r, lambda + 2) * wp * sph * j0(r * sph * xp) * (i1 + C * taylor);
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double tot = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) tot += red[w];
+        out[blockIdx.x] = 4.0 * M_PI * M_PI * tot;
+    }
+}
+
+// W[e] = vals[map[e]] for the n entries of a weight table.
+__global__ void scatter_kernel(double *__restrict__ W, const double *__restrict__ vals,
+                               const int *__restrict__ map, long long n)
+{
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+         e += (long long)gridDim.x * blockDim.x)
+        W[e] = vals[map[e]];
+}
+
 }  // namespace
+
+cudaError_t weights_graze(double *vals, const double *pairs, int npairs, double L_v,
+                          double lambda, double glance, int npan, const double *te, int nte,
+                          const double *glx, const double *glw, cudaStream_t st)
+{
+    if (npairs <= 0) return cudaSuccess;
+    if (nte < 1 || nte > 62 || npan < 1 || !(glance > 0.0)) return cudaErrorInvalidValue;
+    const double taylor = (2.0 / M_PI) * log(glance) / log(sin(0.5 * glance));
+    graze_kernel<<<npairs, 256, 0, st>>>(vals, pairs, L_v, lambda, glance, taylor, npan, te,
+                                         nte, glx, glw);
+    return cudaGetLastError();
+}
+
+cudaError_t weights_scatter(double *W, const double *vals, const int *map, long long n,
+                            cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    long long blocks = (n + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    scatter_kernel<<<(unsigned)blocks, 256, 0, st>>>(W, vals, map, n);
+    return cudaGetLastError();
+}
 
 cudaError_t weights_landau(double *W, int row0, int nrows, const double *zeta, int N,
                            double L_v, double lambda, const double *glx, const double *glw,

@@ -130,3 +130,25 @@ def init_1d(v: np.ndarray, nX: int, order: int, ic: int, TWall: float = 1.0,
         else:
             out[l] = left
     return out
+
+
+def moment_residual(v: np.ndarray, Q) -> dict:
+    """Largest |mass|, |momentum| and |energy| moment of the rows of Q (B x
+    N^3, numpy or torch) with the trapezoid weights of conserve.c, each over
+    the largest of |Q| times the moment's natural scale (the check of the
+    FP64 conservation projection)."""
+    Q = np.asarray(Q.detach().cpu().numpy() if hasattr(Q, "detach") else Q, dtype=np.float64)
+    N = v.size
+    wt = np.ones(N)
+    wt[0] = wt[-1] = 0.5
+    dv = v[1] - v[0]
+    w = (wt[:, None, None] * wt[None, :, None] * wt[None, None, :] * dv ** 3).reshape(-1)
+    vx, vy, vz = (a.reshape(-1) for a in np.meshgrid(v, v, v, indexing="ij"))
+    e = 0.5 * (vx ** 2 + vy ** 2 + vz ** 2)
+    mom = np.stack([Q @ w, Q @ (w * vx), Q @ (w * vy), Q @ (w * vz), Q @ (w * e)], 1)
+    scale = np.abs(Q).max(axis=1, keepdims=True) * np.array(
+        [w.sum(), (w * np.abs(vx)).sum(), (w * np.abs(vy)).sum(), (w * np.abs(vz)).sum(),
+         (w * e).sum()])[None, :]
+    r = np.abs(mom) / np.maximum(scale, 1e-300)
+    return {"mass": float(r[:, 0].max()), "momentum": float(r[:, 1:4].max()),
+            "energy": float(r[:, 4].max())}

@@ -145,3 +145,54 @@ def test_gelu_erf_approximation_bound():
     poly = ((((f32(a5) * t + f32(a4)) * t + f32(a3)) * t + f32(a2)) * t + f32(a1)) * t
     r = np.copysign((f32(1) - poly * np.exp(-(ax * ax)).astype(f32)).astype(f32), x)
     assert np.abs(r - erf(x.astype(np.float64))).max() < 1e-6
+
+
+def test_equilibrium_form_gradients_match_finite_differences():
+    """The equilibrium-exact loss (network on [f; M_f], output difference)
+    against central finite differences of itself, every parameter."""
+    spec, theta, net = _small(seed=7)
+    f, Q = _data(spec, 2, 4)
+    v = np.linspace(-3.0, 3.0, spec.N)
+    M = fo.maxwellian_of(f.reshape(2, -1), v).reshape(f.shape)
+    loss, g = net.loss_grad(f, Q, floor=0.1, M=M)
+    ga = fo.pack(spec, g)
+    eps = 1e-6
+    gn = np.empty_like(theta)
+    for i in range(theta.size):
+        tp, tm = theta.copy(), theta.copy()
+        tp[i] += eps
+        tm[i] -= eps
+        lp, _ = fo.Net(spec, tp, sigma=0.7).loss_grad(f, Q, floor=0.1, M=M)
+        lm, _ = fo.Net(spec, tm, sigma=0.7).loss_grad(f, Q, floor=0.1, M=M)
+        gn[i] = (lp - lm) / (2 * eps)
+    assert loss > 0
+    err = np.abs(ga - gn).max() / np.abs(gn).max()
+    assert err < 1e-6, err
+
+
+def test_equilibrium_form_vanishes_at_equilibrium():
+    """Q(f) = P(f) - P(M_f) is zero for f = M_f, for any parameters."""
+    spec, theta, net = _small(seed=9)
+    v = np.linspace(-3.0, 3.0, spec.N)
+    f = np.random.default_rng(2).uniform(0.1, 1.0, (2, spec.N ** 3))
+    M = fo.maxwellian_of(f, v)
+    assert np.abs(net.predict_eq(M, M)).max() == 0.0
+    assert np.abs(net.predict_eq(f, M)).max() > 0.0
+
+
+def test_maxwellian_of_keeps_the_moments():
+    """The Maxwellian of f has f's density, bulk velocity and temperature up
+    to the grid's quadrature error (a wide grid keeps it small)."""
+    from spectralbte_gb300.workloads import maxwellian
+    N = 24
+    v = np.linspace(-8.0, 8.0, N)
+    f = 0.6 * maxwellian(v, 1.0, (0.4, 0.0, -0.2), 1.3) + 0.4 * maxwellian(v, 1.0, (-0.5, 0.1, 0), 0.8)
+    M = fo.maxwellian_of(f.reshape(1, -1), v).reshape(N, N, N)
+    wt = np.ones(N)
+    wt[0] = wt[-1] = 0.5
+    dv = v[1] - v[0]
+    w = wt[:, None, None] * wt[None, :, None] * wt[None, None, :] * dv ** 3
+    vx = v[:, None, None]
+    for g in (f, M):
+        assert abs((w * g).sum() - 1.0) < 1e-6
+    assert abs((w * vx * f).sum() - (w * vx * M).sum()) < 1e-6

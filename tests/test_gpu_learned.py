@@ -257,3 +257,131 @@ def test_channel_mix_profiling_counts_launches(gpu):
     net.set_profiling(True)   # switching on again starts a new count
     assert net.kernel_time() == (0.0, 0)
     net.set_profiling(False)
+
+
+def _eq_data(B, seed, n, L_v=4.0):
+    """f from the mixture family on an n-point grid, its Maxwellian (oracle),
+    and random targets; f rounded to FP32 as the training path stores it."""
+    import math
+    rng = np.random.default_rng(seed)
+    v = np.linspace(-L_v, L_v, n)
+    vx, vy, vz = v[:, None, None], v[None, :, None], v[None, None, :]
+    f = np.zeros((B, n, n, n))
+    for b in range(B):
+        for _ in range(2):
+            u = rng.uniform(-0.8, 0.8, 3)
+            T = rng.uniform(0.6, 1.6)
+            f[b] += rng.uniform(0.3, 1.0) * (2 * math.pi * T) ** -1.5 * np.exp(
+                -((vx - u[0]) ** 2 + (vy - u[1]) ** 2 + (vz - u[2]) ** 2) / (2 * T))
+    f = f.reshape(B, -1).astype(np.float32).astype(np.float64)
+    M = fo.maxwellian_of(f, v)
+    Q = rng.normal(size=(B, n ** 3)).astype(np.float32)
+    return v, f, M, Q
+
+
+@pytest.mark.parametrize("B,shape", [(3, "small16"), (5, "wide16"), (4, "small")])
+def test_equilibrium_form_forward_matches_oracle(gpu, B, shape):
+    """P(f) - P(M_f) on the device (one batch [f; M_f], the Maxwellian built
+    by the device) against the oracle with the same rounding points."""
+    import torch
+    net, spec, prec = _net(gpu, seed=13, shape=shape)
+    v, f, M, _ = _eq_data(B, 40 + B, spec.N)
+    net.set_equilibrium(True, v)
+    assert net.equilibrium
+    theta = net.get_params().astype(np.float64)
+    fd = torch.from_numpy(f).cuda()
+    Qd = torch.zeros_like(fd)
+    net.predict(fd, Qd, B)
+    got = Qd.cpu().numpy()
+    o_r = fo.Net(spec, theta, sigma=0.5, rounding=True, precision=prec)
+    o64 = fo.Net(spec, theta, sigma=0.5)
+    want_r = o_r.predict_eq(f, M).reshape(B, -1)
+    want = o64.predict_eq(f, M).reshape(B, -1)
+    # the difference of two outputs: the scale of the rounding gap is that of
+    # either output, not of their difference
+    ref = np.linalg.norm(o64.predict(f))
+    gap = np.linalg.norm(want_r - want) / ref
+    assert np.linalg.norm(got - want_r) / ref < max(1e-3, 2 * gap), gap
+    assert np.linalg.norm(got - want) / ref < 3e-2
+    # switching the form off restores the plain network output
+    net.set_equilibrium(False)
+    P = torch.zeros_like(fd)
+    net.predict(fd, P, B)
+    assert rel_l2(P.cpu().numpy(), o_r.predict(f).reshape(B, -1)) < max(1e-3, 2 * gap)
+
+
+@pytest.mark.parametrize("B,shape,floor", [(4, "small16", 0.1), (3, "wide16", 0.1),
+                                           (5, "small", 0.0)])
+def test_equilibrium_form_gradients_match_oracle(gpu, B, shape, floor):
+    import torch
+    net, spec, prec = _net(gpu, seed=17, shape=shape)
+    v, f, M, Q = _eq_data(B, 60 + B, spec.N)
+    net.set_equilibrium(True, v)
+    net.set_loss_floor(floor)
+    theta = net.get_params().astype(np.float64)
+    loss, g = net.loss_grad(torch.from_numpy(f.astype(np.float32)).cuda(),
+                            torch.from_numpy(Q).cuda(), B)
+    lr_, gr = fo.Net(spec, theta, sigma=0.5, rounding=True, precision=prec).loss_grad(
+        f, Q.astype(np.float64), floor, M=M)
+    l64, g64 = fo.Net(spec, theta, sigma=0.5).loss_grad(f, Q.astype(np.float64), floor, M=M)
+    assert abs(loss - lr_) <= 1e-4 * lr_
+    off, _ = spec.layout()
+    for k, (o, n) in off.items():
+        gk = g[o:o + n].astype(np.float64)
+        gap = rel_l2(gr[k].reshape(-1), g64[k].reshape(-1))
+        assert rel_l2(gk, gr[k].reshape(-1)) < max(5e-3, 2 * gap), (k, gap)
+        assert rel_l2(gk, g64[k].reshape(-1)) < 5e-2, k
+
+
+def test_equilibrium_form_is_small_at_equilibrium(gpu):
+    """On a Maxwellian the equilibrium form returns (nearly) zero for any
+    parameters: M_f differs from f = M only by the grid's moment quadrature,
+    and the network output of the difference scales with it.  The plain form
+    of the same untrained network returns an O(1) output there."""
+    import torch
+    from spectralbte_gb300.workloads import maxwellian
+    n = 16
+    net = gpu.FourierOperator(n, 16, 8, 3, 32, seed=21, precision=1)
+    net.output_scale = 0.5
+    v = np.linspace(-7.0, 7.0, n)
+    f = np.stack([maxwellian(v, 1.0, (0.3, -0.1, 0.0), 1.1).reshape(-1),
+                  maxwellian(v, 0.7, (0.0, 0.2, 0.4), 0.9).reshape(-1)])
+    fd = torch.from_numpy(f).cuda()
+    P = torch.zeros_like(fd)
+    net.predict(fd, P, 2)
+    net.set_equilibrium(True, v)
+    D = torch.zeros_like(fd)
+    net.predict(fd, D, 2)
+    torch.cuda.synchronize()
+    ratio = (torch.linalg.vector_norm(D, dim=1) / torch.linalg.vector_norm(P, dim=1)).max()
+    assert ratio < 1e-2, float(ratio)
+
+
+def test_floored_spot_check(gpu):
+    """With a floor eps the check divides by sqrt(|Q|^2 + eps mean |Q_net|^2):
+    the recorded distance equals that formula for the checked instance, and is
+    below the unfloored one."""
+    import torch
+    from spectralbte_gb300 import learned as lrn
+    plan = _plan(gpu)
+    net, _, _ = _net(gpu, seed=5)
+    B = 6
+    f = lrn.sample_f(plan.v, "mixture", B, seed=8)
+    Qn = torch.empty_like(f)
+    net.predict(f, Qn, B)
+    plan.conserve_device(Qn, B)
+    Qp = torch.empty_like(f)
+    plan.computeQ_device(f, Qp, B, gpu.FP32 | gpu.CONSERVE)
+    torch.cuda.synchronize()
+    d = torch.linalg.vector_norm(Qn[0] - Qp[0]).item()
+    q2 = torch.linalg.vector_norm(Qp[0]).item() ** 2
+    msq = (Qn.pow(2).sum() / B).item()
+    Q = torch.empty_like(f)
+    for eps, want in ((0.0, d / np.sqrt(q2)), (0.5, d / np.sqrt(q2 + 0.5 * msq))):
+        plan.set_learned(net, tol=1e9, check_every=1)
+        plan.set_learned_floor(eps)
+        plan.computeQ_device(f, Q, B, gpu.FP32 | gpu.CONSERVE | gpu.LEARNED)
+        torch.cuda.synchronize()
+        got = plan.learned_stats()["last_err"]
+        assert abs(got - want) <= 1e-9 * want, (eps, got, want)
+    plan.set_learned(None)
