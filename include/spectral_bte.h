@@ -179,6 +179,20 @@ int spectral_plan_get_weights(spectral_plan *plan, double *W_host,
    double integral of gHat3L, no trapezoid factors) for the plan's grid. */
 int spectral_plan_generate_weights_landau(spectral_plan *plan, double lambda);
 int spectral_plan_set_conservation(spectral_plan *plan, double mass);
+/* Isotropic weights with the radial integral of weights.c:156-160 in closed
+   form (lambda 0 or 1 only; the quadrature covers every lambda): the same
+   table as spectral_plan_generate_weights_iso to ~1e-14, in a fraction of
+   the time.  fp64_table = 1 stores the FP64 table as usual.  fp64_table = 0
+   builds only the row-pair FP32 table of the convolution, directly from the
+   closed form, and never holds the FP64 table (8 N^6 bytes: 8.6 GB at
+   N = 32, 98 GB at N = 48): the plan then serves SPECTRAL_FP32 calls only
+   (FP64 calls and spectral_plan_get_weights return SPECTRAL_ERR_WEIGHTS), in
+   the row-pair form, and supports N = 48.  The reference's commented-out
+   closed form (weights.c:216-253) and its unimplemented weightgen option
+   (boltz.c:56,162-164) point at this. */
+int spectral_plan_generate_weights_closed(spectral_plan *plan, double lambda,
+                                          double d_i, double d_j, double m_i,
+                                          double m_j, int fp64_table);
 /* Grazing-collision weights: gHat3 of the stand-alone generator
    (MPIcollisionRoutines.c:33-205, eps-linear cross section with the
    Coulomb-case Taylor term below theta = sqrt(glance)), no trapezoid

@@ -127,6 +127,7 @@ def lib() -> C.CDLL:
         "spectral_plan_generate_weights_iso": (i, [v, d, d, d, d, d]),
         "spectral_plan_generate_weights_landau": (i, [v, d]),
         "spectral_plan_generate_weights_grazing": (i, [v, d, d]),
+        "spectral_plan_generate_weights_closed": (i, [v, d, d, d, d, d, i]),
         "spectral_weights_generator": (i, [i, d, d, d, d]),
         "initialize_weights_AnIso": (None, [i, _dp, d, d, i, C.POINTER(_dp), d]),
         "spectral_plan_get_weights": (i, [v, _dp, C.c_longlong, C.c_longlong]),
@@ -385,6 +386,14 @@ class Plan:
     def generate_weights_iso(self, lam: float, d_i=2.0, d_j=2.0, m_i=1.0, m_j=1.0):
         _check(self.L.spectral_plan_generate_weights_iso(self.h, float(lam), d_i, d_j, m_i, m_j),
                "generate_weights_iso")
+
+    def generate_weights_closed(self, lam: float, fp64_table: bool = True, d_i=2.0, d_j=2.0,
+                                m_i=1.0, m_j=1.0):
+        """Isotropic weights from the closed-form radial integral (lambda 0, 1);
+        fp64_table=False keeps only the row-pair FP32 table (FP32 calls only)."""
+        _check(self.L.spectral_plan_generate_weights_closed(self.h, float(lam), d_i, d_j, m_i,
+                                                            m_j, 1 if fp64_table else 0),
+               "generate_weights_closed")
 
     def generate_weights_grazing(self, lam: float, glance: float):
         """Grazing-collision weights (gHat3 of the stand-alone generator)."""

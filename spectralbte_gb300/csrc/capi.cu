@@ -266,6 +266,9 @@ struct WeightsDev {
     float *w32 = nullptr;    // tiled FP32 (built on first FP32 use)
     float2 *w32x2 = nullptr; // tiled (w, w) pairs (built on first variant-4 use)
     float *wsym = nullptr;   // partner-summed FP32 tiles (built on first symmetric use)
+    // the row-pair FP32 table alone, built from the closed form with no FP64
+    // table (spectral_plan_generate_weights_closed with fp64_table = 0)
+    bool f32_only = false;
     void release()
     {
         dfree(w64);
@@ -273,7 +276,9 @@ struct WeightsDev {
         dfree(w32x2);
         dfree(wsym);
         N = 0;
+        f32_only = false;
     }
+    bool ready() const { return w64 || (f32_only && wsym); }
 };
 
 // Device W from a flat host or device array, or from host row pointers.
@@ -319,9 +324,18 @@ static int upload_weights(WeightsDev &wd, int N, const double *flat,
     return kOk;
 }
 
+static int need_w64(const WeightsDev &wd, const char *what)
+{
+    if (wd.w64) return kOk;
+    set_error(kErrWeights, "%s needs the FP64 weight table; the plan holds only the row-pair "
+                           "FP32 table of the closed-form weights", what);
+    return kErrWeights;
+}
+
 static int ensure_w32(WeightsDev &wd, cudaStream_t st)
 {
     if (wd.w32) return kOk;
+    SBTE_TRY(need_w64(wd, "the every-row FP32 convolution"));
     const long long n3 = (long long)wd.N * wd.N * wd.N;
     SBTE_TRY(dalloc(&wd.w32, (size_t)(n3 * n3)));
     SBTE_LAUNCH(weights_to_tiled_f32(wd.w64, wd.w32, wd.N, st), 1);
@@ -332,6 +346,7 @@ static int ensure_w32(WeightsDev &wd, cudaStream_t st)
 static int ensure_wsym(WeightsDev &wd, cudaStream_t st)
 {
     if (wd.wsym) return kOk;
+    SBTE_TRY(need_w64(wd, "the row-pair table"));
     const long long nn = (long long)wd.N * wd.N;
     SBTE_TRY(dalloc(&wd.wsym, (size_t)(nn * sym_max_slots(wd.N) * nn)));
     SBTE_LAUNCH(weights_to_sym_f32(wd.w64, wd.wsym, wd.N, st), 1);
@@ -342,6 +357,7 @@ static int ensure_wsym(WeightsDev &wd, cudaStream_t st)
 static int ensure_w32x2(WeightsDev &wd, cudaStream_t st)
 {
     if (wd.w32x2) return kOk;
+    SBTE_TRY(need_w64(wd, "convolution variant 4"));
     const long long n3 = (long long)wd.N * wd.N * wd.N;
     SBTE_TRY(dalloc(&wd.w32x2, (size_t)(n3 * n3)));
     SBTE_LAUNCH(weights_to_tiled_f32x2(wd.w64, wd.w32x2, wd.N, st), 1);
@@ -545,6 +561,91 @@ static int generate_graze_device(WeightsDev &wd, int N, double L_v, double lambd
         set_error(kErrCuda, "grazing weights: %s", cudaGetErrorString(e));
         return kErrCuda;
     }
+    return kOk;
+}
+
+// The isotropic weights of weights.c:265-281 with the closed-form radial
+// integral (lambda 0 or 1; weights.cu).  fp64_table: into wd.w64 (every path
+// of the plan then works as with quadrature weights).  Otherwise only the
+// row-pair FP32 table of the convolution is built, directly, so no FP64 table
+// is ever held: 8 N^6 bytes (8.6 GB at N = 32, 98 GB at N = 48) are never
+// allocated, and the plan runs FP32 calls only.
+static int generate_closed_device(WeightsDev &wd, const IsoWeightSpec &s, bool fp64_table,
+                                  cudaStream_t st)
+{
+    const int N = s.N;
+    const long long n3 = (long long)N * N * N;
+    if (!(s.lambda == 0.0 || s.lambda == 1.0)) {
+        set_error(kErrUnsupported, "closed-form weights: lambda must be 0 or 1 (got %g)",
+                  s.lambda);
+        return kErrUnsupported;
+    }
+    if (!fp64_table && (N % 2 != 0 || N > 64)) {
+        set_error(kErrUnsupported, "row-pair weights: N must be even and <= 64 (got %d)", N);
+        return kErrUnsupported;
+    }
+    WeightParams wp;
+    wp.N = N;
+    wp.L_v = s.L_v;
+    wp.lambda = s.lambda;
+    wp.mu = s.m_j / (s.m_i + s.m_j);
+    wp.dfac = 0.25 * pow(0.5 * (s.d_i + s.d_j), 2);
+    const double deta = s.zeta[1] - s.zeta[0];
+    wp.prefactor = 16.0 * M_PI * M_PI * deta * deta * deta / pow(2.0 * M_PI, 1.5) / (4.0 * M_PI);
+    wp.zmax = std::max(fabs(s.zeta[0]), fabs(s.zeta[N - 1]));
+    // every nonzero gain argument mu |zeta| and |xi - mu zeta| must be at
+    // least 1/2 / L_v: the smallest nonzero |xi_a - mu zeta_a| over one axis
+    // bounds the second from below, and mu min |zeta_a| the first
+    const double small = 0.5 / s.L_v;
+    double m1 = 1e300, m0 = 1e300;
+    for (int a = 0; a < N; a++) {
+        const double za = fabs(s.zeta[a]);
+        if (za != 0.0) m0 = std::min(m0, wp.mu * za);
+        for (int b = 0; b < N; b++) {
+            const double d = fabs(s.zeta[b] - wp.mu * s.zeta[a]);
+            if (d != 0.0) m1 = std::min(m1, d);
+        }
+    }
+    if (m0 < small || m1 < small) {
+        set_error(kErrUnsupported, "closed-form weights: a gain argument below 1/(2 L_v) "
+                                   "on this grid; use the quadrature");
+        return kErrUnsupported;
+    }
+    wd.release();
+    double *d_zeta = nullptr;
+    SBTE_TRY(dalloc(&d_zeta, N));
+    int rc = kOk;
+    cudaError_t e = cudaMemcpyAsync(d_zeta, s.zeta.data(), sizeof(double) * N,
+                                    cudaMemcpyHostToDevice, st);
+    if (fp64_table) {
+        if ((rc = dalloc(&wd.w64, (size_t)(n3 * n3))) != kOk) {
+            dfree(d_zeta);
+            return rc;
+        }
+        const int chunk = 4096;
+        for (long long r0 = 0; r0 < n3 && e == cudaSuccess; r0 += chunk) {
+            const int nr = (int)std::min<long long>(chunk, n3 - r0);
+            e = weights_iso_closed(wd.w64 + r0 * n3, (int)r0, nr, d_zeta, wp, st);
+            if (e == cudaSuccess) count(1);
+        }
+    } else {
+        const long long nn = (long long)N * N;
+        if ((rc = dalloc(&wd.wsym, (size_t)(nn * sym_max_slots(N) * nn))) != kOk) {
+            dfree(d_zeta);
+            return rc;
+        }
+        if (e == cudaSuccess) e = weights_sym_closed(wd.wsym, d_zeta, wp, st);
+        if (e == cudaSuccess) count(1);
+        wd.f32_only = true;
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    dfree(d_zeta);
+    if (e != cudaSuccess) {
+        wd.release();
+        set_error(kErrCuda, "closed-form weights: %s", cudaGetErrorString(e));
+        return kErrCuda;
+    }
+    wd.N = N;
     return kOk;
 }
 
@@ -910,6 +1011,8 @@ static int resolve_f32(spectral_plan_s *p, bool maxpreserve, ConvF32Config &cfg,
 {
     const int N = p->N;
     cfg = p->tune;
+    if (!p->W.w64 && !(cfg.variant == 2 || cfg.variant == 3 || cfg.variant == 5))
+        cfg = ConvF32Config{64, 2, cfg.flush, 3, 8};  // the row-pair table alone
     if (!conv_f32_supported(N, cfg, maxpreserve)) {
         // the two-pair form stages twice the rows: fall back to a narrower
         // instance group that fits in shared memory
@@ -922,7 +1025,9 @@ static int resolve_f32(spectral_plan_s *p, bool maxpreserve, ConvF32Config &cfg,
                 found = true;
             }
         if (!found) {
-            set_error(kErrUnsupported, "FP32 convolution supports N in {8,16,24,32}; N=%d", N);
+            set_error(kErrUnsupported,
+                      "FP32 convolution supports N in {8,16,24,32} (and 48 in the row-pair "
+                      "form); N=%d", N);
             return kErrUnsupported;
         }
     }
@@ -1088,10 +1193,11 @@ static int computeQ_dev(spectral_plan_s *p, const double *f, double *Q, int B,
         set_error(kErrArg, "computeQ: bad arguments");
         return kErrArg;
     }
-    if (!p->W.w64) {
+    if (!p->W.ready()) {
         set_error(kErrWeights, "computeQ: the plan has no weights");
         return kErrWeights;
     }
+    if (!p->W.w64 && !(flags & SPECTRAL_FP32)) return need_w64(p->W, "the FP64 operator");
     SBTE_CUDA(cudaSetDevice(p->device));
     if (flags & SPECTRAL_LEARNED) return learned_q(p, f, Q, B, flags, st);
     const bool mp = (flags & SPECTRAL_MAXPRESERVE) != 0;
@@ -1212,6 +1318,26 @@ int spectral_plan_generate_weights_iso(spectral_plan *p, double lambda, double d
     s.m_j = m_j;
     s.zeta = p->zeta;
     return generate_iso_device(p->W, s, p->stream);
+}
+
+int spectral_plan_generate_weights_closed(spectral_plan *p, double lambda, double d_i,
+                                          double d_j, double m_i, double m_j, int fp64_table)
+{
+    if (!p) {
+        set_error(kErrArg, "spectral_plan_generate_weights_closed: null plan");
+        return kErrArg;
+    }
+    SBTE_CUDA(cudaSetDevice(p->device));
+    IsoWeightSpec s;
+    s.N = p->N;
+    s.L_v = p->L_v;
+    s.lambda = lambda;
+    s.d_i = d_i;
+    s.d_j = d_j;
+    s.m_i = m_i;
+    s.m_j = m_j;
+    s.zeta = p->zeta;
+    return generate_closed_device(p->W, s, fp64_table != 0, p->stream);
 }
 
 int spectral_plan_generate_weights_grazing(spectral_plan *p, double lambda, double glance)
@@ -1409,7 +1535,7 @@ int spectral_1d_step(spectral_plan *p, double *f_dev, int flags, void *stream)
     if (!p || !p->t1d || !f_dev)
         return set_error(kErrNotInit, "spectral_1d_step: call spectral_1d_setup first"),
                kErrNotInit;
-    if (!p->W.w64) return set_error(kErrWeights, "spectral_1d_step: no weights"), kErrWeights;
+    if (!p->W.ready()) return set_error(kErrWeights, "spectral_1d_step: no weights"), kErrWeights;
     SBTE_CUDA(cudaSetDevice(p->device));
     return step_1d(p, f_dev, flags, (cudaStream_t)stream);
 }
@@ -1555,7 +1681,7 @@ int spectral_plan_inject_stall(spectral_plan *p, int slot, long long limit_clock
 int spectral_plan_autotune(spectral_plan *p, int B, int flags, int *chosen)
 {
     if (!p || B < 1) return set_error(kErrArg, "bad arguments"), kErrArg;
-    if (!p->W.w64) return set_error(kErrWeights, "autotune: no weights"), kErrWeights;
+    if (!p->W.ready()) return set_error(kErrWeights, "autotune: no weights"), kErrWeights;
     SBTE_CUDA(cudaSetDevice(p->device));
     SBTE_TRY(ensure32(p, B));
     const bool two = (flags & SPECTRAL_MAXPRESERVE) != 0;
@@ -1571,6 +1697,9 @@ int spectral_plan_autotune(spectral_plan *p, int B, int flags, int *chosen)
     ConvF32Config bestc = p->tune;
     for (ConvF32Config c : cands) {
         if (!conv_f32_supported(p->N, c, two)) continue;
+        // a plan with only the row-pair table runs the row-pair variants
+        if (!p->W.w64 && !(p->sym && (c.variant == 2 || c.variant == 3 || c.variant == 5)))
+            continue;
         // time each variant in the form the plan would run it
         c.sym = (p->sym && (c.variant == 2 || c.variant == 3 || c.variant == 5)) ? 1 : 0;
         const float *Wt = nullptr;

@@ -335,7 +335,7 @@ __global__ void tile_weights_kernel(const double *__restrict__ W,
 // them), then fill Wsym[zrow][slot][zz][xz].  FP64 sum, one FP32 rounding.
 __global__ void sym_weights_kernel(const double *__restrict__ W, float *__restrict__ Wsym, int N)
 {
-    __shared__ short rows[32 * 32 / 2 + 2];
+    __shared__ short rows[64 * 64 / 2 + 2];
     __shared__ int nrows;
     const int nn = N * N, h = N / 2;
     const long long n3 = (long long)nn * N;
@@ -469,7 +469,7 @@ cudaError_t weights_to_tiled_f32(const double *W, float *Wblk, int N,
 
 cudaError_t weights_to_sym_f32(const double *W, float *Wsym, int N, cudaStream_t st)
 {
-    if (N % 2 != 0 || N > 32 || N < 2) return cudaErrorInvalidValue;
+    if (N % 2 != 0 || N > 64 || N < 2) return cudaErrorInvalidValue;
     sym_weights_kernel<<<N * N, 256, 0, st>>>(W, Wsym, N);
     return cudaGetLastError();
 }

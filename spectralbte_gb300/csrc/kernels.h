@@ -209,6 +209,13 @@ cudaError_t weights_iso(double *W, int row0, int nrows, const double *zeta,
 // Landau weights (aniso_weights.c:370-425) for rows [row0, row0 + nrows)
 // into W[row - row0][N^3] (FP64); glx, glw: the 64-point Gauss-Legendre rule
 // on [-1, 1] (device).
+// Isotropic weights with the closed-form radial integral (lambda 0 or 1;
+// weights.cu): FP64 rows [row0, row0 + nrows), or the row-pair FP32 table of
+// the convolution (the layout of weights_to_sym_f32) with no FP64 table.
+cudaError_t weights_iso_closed(double *W, int row0, int nrows, const double *zeta,
+                               const WeightParams &wp, cudaStream_t st);
+cudaError_t weights_sym_closed(float *Wsym, const double *zeta, const WeightParams &wp,
+                               cudaStream_t st);
 // Grazing-collision weights (MPIcollisionRoutines.c:33-205), one value per
 // (zeta, xi) pair of pairs[6 u ..]: npan 16-point panels in r and phi, the
 // nte theta panels between te[0..nte]; glx, glw the 16-point rule.

@@ -138,6 +138,141 @@ rows_kernel(double *__restrict__ W, int row0, const double *__restrict__ zeta,
     }
 }
 
+// ---------------------------------------------------- closed-form weights ---
+// The radial integral of ghat (weights.c:156-160) in closed form for
+// lambda = 0 and 1, derived from the integrand.  With s(x) = sin x / x and
+// q(x) = (1 - cos x) / x^2 = s(x/2)^2 / 2:
+//   gain, lambda 0: int_0^L r^2 s(ra) s(rb) dr = L/(2ab) [s(Ld) - s(Le)]
+//   gain, lambda 1: int_0^L r^3 s(ra) s(rb) dr = L^2/(2ab) [s(Ld) - q(Ld) - s(Le) + q(Le)]
+//     (d = a - b, e = a + b: 2 sin A sin B = cos(A - B) - cos(A + B), and
+//     int_0^L r cos(rk) dr = L^2 [s(Lk) - q(Lk)]);
+//   loss, lambda 0: int_0^L r^2 s(rc) dr = (sin x - x cos x) / c^3
+//   loss, lambda 1: int_0^L r^3 s(rc) dr = ((2 - x^2) cos x + 2 x sin x - 2) / c^4
+//     (x = Lc; below x = 1/2 the series L^(lambda+3) sum_k (-1)^k x^2k /
+//     ((2k+1)! (2k+lambda+3)) avoids the cancellation).
+// A gain argument of exactly 0 turns the gain into the loss form of the
+// other.  The host admits a grid only when every nonzero gain argument is at
+// least 1/2 / L (otherwise 1/(ab) would cost digits).
+__device__ __forceinline__ double sinc_d(double x) { return x != 0.0 ? sin(x) / x : 1.0; }
+
+__device__ double loss_closed_d(double c, int lam, double L)
+{
+    const double x = L * c;
+    const double Lp = lam == 0 ? L * L * L : L * L * L * L;
+    if (x < 0.5) {
+        double term = 1.0, sum = 0.0;
+        for (int k = 0; k < 12; k++) {
+            sum += term / (2.0 * k + lam + 3.0);
+            term *= -x * x / ((2.0 * k + 2.0) * (2.0 * k + 3.0));
+        }
+        return Lp * sum;
+    }
+    double sx, cx;
+    sincos(x, &sx, &cx);
+    if (lam == 0) return (sx - x * cx) / (c * c * c);
+    return ((2.0 - x * x) * cx + 2.0 * x * sx - 2.0) / (c * c * c * c);
+}
+
+__device__ __forceinline__ double q_stable_d(double x)
+{
+    const double h = sinc_d(0.5 * x);
+    return 0.5 * h * h;
+}
+
+__device__ double ghat_closed_d(double a0, double a1, double a2, int lam, double L)
+{
+    double gain;
+    if (a0 == 0.0 && a2 == 0.0)
+        gain = lam == 0 ? L * L * L / 3.0 : L * L * L * L / 4.0;
+    else if (a0 == 0.0)
+        gain = loss_closed_d(a2, lam, L);
+    else if (a2 == 0.0)
+        gain = loss_closed_d(a0, lam, L);
+    else {
+        const double d = L * (a0 - a2), e = L * (a0 + a2);
+        if (lam == 0)
+            gain = L / (2.0 * a0 * a2) * (sinc_d(d) - sinc_d(e));
+        else
+            gain = L * L / (2.0 * a0 * a2) * (sinc_d(d) - q_stable_d(d) - sinc_d(e) + q_stable_d(e));
+    }
+    return gain - loss_closed_d(a1, lam, L);
+}
+
+// W[zeta = (i, j, k)][xi = (l, m, n)] (weights.c:265-281 with the closed
+// radial integral): wt(l) wt(m) wt(n) dfac prefactor ghat(a0, a1, a2),
+// a0 = mu |zeta|, a1 = |xi|, a2 = |xi - mu zeta|.
+__device__ __forceinline__ double w_closed(const double *__restrict__ zeta, const WeightParams &wp,
+                                           int lam, int i, int j, int k, int l, int m, int n)
+{
+    const int N = wp.N;
+    const double z1 = zeta[i], z2 = zeta[j], z3 = zeta[k];
+    const double k1 = zeta[l], k2 = zeta[m], k3 = zeta[n];
+    const double mu = wp.mu;
+    const double a0 = mu * sqrt(z1 * z1 + z2 * z2 + z3 * z3);
+    const double a1 = sqrt(k1 * k1 + k2 * k2 + k3 * k3);
+    const double d1 = k1 - mu * z1, d2 = k2 - mu * z2, d3 = k3 - mu * z3;
+    const double a2 = sqrt(d1 * d1 + d2 * d2 + d3 * d3);
+    return wtn(l, N) * wtn(m, N) * wtn(n, N) * wp.dfac *
+           (wp.prefactor * ghat_closed_d(a0, a1, a2, lam, wp.L_v));
+}
+
+// FP64 rows [row0, row0 + nrows) of the table, row-major.
+__global__ void __launch_bounds__(256)
+iso_closed_kernel(double *__restrict__ W, int row0, int nrows, const double *__restrict__ zeta,
+                  WeightParams wp, int lam)
+{
+    const int N = wp.N;
+    const long long n3 = (long long)N * N * N;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < nrows * n3;
+         e += (long long)gridDim.x * blockDim.x) {
+        const long long z = row0 + e / n3, x = e % n3;
+        W[e] = w_closed(zeta, wp, lam, (int)(z / (N * N)), (int)((z / N) % N), (int)(z % N),
+                        (int)(x / (N * N)), (int)((x / N) % N), (int)(x % N));
+    }
+}
+
+// The row-pair FP32 table of the warp-specialised convolution, from the
+// closed form, with no FP64 table: for zeta-row (zx, zy) (one CTA) and each
+// run slot r (rows whose partner s(r) = (zeta + N/2 - r) mod N does not
+// precede them), Wsym[zrow][slot][zz][xz] = W[zeta][r, xz] +
+// W[zeta][s(r), (zz + N/2 - xz) mod N] (the second term only when s(r) != r),
+// summed in FP64 and rounded once, as weights_to_sym_f32 does from a table.
+__global__ void __launch_bounds__(256)
+sym_closed_kernel(float *__restrict__ Wsym, const double *__restrict__ zeta, WeightParams wp,
+                  int lam)
+{
+    __shared__ short rows[64 * 64 / 2 + 2];
+    __shared__ int nrows;
+    const int N = wp.N, nn = N * N, h = N / 2;
+    const int zrow = blockIdx.x, zx = zrow / N, zy = zrow % N;
+    const int ms = sym_max_slots(N);
+    if (threadIdx.x == 0) {
+        int k = 0;
+        for (int r = 0; r < nn && k < ms; r++) {
+            const int sx = (zx + h - r / N + N) % N, sy = (zy + h - r % N + N) % N;
+            if (sx * N + sy >= r) rows[k++] = (short)r;
+        }
+        nrows = k;
+    }
+    __syncthreads();
+    const int nr = nrows;
+    float *out = Wsym + (long long)zrow * ms * nn;
+    for (int t = threadIdx.x; t < ms * nn; t += blockDim.x) {
+        const int slot = t / nn, zz = (t % nn) / N, xz = t % N;
+        double w = 0.0;
+        if (slot < nr) {
+            const int r = rows[slot];
+            const int sx = (zx + h - r / N + N) % N, sy = (zy + h - r % N + N) % N;
+            w = w_closed(zeta, wp, lam, zx, zy, zz, r / N, r % N, xz);
+            if (sx * N + sy != r) {
+                const int sz = (zz + h - xz + N) % N;
+                w += w_closed(zeta, wp, lam, zx, zy, zz, sx, sy, sz);
+            }
+        }
+        out[t] = (float)w;
+    }
+}
+
 // Landau weights (gHat3L, aniso_weights.c:370-400, as generate_conv_weights_AnIso
 // fills them, :402-425): one thread per (zeta, xi) entry,
 //   W = 2 pi  GL64_{r in [0, L_v]} r^{lambda+2}  GL64_{theta in [0, pi]}
@@ -305,6 +440,28 @@ cudaError_t weights_scatter(double *W, const double *vals, const int *map, long 
     long long blocks = (n + 255) / 256;
     if (blocks > 152 * 16) blocks = 152 * 16;
     scatter_kernel<<<(unsigned)blocks, 256, 0, st>>>(W, vals, map, n);
+    return cudaGetLastError();
+}
+
+cudaError_t weights_iso_closed(double *W, int row0, int nrows, const double *zeta,
+                               const WeightParams &wp, cudaStream_t st)
+{
+    const int lam = wp.lambda == 0.0 ? 0 : (wp.lambda == 1.0 ? 1 : -1);
+    if (lam < 0) return cudaErrorInvalidValue;
+    const long long total = (long long)nrows * wp.N * wp.N * wp.N;
+    if (total <= 0) return cudaSuccess;
+    long long blocks = (total + 255) / 256;
+    if (blocks > 152 * 32) blocks = 152 * 32;
+    iso_closed_kernel<<<(unsigned)blocks, 256, 0, st>>>(W, row0, nrows, zeta, wp, lam);
+    return cudaGetLastError();
+}
+
+cudaError_t weights_sym_closed(float *Wsym, const double *zeta, const WeightParams &wp,
+                               cudaStream_t st)
+{
+    const int lam = wp.lambda == 0.0 ? 0 : (wp.lambda == 1.0 ? 1 : -1);
+    if (lam < 0 || wp.N % 2 != 0 || wp.N < 2 || wp.N > 64) return cudaErrorInvalidValue;
+    sym_closed_kernel<<<wp.N * wp.N, 256, 0, st>>>(Wsym, zeta, wp, lam);
     return cudaGetLastError();
 }
 
