@@ -536,6 +536,44 @@ def run_learned_only(args):
     return 0
 
 
+def run_network_only(args):
+    """The learned operator's network alone (spectral_fno_predict, no plan,
+    no weight table on the device) on B two-Maxwellian instances at N=32:
+    the small case for profiling its kernels."""
+    import torch
+    import spectralbte_gb300 as sb
+    torch.cuda.set_device(0)
+    N, L_v, B = args.n, LV_DEF, args.batch
+    path = args.learned or os.path.join(ROOT, "spectralbte_gb300", "models", f"fno_n{N}.npz")
+    net = sb.FourierOperator.load(path) if os.path.exists(path) else sb.FourierOperator(N)
+    v, _ = sb.grid_0d(N, L_v)
+    fd = torch.from_numpy(two_maxwellian_batch(v, B, args.seed)).cuda()
+    Q = torch.empty_like(fd)
+    for _ in range(args.warmup):
+        net.predict(fd, Q, B)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    k0 = sb.kernel_launches()
+    e0.record()
+    for _ in range(args.steps):
+        net.predict(fd, Q, B)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    peaks, _ = load_peaks()
+    w = learned_work(N, net.width, net.modes, net.layers, net.hidden)
+    gbs = (w["bytes"] - 24 * N ** 3) * B / (ms / 1e3) / 1e9  # no conservation pass here
+    print(json.dumps({
+        "metric": "network evaluations/s (learned operator, no projection)", "impl": "ours",
+        "value": B / (ms / 1e3), "unit": "evals/s", "ms_per_step": ms, "steps": args.steps,
+        "warmup": args.warmup, "n_gpus": 1, "higher_is_better": True,
+        "config": {"workload": f"N={N}, {B} two-Maxwellian instances, network only"},
+        "gpu_launches": sb.kernel_launches() - k0,
+        "roofline": {"bound": "hbm", "achieved": gbs, "peak": float(peaks["hbm_gbs"]),
+                     "unit": "GB/s", "frac": gbs / float(peaks["hbm_gbs"])}}), flush=True)
+    return 0
+
+
 def run_bkw(args):
     """Config 1: 0D Maxwell molecules, N=16, L_v=5, one BKW instance (K=0.65),
     dt = 0.01, 200 RK2 steps of the plain FP64 operator with maxPreserve and
@@ -935,7 +973,7 @@ def main():
                     help="timed calls of the plain FP64 operator (at least 10)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="n32",
-                    choices=["n32", "uneven", "learned", "shock", "heat", "bkw"])
+                    choices=["n32", "uneven", "learned", "network", "shock", "heat", "bkw"])
     ap.add_argument("--nsteps", type=int, default=0,
                     help="time steps of the shock / heat workloads (default: the config's)")
     ap.add_argument("--learned", default="",
@@ -952,6 +990,8 @@ def main():
         return run_uneven(args)
     if args.workload == "learned" and args.impl != "reference":
         return run_learned_only(args)
+    if args.workload == "network" and args.impl != "reference":
+        return run_network_only(args)
     if args.workload in CFG_1D and args.impl != "reference":
         return run_1d(args)
     if args.workload == "bkw" and args.impl != "reference":

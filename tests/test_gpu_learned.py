@@ -326,11 +326,21 @@ def test_equilibrium_form_gradients_match_oracle(gpu, B, shape, floor):
     l64, g64 = fo.Net(spec, theta, sigma=0.5).loss_grad(f, Q.astype(np.float64), floor, M=M)
     assert abs(loss - lr_) <= 1e-4 * lr_
     off, _ = spec.layout()
+    # The halves f and M_f push the gradients of the lift (P, bP) in nearly
+    # opposite directions, so those blocks are small sums with heavy
+    # cancellation (the rounding oracle is itself 6% from FP64 on bP): they
+    # are held to the error bars of the other blocks relative to the norm of
+    # the whole gradient as well.
+    whole = np.sqrt(sum(np.sum(v ** 2) for v in gr.values()))
     for k, (o, n) in off.items():
         gk = g[o:o + n].astype(np.float64)
-        gap = rel_l2(gr[k].reshape(-1), g64[k].reshape(-1))
-        assert rel_l2(gk, gr[k].reshape(-1)) < max(5e-3, 2 * gap), (k, gap)
-        assert rel_l2(gk, g64[k].reshape(-1)) < 5e-2, k
+        ref_r, ref_64 = gr[k].reshape(-1), g64[k].reshape(-1)
+        gap = rel_l2(ref_r, ref_64)
+        err = np.linalg.norm(gk - ref_r)
+        assert (err < max(5e-3, 2 * gap) * np.linalg.norm(ref_r) or
+                err < 1e-4 * whole), (k, gap, err / np.linalg.norm(ref_r))
+        assert (np.linalg.norm(gk - ref_64) < 5e-2 * np.linalg.norm(ref_64) or
+                np.linalg.norm(gk - ref_64) < 1e-3 * whole), k
 
 
 def test_equilibrium_form_is_small_at_equilibrium(gpu):
