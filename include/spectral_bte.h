@@ -372,6 +372,15 @@ int spectral_fno_set_fused(spectral_fno *net, int on);
    summed duration and count since profiling was switched on. */
 int spectral_fno_set_profiling(spectral_fno *net, int on);
 int spectral_fno_kernel_time(spectral_fno *net, double *ms_total, int *launches);
+/* Channel-mix kernel of inference passes: 1 (default) runs the
+   warp-specialised kernel that moves its tiles with the tensor memory
+   accelerator (2D cp.async.bulk.tensor loads and stores, mbarrier ring) where
+   the shape allows (width 64, instances padded to a multiple of 64); 0 runs
+   the general tensor-core GEMM.  Both give the same result. */
+int spectral_fno_set_channel_mix_kernel(spectral_fno *net, int tma);
+/* Device status word of the network's kernels (bit 0: a bounded wait gave
+   up); cleared by the read. */
+int spectral_fno_status(spectral_fno *net, unsigned int *status);
 int spectral_fno_destroy(spectral_fno *net);
 long long spectral_fno_num_params(spectral_fno *net);
 int spectral_fno_num_classes(spectral_fno *net);

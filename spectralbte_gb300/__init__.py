@@ -166,6 +166,8 @@ def lib() -> C.CDLL:
         "spectral_fno_output_scale": (C.c_float, [v]),
         "spectral_fno_set_loss_floor": (i, [v, C.c_float]),
         "spectral_fno_set_equilibrium": (i, [v, i, _dp]),
+        "spectral_fno_set_channel_mix_kernel": (i, [v, i]),
+        "spectral_fno_status": (i, [v, C.POINTER(C.c_uint)]),
         "spectral_fno_equilibrium": (i, [v]),
         "spectral_plan_set_learned_floor": (i, [v, d]),
         "spectral_fno_predict": (i, [v, v, v, i, v]),
@@ -575,6 +577,16 @@ class FourierOperator:
     @output_scale.setter
     def output_scale(self, sigma: float):
         _check(self.L.spectral_fno_set_output_scale(self.h, float(sigma)), "fno_set_output_scale")
+
+    def set_channel_mix_kernel(self, tma: bool):
+        """1: the TMA warp-specialised channel mix in inference (default); 0: gemm_sa."""
+        _check(self.L.spectral_fno_set_channel_mix_kernel(self.h, 1 if tma else 0),
+               "fno_set_channel_mix_kernel")
+
+    def status(self) -> int:
+        s = C.c_uint()
+        _check(self.L.spectral_fno_status(self.h, C.byref(s)), "fno_status")
+        return s.value
 
     def set_fused(self, on: bool):
         _check(self.L.spectral_fno_set_fused(self.h, 1 if on else 0), "fno_set_fused")

@@ -36,13 +36,17 @@
 // contiguous stream (fno_gemm.cuh), and every weight gradient a gemm_nt.
 #include "common.cuh"
 #include "fno.h"
+#include "fno_cm.cuh"
 #include "fno_fused.cuh"
 #include "fno_gemm.cuh"
 #include "kernels.h"
 #include "../../include/spectral_bte.h"
 
+#include <cudaTypedefs.h>
+
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <cstring>
 #include <map>
 #include <type_traits>
@@ -727,6 +731,10 @@ struct spectral_fno_s {
     double *d_v = nullptr;
     double *fM = nullptr;
     int capM = 0;
+    // channel mix of inference passes: 1 = the TMA warp-specialised kernel
+    // (fno_cm.cuh) where the shape allows, 0 = gemm_sa
+    int cm_tma = 1;
+    unsigned int *d_status = nullptr;  // bounded-wait timeouts of that kernel
     float *params = nullptr, *grads = nullptr, *am = nullptr, *av = nullptr;
     long long adam_t = 0;
     int prec = 0;                      // 0: BF16 elements, 1: FP16 elements
@@ -777,6 +785,7 @@ struct spectral_fno_s {
         cudaFree(cls);
         cudaFree(d_v);
         cudaFree(fM);
+        cudaFree(d_status);
     }
 };
 
@@ -1023,6 +1032,74 @@ int fused_layer(spectral_fno_s *n, int l, const uint16_t *hin, uint16_t *hout, f
     return kOk;
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library); null where the driver does not provide it.
+PFN_cuTensorMapEncodeTiled_v12000 tma_encode_fn()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                             cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    });
+    return fn;
+}
+
+// A 2D tensor map over a [rows][Bp] array of 16-bit elements (rows = points x
+// channels), box = box_y rows x box_x elements.
+bool act_map(CUtensorMap *m, const void *base, long long Bp, long long rows, int box_x,
+             int box_y, bool swizzle128)
+{
+    auto enc = tma_encode_fn();
+    if (!enc) return false;
+    const cuuint64_t dim[2] = {(cuuint64_t)Bp, (cuuint64_t)rows};
+    const cuuint64_t stride[1] = {(cuuint64_t)Bp * 2};
+    const cuuint32_t box[2] = {(cuuint32_t)box_x, (cuuint32_t)box_y};
+    const cuuint32_t estr[2] = {1, 1};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, const_cast<void *>(base), dim, stride, box,
+               estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               swizzle128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
+           CUDA_SUCCESS;
+}
+
+constexpr int kCmStages = 3;
+
+// The channel mix of one inference layer by cm_ws_kernel when the shape
+// allows it (64 channels, Bp a multiple of 64, tensor maps available): ran
+// tells whether it did (else the caller uses gemm_sa); returns a status.
+template <typename E>
+int channel_mix_tma(spectral_fno_s *n, int l, const uint16_t *hin, const uint16_t *S,
+                    uint16_t *hout, bool gelu, int Bp, cudaStream_t st, bool &ran)
+{
+    ran = false;
+    if (!n->cm_tma || n->C != kCmC || Bp % kCmBN != 0 || !n->d_status) return kOk;
+    const long long rows = n->P * kCmC;
+    CUtensorMap tH, tS, tO;
+    if (!act_map(&tH, hin, Bp, rows, kCmBN, kCmC, true) ||
+        !act_map(&tS, S, Bp, rows, kCmBN, kCmC, true) ||
+        !act_map(&tO, hout, Bp, rows, 16, kCmC, false))
+        return kOk;
+    using L = CmLayout<kCmStages>;
+    auto kern = cm_ws_kernel<E, kCmStages>;
+    FNO_LAUNCH(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)L::kAlloc));
+    const int nb = Bp / kCmBN;
+    const long long total = n->P * nb;
+    const int grid = (int)std::min<long long>(total, 152LL * 3);
+    kern<<<grid, kCmThreads, L::kAlloc, st>>>(tH, tS, tO, n->params + n->oW[l],
+                                              n->params + n->ob[l], gelu ? 1 : 0, nb, total,
+                                              kWaitLimitClocks, n->d_status);
+    add_launches(1);
+    FNO_LAUNCH(cudaGetLastError());
+    ran = true;
+    return kOk;
+}
+
 // The next event pair for a timed channel-mix launch, or null when profiling
 // is off or the stream is being captured into a graph.
 std::pair<cudaEvent_t, cudaEvent_t> *prof_pair(spectral_fno_s *n, cudaStream_t st)
@@ -1075,6 +1152,17 @@ int forward(spectral_fno_s *n, const T *f, int B, int Bp, bool train, cudaStream
             continue;
         }
         FNO_TRY(spectral_inv<E>(n, n->Y, n->S, nullptr, 1.f, Bp, st));
+        if (!train) {
+            auto *ev = prof_pair(n, st);
+            if (ev) cudaEventRecord(ev->first, st);
+            bool ran = false;
+            FNO_TRY(channel_mix_tma<E>(n, l, hin, n->S, hout, gelu, Bp, st, ran));
+            if (ran) {
+                if (ev) cudaEventRecord(ev->second, st);
+                continue;
+            }
+            if (ev) n->pev_used--;  // not used: gemm_sa takes its own pair below
+        }
         SaArgs a = sa_base(prm + n->oW[l], C, 1, 0, (int)C, (int)C);
         a.B = sv(hin, Bp, Bp, C * Bp);
         a.C = sv(hout, Bp, Bp, C * Bp);
@@ -1489,6 +1577,11 @@ int spectral_fno_create(spectral_fno **out, int N, int width, int modes, int lay
         const float one = 1.f;
         if ((rc = up(&n->gs, &one, 1)) != kOk) return fail(rc);
     }
+    if (cudaMalloc((void **)&n->d_status, sizeof(unsigned)) != cudaSuccess ||
+        cudaMemset(n->d_status, 0, sizeof(unsigned)) != cudaSuccess) {
+        set_error(kErrNoMem, "spectral_fno_create: status word");
+        return fail(kErrNoMem);
+    }
     if (cudaMalloc((void **)&n->cls, sizeof(int) * tab.size()) != cudaSuccess ||
         cudaMemcpy(n->cls, tab.data(), sizeof(int) * tab.size(), cudaMemcpyHostToDevice) !=
             cudaSuccess) {
@@ -1617,6 +1710,28 @@ int spectral_fno_set_equilibrium(spectral_fno *n, int on, const double *v)
 }
 
 int spectral_fno_equilibrium(spectral_fno *n) { return n ? n->eq : -1; }
+
+int spectral_fno_set_channel_mix_kernel(spectral_fno *n, int tma)
+{
+    if (!n) {
+        set_error(kErrArg, "spectral_fno_set_channel_mix_kernel: null handle");
+        return kErrArg;
+    }
+    n->cm_tma = tma ? 1 : 0;
+    return kOk;
+}
+
+int spectral_fno_status(spectral_fno *n, unsigned int *status)
+{
+    if (!n || !status) {
+        set_error(kErrArg, "spectral_fno_status: bad arguments");
+        return kErrArg;
+    }
+    if (cudaSetDevice(n->device) != cudaSuccess) return kErrCuda;
+    FNO_LAUNCH(cudaMemcpy(status, n->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    FNO_LAUNCH(cudaMemset(n->d_status, 0, sizeof(unsigned)));
+    return kOk;
+}
 
 int spectral_fno_set_loss_floor(spectral_fno *n, float eps)
 {

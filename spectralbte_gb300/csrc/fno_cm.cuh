@@ -1,0 +1,219 @@
+// fno_cm.cuh -- the channel mix of a spectral layer for inference,
+// warp-specialised around the tensor memory accelerator (TMA):
+//
+//   h'[p][d][b] = act(sum_c W[d][c] h[p][c][b] + bias[d] + S[p][d][b])
+//
+// for 64 channels, activations [point][channel][instance] in 16-bit
+// elements, Bp (instances, padded) a multiple of 64.  One work item is one
+// point p and 64 instances: a 64 x 64 input tile of h and the same tile of
+// the spectral sum S, 16 KB in all, and a 64 x 64 output tile.
+//
+//  * One producer warp (one elected thread) loads both tiles of an item with
+//    two 2D TMA copies (cp.async.bulk.tensor, 128-byte swizzle) into a
+//    ST-deep ring, each stage guarded by a "full" mbarrier (transaction
+//    bytes) and an "empty" mbarrier (one arrival per consumer warp).
+//  * Four consumer warps each own 16 of the item's 64 instance columns: the
+//    64 x 64 x 16 product on the tensor cores (mma.sync m16n8k16, FP32
+//    accumulation, W resident in shared memory), then bias + S + GELU in
+//    registers, the 16-bit result into a per-warp staging tile, and a 2D TMA
+//    store of that 64 x 16 tile (cp.async.bulk.tensor ... bulk_group), double
+//    buffered so the store overlaps the next item.
+//  * No block-wide barrier inside the loop: warps only wait on mbarriers, and
+//    every wait is bounded.  A wait that runs out sets kStatusTimeout in the
+//    status word and the thread drains its own outstanding copies before it
+//    leaves.
+// The swizzle: with 128-byte rows, TMA stores the 16-byte chunk c of row r at
+// chunk c ^ (r & 7) (stage tiles are 1024-byte aligned), so the transposed
+// ldmatrix of 8 rows and the epilogue's reads of S hit 8 distinct chunks.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "common.cuh"
+#include "fno_gemm.cuh"
+#include "mbarrier.cuh"
+
+namespace sbte {
+namespace fno {
+
+constexpr int kCmC = 64;        // channels in and out
+constexpr int kCmBN = 64;       // instances per item
+constexpr int kCmWarps = 4;     // consumer warps (16 columns each)
+constexpr int kCmThreads = 32 * (kCmWarps + 1);
+
+template <int ST> struct CmLayout {
+    static constexpr int kTile = kCmC * kCmBN * 2;            // 8 KB, one 16-bit tile
+    static constexpr int kStage = 2 * kTile;                  // h tile + S tile
+    static constexpr int kWP = kCmC + 8;                      // padded W row (elements)
+    static constexpr int kW = kCmC * kWP * 2;                 // 9 KB
+    static constexpr int kStg = kCmC * 16 * 2;                // 2 KB: 64 rows x 16 columns
+    static constexpr size_t kStageOff = 0;
+    static constexpr size_t kWOff = (size_t)ST * kStage;
+    static constexpr size_t kStgOff = kWOff + kW;
+    static constexpr size_t kBytes = kStgOff + (size_t)kCmWarps * 2 * kStg;
+    static constexpr size_t kAlloc = kBytes + 1024;           // room to align the base
+};
+
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y,
+                                            uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap *map, const void *src, int x,
+                                             int y)
+{
+    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];"
+                 ::"l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(src))
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;"); }
+__device__ __forceinline__ void bulk_wait_read1()
+{
+    asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+template <typename E, int ST>
+__global__ void __launch_bounds__(kCmThreads, 3)
+cm_ws_kernel(const __grid_constant__ CUtensorMap tH, const __grid_constant__ CUtensorMap tS,
+             const __grid_constant__ CUtensorMap tO, const float *__restrict__ W,
+             const float *__restrict__ bias, int act, int nb, long long total,
+             long long wait_limit, unsigned int *__restrict__ status)
+{
+    using T2 = typename Elem<E>::T2;
+    using L = CmLayout<ST>;
+    extern __shared__ unsigned char cm_smem_raw[];
+    unsigned char *smem = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(cm_smem_raw) + 1023) & ~(uintptr_t)1023);
+    __shared__ uint64_t full[ST], empty[ST];
+    E *sW = reinterpret_cast<E *>(smem + L::kWOff);
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (tid == 0) {
+        for (int s = 0; s < ST; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], kCmWarps);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    // W (FP32 parameters) -> 16-bit, padded rows
+    for (int e = tid; e < kCmC * kCmC; e += kCmThreads) {
+        const int m = e / kCmC, k = e % kCmC;
+        sW[m * L::kWP + k] = Elem<E>::cvt(W[e]);
+    }
+    __syncthreads();
+
+    if (warp == kCmWarps) {
+        // ------------------------------------------------------ producer
+        if (lane != 0) return;
+        long long it = 0;
+        for (long long i = blockIdx.x; i < total; i += gridDim.x, it++) {
+            const int s = (int)(it % ST);
+            if (it >= ST &&
+                !mbar_wait_bounded(&empty[s], (uint32_t)(((it / ST) - 1) & 1), wait_limit)) {
+                atomicOr(status, kStatusTimeout);
+                // drain: the stages issued since the one that never came back
+                for (long long j = it - ST + 1; j < it; j++)
+                    (void)mbar_wait_bounded(&full[j % ST], (uint32_t)((j / ST) & 1), wait_limit);
+                return;
+            }
+            const int p = (int)(i / nb), b0 = (int)(i % nb) * kCmBN;
+            unsigned char *st = smem + L::kStageOff + (size_t)s * L::kStage;
+            mbar_expect_tx(&full[s], (uint32_t)L::kStage);
+            tma_load_2d(st, &tH, b0, p * kCmC, &full[s]);
+            tma_load_2d(st + L::kTile, &tS, b0, p * kCmC, &full[s]);
+        }
+        return;
+    }
+
+    // ---------------------------------------------------------- consumers
+    const int g = lane >> 2, t = lane & 3;
+    const int col0 = warp * 16;  // this warp's 16 columns of the 64
+    float bm[4][2];
+#pragma unroll
+    for (int fm = 0; fm < 4; fm++) {
+        bm[fm][0] = bias[16 * fm + g];
+        bm[fm][1] = bias[16 * fm + g + 8];
+    }
+    E *stg0 = reinterpret_cast<E *>(smem + L::kStgOff + (size_t)warp * 2 * L::kStg);
+    long long it = 0;
+    for (long long i = blockIdx.x; i < total; i += gridDim.x, it++) {
+        const int s = (int)(it % ST);
+        if (!mbar_wait_bounded(&full[s], (uint32_t)((it / ST) & 1), wait_limit)) {
+            atomicOr(status, kStatusTimeout);
+            for (long long j = it + 1; j < it + ST && j < total; j++)
+                (void)mbar_wait_bounded(&full[j % ST], (uint32_t)((j / ST) & 1), wait_limit);
+            if (lane == 0) bulk_wait_all();
+            return;
+        }
+        const unsigned char *st = smem + L::kStageOff + (size_t)s * L::kStage;
+        const E *sB = reinterpret_cast<const E *>(st);
+        const unsigned char *sS = st + L::kTile;
+        float acc[4][2][4];
+#pragma unroll
+        for (int fm = 0; fm < 4; fm++)
+#pragma unroll
+            for (int fn = 0; fn < 2; fn++)
+#pragma unroll
+                for (int r = 0; r < 4; r++) acc[fm][fn][r] = 0.f;
+#pragma unroll
+        for (int kk = 0; kk < kCmC; kk += 16) {
+            uint32_t a[4][4], b[4];
+#pragma unroll
+            for (int fm = 0; fm < 4; fm++)
+                ldsm_x4(a[fm], sW + (16 * fm + (lane & 15)) * L::kWP + kk + (lane >> 4) * 8);
+            const int krow = kk + (lane & 15);
+            const int chunk = (col0 >> 3) + (lane >> 4);
+            ldsm_x4_t(b, reinterpret_cast<const unsigned char *>(sB) + krow * 128 +
+                             ((chunk ^ (krow & 7)) << 4));
+#pragma unroll
+            for (int fm = 0; fm < 4; fm++) {
+                mma16816<E>(acc[fm][0], a[fm], b[0], b[1]);
+                mma16816<E>(acc[fm][1], a[fm], b[2], b[3]);
+            }
+        }
+        // the staging tile of this item: its store two items ago has read it
+        E *stg = stg0 + (it & 1) * (kCmC * 16);
+        if (lane == 0) bulk_wait_read1();
+        __syncwarp();
+#pragma unroll
+        for (int fm = 0; fm < 4; fm++)
+#pragma unroll
+            for (int hh = 0; hh < 2; hh++) {
+                const int m = 16 * fm + g + 8 * hh;
+#pragma unroll
+                for (int fn = 0; fn < 2; fn++) {
+                    const int c = col0 + 8 * fn + 2 * t;  // column in the 64-wide tile
+                    const T2 sv = *reinterpret_cast<const T2 *>(
+                        sS + m * 128 + ((((c >> 3) ^ (m & 7))) << 4) + (c & 7) * 2);
+                    const float2 ad = Elem<E>::f2(sv);
+                    const float z0 = acc[fm][fn][2 * hh] + bm[fm][hh] + ad.x;
+                    const float z1 = acc[fm][fn][2 * hh + 1] + bm[fm][hh] + ad.y;
+                    *reinterpret_cast<T2 *>(stg + m * 16 + 8 * fn + 2 * t) =
+                        act ? Elem<E>::cvt2(gelu_f(z0), gelu_f(z1)) : Elem<E>::cvt2(z0, z1);
+                }
+            }
+        fence_async_smem();
+        __syncwarp();
+        if (lane == 0) {
+            mbar_arrive(&empty[s]);  // stage s read by this warp
+            const int p = (int)(i / nb), b0 = (int)(i % nb) * kCmBN;
+            tma_store_2d(&tO, stg, b0 + col0, p * kCmC);
+            bulk_commit();
+        }
+    }
+    if (lane == 0) bulk_wait_all();
+}
+
+}  // namespace fno
+}  // namespace sbte

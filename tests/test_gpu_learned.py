@@ -395,3 +395,25 @@ def test_floored_spot_check(gpu):
         got = plan.learned_stats()["last_err"]
         assert abs(got - want) <= 1e-9 * want, (eps, got, want)
     plan.set_learned(None)
+
+
+@pytest.mark.parametrize("B,prec", [(64, 1), (128, 0), (40, 1)])
+def test_tma_channel_mix_matches_gemm(gpu, B, prec):
+    """The inference channel mix through the TMA warp-specialised kernel
+    (width 64, instances padded to a multiple of 64) equals the general
+    tensor-core GEMM: same products in the same order, same epilogue.  At
+    B = 40 (padded to 40) the general GEMM runs either way."""
+    import torch
+    net = gpu.FourierOperator(16, 64, 8, 3, 32, seed=4, precision=prec)
+    net.output_scale = 0.5
+    rng = np.random.default_rng(B)
+    f = torch.from_numpy(rng.uniform(0.05, 1.0, (B, 16 ** 3))).cuda()
+    out = {}
+    for tma in (True, False):
+        net.set_channel_mix_kernel(tma)
+        Q = torch.empty_like(f)
+        net.predict(f, Q, B)
+        torch.cuda.synchronize()
+        out[tma] = Q.cpu().numpy()
+    assert net.status() == 0
+    assert np.abs(out[True] - out[False]).max() <= 1e-6 * np.abs(out[False]).max()
