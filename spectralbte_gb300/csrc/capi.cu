@@ -595,15 +595,17 @@ static int generate_closed_device(WeightsDev &wd, const IsoWeightSpec &s, bool f
     wp.zmax = std::max(fabs(s.zeta[0]), fabs(s.zeta[N - 1]));
     // every nonzero gain argument mu |zeta| and |xi - mu zeta| must be at
     // least 1/2 / L_v: the smallest nonzero |xi_a - mu zeta_a| over one axis
-    // bounds the second from below, and mu min |zeta_a| the first
+    // bounds the second from below, and mu min |zeta_a| the first.  Values
+    // below ztol (1e-9 of the grid step) are zeros that rounding left.
     const double small = 0.5 / s.L_v;
+    wp.ztol = 1e-9 * fabs(deta);
     double m1 = 1e300, m0 = 1e300;
     for (int a = 0; a < N; a++) {
         const double za = fabs(s.zeta[a]);
-        if (za != 0.0) m0 = std::min(m0, wp.mu * za);
+        if (wp.mu * za >= wp.ztol) m0 = std::min(m0, wp.mu * za);
         for (int b = 0; b < N; b++) {
             const double d = fabs(s.zeta[b] - wp.mu * s.zeta[a]);
-            if (d != 0.0) m1 = std::min(m1, d);
+            if (d >= wp.ztol) m1 = std::min(m1, d);
         }
     }
     if (m0 < small || m1 < small) {

@@ -194,6 +194,9 @@ struct WeightParams {
     int N;
     double L_v, lambda, mu, dfac, prefactor;
     double zmax;  // max |zeta_a| over the grid
+    // closed form: a gain argument below ztol is a zero of exact arithmetic
+    // left by rounding (xi = mu zeta up to the last bit) and is taken as 0
+    double ztol = 0.0;
 };
 // Largest panel count the row kernel supports (16 nodes per panel).
 constexpr int kWeightMaxPanels = 160;

@@ -212,8 +212,11 @@ __device__ __forceinline__ double w_closed(const double *__restrict__ zeta, cons
     const double a1 = sqrt(k1 * k1 + k2 * k2 + k3 * k3);
     const double d1 = k1 - mu * z1, d2 = k2 - mu * z2, d3 = k3 - mu * z3;
     const double a2 = sqrt(d1 * d1 + d2 * d2 + d3 * d3);
+    // a zero of exact arithmetic that rounding left as a few ulps: the gain is
+    // continuous there, and its a2 -> 0 branch is the accurate one
     return wtn(l, N) * wtn(m, N) * wtn(n, N) * wp.dfac *
-           (wp.prefactor * ghat_closed_d(a0, a1, a2, lam, wp.L_v));
+           (wp.prefactor * ghat_closed_d(a0 < wp.ztol ? 0.0 : a0, a1, a2 < wp.ztol ? 0.0 : a2,
+                                         lam, wp.L_v));
 }
 
 // FP64 rows [row0, row0 + nrows) of the table, row-major.

@@ -328,19 +328,16 @@ def test_equilibrium_form_gradients_match_oracle(gpu, B, shape, floor):
     off, _ = spec.layout()
     # The halves f and M_f push the gradients of the lift (P, bP) in nearly
     # opposite directions, so those blocks are small sums with heavy
-    # cancellation (the rounding oracle is itself 6% from FP64 on bP): they
-    # are held to the error bars of the other blocks relative to the norm of
-    # the whole gradient as well.
-    whole = np.sqrt(sum(np.sum(v ** 2) for v in gr.values()))
+    # cancellation: 16-bit rounding alone moves them by several percent (the
+    # rounding oracle's distance from FP64, gap).  Every block is held to the
+    # rounding oracle within max(5e-3, 3 gap) and to FP64 within
+    # max(5e-2, 2 gap); an indexing or formula error is O(1).
     for k, (o, n) in off.items():
         gk = g[o:o + n].astype(np.float64)
         ref_r, ref_64 = gr[k].reshape(-1), g64[k].reshape(-1)
         gap = rel_l2(ref_r, ref_64)
-        err = np.linalg.norm(gk - ref_r)
-        assert (err < max(5e-3, 2 * gap) * np.linalg.norm(ref_r) or
-                err < 1e-4 * whole), (k, gap, err / np.linalg.norm(ref_r))
-        assert (np.linalg.norm(gk - ref_64) < 5e-2 * np.linalg.norm(ref_64) or
-                np.linalg.norm(gk - ref_64) < 1e-3 * whole), k
+        assert rel_l2(gk, ref_r) < max(5e-3, 3 * gap), (k, gap, rel_l2(gk, ref_r))
+        assert rel_l2(gk, ref_64) < max(5e-2, 2 * gap), (k, gap, rel_l2(gk, ref_64))
 
 
 def test_equilibrium_form_is_small_at_equilibrium(gpu):
