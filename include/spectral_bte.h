@@ -431,8 +431,8 @@ int spectral_plan_set_learned(spectral_plan *plan, spectral_fno *net,
 /* Floor of the spot check (default 0): with eps > 0 the check's distance is
    |Q_net - Q| / sqrt(|Q|^2 + eps * mean over the batch of |Q_net,b|^2), the
    normalisation of the training loss with the same eps.  Near equilibrium
-   Q -> 0 for every method, and the plain FP32 operator itself then differs
-   from FP64 by more than 1e-3 of |Q|; the floor measures the error against
+   Q -> 0, so the relative distance of any approximation with a given
+   absolute error grows without bound; the floor measures the error against
    the collision term's scale in the batch instead. */
 int spectral_plan_set_learned_floor(spectral_plan *plan, double eps);
 int spectral_plan_learned_stats(spectral_plan *plan, long long *calls,
