@@ -578,9 +578,10 @@ class FourierOperator:
     def output_scale(self, sigma: float):
         _check(self.L.spectral_fno_set_output_scale(self.h, float(sigma)), "fno_set_output_scale")
 
-    def set_channel_mix_kernel(self, tma: bool):
-        """1: the TMA warp-specialised channel mix in inference (default); 0: gemm_sa."""
-        _check(self.L.spectral_fno_set_channel_mix_kernel(self.h, 1 if tma else 0),
+    def set_channel_mix_kernel(self, mode):
+        """Inference channel mix: 1 (default), 2, 3 = shapes of the TMA
+        warp-specialised kernel; 0 (or False) = the general GEMM."""
+        _check(self.L.spectral_fno_set_channel_mix_kernel(self.h, int(mode)),
                "fno_set_channel_mix_kernel")
 
     def status(self) -> int:

@@ -1067,35 +1067,50 @@ bool act_map(CUtensorMap *m, const void *base, long long Bp, long long rows, int
            CUDA_SUCCESS;
 }
 
-constexpr int kCmStages = 3;
-
 // The channel mix of one inference layer by cm_ws_kernel when the shape
 // allows it (64 channels, Bp a multiple of 64, tensor maps available): ran
 // tells whether it did (else the caller uses gemm_sa); returns a status.
+// Kernel shapes (spectral_fno_set_channel_mix_kernel): 1 = 4 consumer warps,
+// 3 stages, 3 CTAs per SM; 2 = 8 consumer warps (two row halves), 3 stages,
+// 2 CTAs per SM; 3 = 4 consumer warps, 4 stages, 2 CTAs per SM.
+template <typename E, int ST, int RW, int MINB>
+int launch_cm(spectral_fno_s *n, int l, const CUtensorMap &tH, const CUtensorMap &tS,
+              const CUtensorMap &tO, bool gelu, int nb, long long total, cudaStream_t st)
+{
+    using L = CmLayout<ST, RW>;
+    auto kern = cm_ws_kernel<E, ST, RW, MINB>;
+    FNO_LAUNCH(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)L::kAlloc));
+    const int grid = (int)std::min<long long>(total, 152LL * MINB);
+    kern<<<grid, L::kThreads, L::kAlloc, st>>>(tH, tS, tO, n->params + n->oW[l],
+                                               n->params + n->ob[l], gelu ? 1 : 0, nb, total,
+                                               kWaitLimitClocks, n->d_status);
+    add_launches(1);
+    FNO_LAUNCH(cudaGetLastError());
+    return kOk;
+}
+
 template <typename E>
 int channel_mix_tma(spectral_fno_s *n, int l, const uint16_t *hin, const uint16_t *S,
                     uint16_t *hout, bool gelu, int Bp, cudaStream_t st, bool &ran)
 {
     ran = false;
-    if (!n->cm_tma || n->C != kCmC || Bp % kCmBN != 0 || !n->d_status) return kOk;
+    if (n->cm_tma <= 0 || n->C != kCmC || Bp % kCmBN != 0 || !n->d_status) return kOk;
     const long long rows = n->P * kCmC;
+    const int rw = n->cm_tma == 2 ? 2 : 1;
     CUtensorMap tH, tS, tO;
     if (!act_map(&tH, hin, Bp, rows, kCmBN, kCmC, true) ||
         !act_map(&tS, S, Bp, rows, kCmBN, kCmC, true) ||
-        !act_map(&tO, hout, Bp, rows, 16, kCmC, false))
+        !act_map(&tO, hout, Bp, rows, 16, kCmC / rw, false))
         return kOk;
-    using L = CmLayout<kCmStages>;
-    auto kern = cm_ws_kernel<E, kCmStages>;
-    FNO_LAUNCH(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)L::kAlloc));
     const int nb = Bp / kCmBN;
     const long long total = n->P * nb;
-    const int grid = (int)std::min<long long>(total, 152LL * 3);
-    kern<<<grid, kCmThreads, L::kAlloc, st>>>(tH, tS, tO, n->params + n->oW[l],
-                                              n->params + n->ob[l], gelu ? 1 : 0, nb, total,
-                                              kWaitLimitClocks, n->d_status);
-    add_launches(1);
-    FNO_LAUNCH(cudaGetLastError());
+    if (n->cm_tma == 2)
+        FNO_TRY((launch_cm<E, 3, 2, 2>(n, l, tH, tS, tO, gelu, nb, total, st)));
+    else if (n->cm_tma == 3)
+        FNO_TRY((launch_cm<E, 4, 1, 2>(n, l, tH, tS, tO, gelu, nb, total, st)));
+    else
+        FNO_TRY((launch_cm<E, 3, 1, 3>(n, l, tH, tS, tO, gelu, nb, total, st)));
     ran = true;
     return kOk;
 }
@@ -1717,7 +1732,11 @@ int spectral_fno_set_channel_mix_kernel(spectral_fno *n, int tma)
         set_error(kErrArg, "spectral_fno_set_channel_mix_kernel: null handle");
         return kErrArg;
     }
-    n->cm_tma = tma ? 1 : 0;
+    if (tma < 0 || tma > 3) {
+        set_error(kErrArg, "spectral_fno_set_channel_mix_kernel: 0 .. 3");
+        return kErrArg;
+    }
+    n->cm_tma = tma;
     return kOk;
 }
 

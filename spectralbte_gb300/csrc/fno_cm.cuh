@@ -12,12 +12,13 @@
 //    two 2D TMA copies (cp.async.bulk.tensor, 128-byte swizzle) into a
 //    ST-deep ring, each stage guarded by a "full" mbarrier (transaction
 //    bytes) and an "empty" mbarrier (one arrival per consumer warp).
-//  * Four consumer warps each own 16 of the item's 64 instance columns: the
-//    64 x 64 x 16 product on the tensor cores (mma.sync m16n8k16, FP32
-//    accumulation, W resident in shared memory), then bias + S + GELU in
-//    registers, the 16-bit result into a per-warp staging tile, and a 2D TMA
-//    store of that 64 x 16 tile (cp.async.bulk.tensor ... bulk_group), double
-//    buffered so the store overlaps the next item.
+//  * 4 RW consumer warps: warp (wr, wc) owns output rows [64/RW wr, +64/RW)
+//    and instance columns [16 wc, +16): its 64/RW x 16 block of the product on
+//    the tensor cores (mma.sync m16n8k16, FP32 accumulation, W resident in
+//    shared memory), then bias + S + GELU in registers, the 16-bit result
+//    into a per-warp staging tile, and a 2D TMA store of that tile
+//    (cp.async.bulk.tensor ... bulk_group), double buffered so the store
+//    overlaps the next item.
 //  * No block-wide barrier inside the loop: warps only wait on mbarriers, and
 //    every wait is bounded.  A wait that runs out sets kStatusTimeout in the
 //    status word and the thread drains its own outstanding copies before it
@@ -40,19 +41,20 @@ namespace fno {
 
 constexpr int kCmC = 64;        // channels in and out
 constexpr int kCmBN = 64;       // instances per item
-constexpr int kCmWarps = 4;     // consumer warps (16 columns each)
-constexpr int kCmThreads = 32 * (kCmWarps + 1);
 
-template <int ST> struct CmLayout {
+template <int ST, int RW> struct CmLayout {
+    static constexpr int kWarps = 4 * RW;                     // consumer warps
+    static constexpr int kThreads = 32 * (kWarps + 1);
+    static constexpr int kRows = kCmC / RW;                   // output rows per warp
     static constexpr int kTile = kCmC * kCmBN * 2;            // 8 KB, one 16-bit tile
     static constexpr int kStage = 2 * kTile;                  // h tile + S tile
     static constexpr int kWP = kCmC + 8;                      // padded W row (elements)
     static constexpr int kW = kCmC * kWP * 2;                 // 9 KB
-    static constexpr int kStg = kCmC * 16 * 2;                // 2 KB: 64 rows x 16 columns
+    static constexpr int kStg = kRows * 16 * 2;               // rows x 16 columns, 16-bit
     static constexpr size_t kStageOff = 0;
     static constexpr size_t kWOff = (size_t)ST * kStage;
     static constexpr size_t kStgOff = kWOff + kW;
-    static constexpr size_t kBytes = kStgOff + (size_t)kCmWarps * 2 * kStg;
+    static constexpr size_t kBytes = kStgOff + (size_t)kWarps * 2 * kStg;
     static constexpr size_t kAlloc = kBytes + 1024;           // room to align the base
 };
 
@@ -83,15 +85,16 @@ __device__ __forceinline__ void fence_async_smem()
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
-template <typename E, int ST>
-__global__ void __launch_bounds__(kCmThreads, 3)
+template <typename E, int ST, int RW, int MINB>
+__global__ void __launch_bounds__(CmLayout<ST, RW>::kThreads, MINB)
 cm_ws_kernel(const __grid_constant__ CUtensorMap tH, const __grid_constant__ CUtensorMap tS,
              const __grid_constant__ CUtensorMap tO, const float *__restrict__ W,
              const float *__restrict__ bias, int act, int nb, long long total,
              long long wait_limit, unsigned int *__restrict__ status)
 {
     using T2 = typename Elem<E>::T2;
-    using L = CmLayout<ST>;
+    using L = CmLayout<ST, RW>;
+    constexpr int kCmWarps = L::kWarps, kCmThreads = L::kThreads, FM = L::kRows / 16;
     extern __shared__ unsigned char cm_smem_raw[];
     unsigned char *smem = reinterpret_cast<unsigned char *>(
         (reinterpret_cast<uintptr_t>(cm_smem_raw) + 1023) & ~(uintptr_t)1023);
@@ -138,12 +141,13 @@ cm_ws_kernel(const __grid_constant__ CUtensorMap tH, const __grid_constant__ CUt
 
     // ---------------------------------------------------------- consumers
     const int g = lane >> 2, t = lane & 3;
-    const int col0 = warp * 16;  // this warp's 16 columns of the 64
-    float bm[4][2];
+    const int col0 = (warp & 3) * 16;        // this warp's 16 columns of the 64
+    const int row0 = (warp >> 2) * L::kRows;  // and its rows
+    float bm[FM][2];
 #pragma unroll
-    for (int fm = 0; fm < 4; fm++) {
-        bm[fm][0] = bias[16 * fm + g];
-        bm[fm][1] = bias[16 * fm + g + 8];
+    for (int fm = 0; fm < FM; fm++) {
+        bm[fm][0] = bias[row0 + 16 * fm + g];
+        bm[fm][1] = bias[row0 + 16 * fm + g + 8];
     }
     E *stg0 = reinterpret_cast<E *>(smem + L::kStgOff + (size_t)warp * 2 * L::kStg);
     long long it = 0;
@@ -159,38 +163,39 @@ cm_ws_kernel(const __grid_constant__ CUtensorMap tH, const __grid_constant__ CUt
         const unsigned char *st = smem + L::kStageOff + (size_t)s * L::kStage;
         const E *sB = reinterpret_cast<const E *>(st);
         const unsigned char *sS = st + L::kTile;
-        float acc[4][2][4];
+        float acc[FM][2][4];
 #pragma unroll
-        for (int fm = 0; fm < 4; fm++)
+        for (int fm = 0; fm < FM; fm++)
 #pragma unroll
             for (int fn = 0; fn < 2; fn++)
 #pragma unroll
                 for (int r = 0; r < 4; r++) acc[fm][fn][r] = 0.f;
 #pragma unroll
         for (int kk = 0; kk < kCmC; kk += 16) {
-            uint32_t a[4][4], b[4];
+            uint32_t a[FM][4], b[4];
 #pragma unroll
-            for (int fm = 0; fm < 4; fm++)
-                ldsm_x4(a[fm], sW + (16 * fm + (lane & 15)) * L::kWP + kk + (lane >> 4) * 8);
+            for (int fm = 0; fm < FM; fm++)
+                ldsm_x4(a[fm], sW + (row0 + 16 * fm + (lane & 15)) * L::kWP + kk + (lane >> 4) * 8);
             const int krow = kk + (lane & 15);
             const int chunk = (col0 >> 3) + (lane >> 4);
             ldsm_x4_t(b, reinterpret_cast<const unsigned char *>(sB) + krow * 128 +
                              ((chunk ^ (krow & 7)) << 4));
 #pragma unroll
-            for (int fm = 0; fm < 4; fm++) {
+            for (int fm = 0; fm < FM; fm++) {
                 mma16816<E>(acc[fm][0], a[fm], b[0], b[1]);
                 mma16816<E>(acc[fm][1], a[fm], b[2], b[3]);
             }
         }
         // the staging tile of this item: its store two items ago has read it
-        E *stg = stg0 + (it & 1) * (kCmC * 16);
+        E *stg = stg0 + (it & 1) * (L::kRows * 16);
         if (lane == 0) bulk_wait_read1();
         __syncwarp();
 #pragma unroll
-        for (int fm = 0; fm < 4; fm++)
+        for (int fm = 0; fm < FM; fm++)
 #pragma unroll
             for (int hh = 0; hh < 2; hh++) {
-                const int m = 16 * fm + g + 8 * hh;
+                const int ml = 16 * fm + g + 8 * hh;  // row in this warp's block
+                const int m = row0 + ml;
 #pragma unroll
                 for (int fn = 0; fn < 2; fn++) {
                     const int c = col0 + 8 * fn + 2 * t;  // column in the 64-wide tile
@@ -199,7 +204,7 @@ cm_ws_kernel(const __grid_constant__ CUtensorMap tH, const __grid_constant__ CUt
                     const float2 ad = Elem<E>::f2(sv);
                     const float z0 = acc[fm][fn][2 * hh] + bm[fm][hh] + ad.x;
                     const float z1 = acc[fm][fn][2 * hh + 1] + bm[fm][hh] + ad.y;
-                    *reinterpret_cast<T2 *>(stg + m * 16 + 8 * fn + 2 * t) =
+                    *reinterpret_cast<T2 *>(stg + ml * 16 + 8 * fn + 2 * t) =
                         act ? Elem<E>::cvt2(gelu_f(z0), gelu_f(z1)) : Elem<E>::cvt2(z0, z1);
                 }
             }
@@ -208,7 +213,7 @@ cm_ws_kernel(const __grid_constant__ CUtensorMap tH, const __grid_constant__ CUt
         if (lane == 0) {
             mbar_arrive(&empty[s]);  // stage s read by this warp
             const int p = (int)(i / nb), b0 = (int)(i % nb) * kCmBN;
-            tma_store_2d(&tO, stg, b0 + col0, p * kCmC);
+            tma_store_2d(&tO, stg, b0 + col0, p * kCmC + row0);
             bulk_commit();
         }
     }

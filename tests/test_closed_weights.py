@@ -55,8 +55,10 @@ def test_plan_without_fp64_table(gpu, N, L_v):
     lam, B = 1.0, 5
     v, zeta = sb.grid_0d(N, L_v)
     f = torch.from_numpy(_two_maxwellians(v, B, 7)).cuda()
+    # both plans run the row-pair form of the same convolution shape
     ref = sb.Plan(N, L_v, v, zeta, B)
     ref.generate_weights_iso(lam)
+    ref.set_tuning(64, 3, 16, variant=3, zs=8)
     Qr = torch.empty_like(f)
     ref.computeQ_device(f, Qr, B, sb.FP32 | sb.CONSERVE)
     Qr_mp = torch.empty_like(f)
@@ -71,6 +73,7 @@ def test_plan_without_fp64_table(gpu, N, L_v):
     plan.generate_weights_closed(lam, fp64_table=False)
     torch.cuda.synchronize()
     free1, _ = torch.cuda.mem_get_info()
+    plan.set_tuning(64, 3, 16, variant=3, zs=8)
     nn = N * N
     sym_bytes = 4 * nn * (nn // 2 + 2) * nn
     fp64_bytes = 8 * N ** 6

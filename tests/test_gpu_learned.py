@@ -331,13 +331,14 @@ def test_equilibrium_form_gradients_match_oracle(gpu, B, shape, floor):
     # cancellation: 16-bit rounding alone moves them by several percent (the
     # rounding oracle's distance from FP64, gap).  Every block is held to the
     # rounding oracle within max(5e-3, 3 gap) and to FP64 within
-    # max(5e-2, 2 gap); an indexing or formula error is O(1).
+    # max(5e-2, 4 gap) (the two distances add); an indexing or formula error
+    # is O(1).
     for k, (o, n) in off.items():
         gk = g[o:o + n].astype(np.float64)
         ref_r, ref_64 = gr[k].reshape(-1), g64[k].reshape(-1)
         gap = rel_l2(ref_r, ref_64)
         assert rel_l2(gk, ref_r) < max(5e-3, 3 * gap), (k, gap, rel_l2(gk, ref_r))
-        assert rel_l2(gk, ref_64) < max(5e-2, 2 * gap), (k, gap, rel_l2(gk, ref_64))
+        assert rel_l2(gk, ref_64) < max(5e-2, 4 * gap), (k, gap, rel_l2(gk, ref_64))
 
 
 def test_equilibrium_form_is_small_at_equilibrium(gpu):
@@ -406,11 +407,12 @@ def test_tma_channel_mix_matches_gemm(gpu, B, prec):
     rng = np.random.default_rng(B)
     f = torch.from_numpy(rng.uniform(0.05, 1.0, (B, 16 ** 3))).cuda()
     out = {}
-    for tma in (True, False):
-        net.set_channel_mix_kernel(tma)
+    for mode in (0, 1, 2, 3):   # 0: the general GEMM; 1-3: shapes of the TMA kernel
+        net.set_channel_mix_kernel(mode)
         Q = torch.empty_like(f)
         net.predict(f, Q, B)
         torch.cuda.synchronize()
-        out[tma] = Q.cpu().numpy()
+        out[mode] = Q.cpu().numpy()
     assert net.status() == 0
-    assert np.abs(out[True] - out[False]).max() <= 1e-6 * np.abs(out[False]).max()
+    for mode in (1, 2, 3):
+        assert np.abs(out[mode] - out[0]).max() <= 1e-6 * np.abs(out[0]).max(), mode
