@@ -377,8 +377,9 @@ int spectral_fno_kernel_time(spectral_fno *net, double *ms_total, int *launches)
    accelerator (2D cp.async.bulk.tensor loads and stores, mbarrier ring) where
    the shape allows (width 64, instances padded to a multiple of 64), with 4
    consumer warps, 3 stages, 3 CTAs per SM; 2 the same with 8 consumer warps
-   and 2 CTAs per SM; 3 with 4 stages and 2 CTAs per SM; 0 runs the general
-   tensor-core GEMM.  All give the same result. */
+   and 2 CTAs per SM; 3 with 4 stages and 2 CTAs per SM; 4 with 8 consumer
+   warps, 2 stages and 3 CTAs per SM; 5 with 16 consumer warps and 2 CTAs per
+   SM; 0 runs the general tensor-core GEMM.  All give the same result. */
 int spectral_fno_set_channel_mix_kernel(spectral_fno *net, int tma);
 /* Device status word of the network's kernels (bit 0: a bounded wait gave
    up); cleared by the read. */

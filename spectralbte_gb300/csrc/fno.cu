@@ -1072,7 +1072,9 @@ bool act_map(CUtensorMap *m, const void *base, long long Bp, long long rows, int
 // tells whether it did (else the caller uses gemm_sa); returns a status.
 // Kernel shapes (spectral_fno_set_channel_mix_kernel): 1 = 4 consumer warps,
 // 3 stages, 3 CTAs per SM; 2 = 8 consumer warps (two row halves), 3 stages,
-// 2 CTAs per SM; 3 = 4 consumer warps, 4 stages, 2 CTAs per SM.
+// 2 CTAs per SM; 3 = 4 consumer warps, 4 stages, 2 CTAs per SM; 4 = 8
+// consumer warps, 2 stages, 3 CTAs per SM; 5 = 16 consumer warps (four row
+// quarters), 3 stages, 2 CTAs per SM.
 template <typename E, int ST, int RW, int MINB>
 int launch_cm(spectral_fno_s *n, int l, const CUtensorMap &tH, const CUtensorMap &tS,
               const CUtensorMap &tO, bool gelu, int nb, long long total, cudaStream_t st)
@@ -1097,7 +1099,7 @@ int channel_mix_tma(spectral_fno_s *n, int l, const uint16_t *hin, const uint16_
     ran = false;
     if (n->cm_tma <= 0 || n->C != kCmC || Bp % kCmBN != 0 || !n->d_status) return kOk;
     const long long rows = n->P * kCmC;
-    const int rw = n->cm_tma == 2 ? 2 : 1;
+    const int rw = (n->cm_tma == 2 || n->cm_tma == 4) ? 2 : (n->cm_tma == 5 ? 4 : 1);
     CUtensorMap tH, tS, tO;
     if (!act_map(&tH, hin, Bp, rows, kCmBN, kCmC, true) ||
         !act_map(&tS, S, Bp, rows, kCmBN, kCmC, true) ||
@@ -1107,6 +1109,10 @@ int channel_mix_tma(spectral_fno_s *n, int l, const uint16_t *hin, const uint16_
     const long long total = n->P * nb;
     if (n->cm_tma == 2)
         FNO_TRY((launch_cm<E, 3, 2, 2>(n, l, tH, tS, tO, gelu, nb, total, st)));
+    else if (n->cm_tma == 4)
+        FNO_TRY((launch_cm<E, 2, 2, 3>(n, l, tH, tS, tO, gelu, nb, total, st)));
+    else if (n->cm_tma == 5)
+        FNO_TRY((launch_cm<E, 3, 4, 2>(n, l, tH, tS, tO, gelu, nb, total, st)));
     else if (n->cm_tma == 3)
         FNO_TRY((launch_cm<E, 4, 1, 2>(n, l, tH, tS, tO, gelu, nb, total, st)));
     else
@@ -1732,8 +1738,8 @@ int spectral_fno_set_channel_mix_kernel(spectral_fno *n, int tma)
         set_error(kErrArg, "spectral_fno_set_channel_mix_kernel: null handle");
         return kErrArg;
     }
-    if (tma < 0 || tma > 3) {
-        set_error(kErrArg, "spectral_fno_set_channel_mix_kernel: 0 .. 3");
+    if (tma < 0 || tma > 5) {
+        set_error(kErrArg, "spectral_fno_set_channel_mix_kernel: 0 .. 5");
         return kErrArg;
     }
     n->cm_tma = tma;

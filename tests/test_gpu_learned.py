@@ -407,12 +407,12 @@ def test_tma_channel_mix_matches_gemm(gpu, B, prec):
     rng = np.random.default_rng(B)
     f = torch.from_numpy(rng.uniform(0.05, 1.0, (B, 16 ** 3))).cuda()
     out = {}
-    for mode in (0, 1, 2, 3):   # 0: the general GEMM; 1-3: shapes of the TMA kernel
+    for mode in range(6):   # 0: the general GEMM; 1-5: shapes of the TMA kernel
         net.set_channel_mix_kernel(mode)
         Q = torch.empty_like(f)
         net.predict(f, Q, B)
         torch.cuda.synchronize()
         out[mode] = Q.cpu().numpy()
     assert net.status() == 0
-    for mode in (1, 2, 3):
+    for mode in range(1, 6):
         assert np.abs(out[mode] - out[0]).max() <= 1e-6 * np.abs(out[0]).max(), mode
