@@ -731,9 +731,11 @@ struct spectral_fno_s {
     double *d_v = nullptr;
     double *fM = nullptr;
     int capM = 0;
-    // channel mix of inference passes: 1 = the TMA warp-specialised kernel
-    // (fno_cm.cuh) where the shape allows, 0 = gemm_sa
-    int cm_tma = 1;
+    // channel mix of inference passes: 1..5 = shapes of the TMA
+    // warp-specialised kernel (fno_cm.cuh) where the shape allows, 0 = gemm_sa;
+    // 4 (8 consumer warps, 2 stages, 3 CTAs per SM) measured fastest on GB300
+    int cm_tma = 4;
+    int ro_tma = 1;  // readout of inference passes by ro_ws_kernel where the shape allows
     unsigned int *d_status = nullptr;  // bounded-wait timeouts of that kernel
     float *params = nullptr, *grads = nullptr, *am = nullptr, *av = nullptr;
     long long adam_t = 0;
@@ -1121,6 +1123,35 @@ int channel_mix_tma(spectral_fno_s *n, int l, const uint16_t *hin, const uint16_
     return kOk;
 }
 
+// The readout of an inference pass by ro_ws_kernel (kind 0, 64 channels,
+// 128 hidden, Bp a multiple of 64, tensor maps available); ran tells whether
+// it did (else the caller uses gemm_sa).
+template <typename E>
+int readout_tma(spectral_fno_s *n, const uint16_t *hL, int Bp, cudaStream_t st, bool &ran)
+{
+    ran = false;
+    if (n->C != kCmC || n->Hd != kRoHid || Bp % kCmBN != 0 || !n->d_status) return kOk;
+    CUtensorMap tH;
+    if (!act_map(&tH, hL, Bp, n->P * kCmC, kCmBN, kCmC, true)) return kOk;
+    constexpr int ST = 3, MINB = 3;
+    using L = RoLayout<ST>;
+    auto kern = ro_ws_kernel<E, ST, MINB>;
+    FNO_LAUNCH(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)L::kAlloc));
+    FNO_LAUNCH(cudaMemsetAsync(n->y, 0, sizeof(float) * (size_t)n->P * Bp, st));
+    const int nb = Bp / kCmBN;
+    const long long total = n->P * nb;
+    const int grid = (int)std::min<long long>(total, 152LL * MINB);
+    const float *prm = n->params;
+    kern<<<grid, L::kThreads, L::kAlloc, st>>>(tH, prm + n->oQ1, prm + n->oc1, prm + n->oq2,
+                                               prm + n->oc2, n->y, Bp, nb, total,
+                                               kWaitLimitClocks, n->d_status);
+    add_launches(1);
+    FNO_LAUNCH(cudaGetLastError());
+    ran = true;
+    return kOk;
+}
+
 // The next event pair for a timed channel-mix launch, or null when profiling
 // is off or the stream is being captured into a graph.
 std::pair<cudaEvent_t, cudaEvent_t> *prof_pair(spectral_fno_s *n, cudaStream_t st)
@@ -1198,6 +1229,11 @@ int forward(spectral_fno_s *n, const T *f, int B, int Bp, bool train, cudaStream
         if (ev) cudaEventRecord(ev->first, st);
         FNO_LAUNCH((launch_sa<E, 64, 64, 2, 2, false, false, kEpiLayer>(a, st)));
         if (ev) cudaEventRecord(ev->second, st);
+    }
+    if (!train && n->kind == 0 && n->ro_tma) {
+        bool ran = false;
+        FNO_TRY(readout_tma<E>(n, Hbuf(n, n->L, train), Bp, st, ran));
+        if (ran) return kOk;
     }
     SaArgs a = sa_base(prm + n->oQ1, C, 1, 0, (int)Hd, (int)C);
     a.B = sv(Hbuf(n, n->L, train), Bp, Bp, C * Bp);
@@ -1743,6 +1779,16 @@ int spectral_fno_set_channel_mix_kernel(spectral_fno *n, int tma)
         return kErrArg;
     }
     n->cm_tma = tma;
+    return kOk;
+}
+
+int spectral_fno_set_readout_kernel(spectral_fno *n, int tma)
+{
+    if (!n) {
+        set_error(kErrArg, "spectral_fno_set_readout_kernel: null handle");
+        return kErrArg;
+    }
+    n->ro_tma = tma ? 1 : 0;
     return kOk;
 }
 

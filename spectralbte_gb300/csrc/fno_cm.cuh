@@ -220,5 +220,154 @@ cm_ws_kernel(const __grid_constant__ CUtensorMap tH, const __grid_constant__ CUt
     if (lane == 0) bulk_wait_all();
 }
 
+// ---------------------------------------------------------------------------
+// The readout for inference, the same warp-specialised structure:
+//   y[p][b] = c2 + sum_m q2[m] gelu(sum_c Q1[m][c] h[p][c][b] + c1[m])
+// with 128 hidden rows m and 64 channels c.  A work item is one point and 64
+// instances: one 64 x 64 tile of h (TMA, 128-byte swizzle) into the ring.
+// Eight consumer warps: warp (wr, wc) computes hidden rows [64 wr, +64) for
+// instance columns [16 wc, +16), reduces q2 . gelu over its 64 rows with warp
+// shuffles, and adds its 16 partial sums into y with global atomics (y zeroed
+// before the launch; the wr = 0 warp adds c2 with its partial).  Each output
+// then receives exactly two additions onto zero, (c2 + part_0) and part_1,
+// and x + y = y + x holds exactly, so the result does not depend on their
+// order.
+constexpr int kRoHid = 128;
+
+template <int ST> struct RoLayout {
+    static constexpr int kWarps = 8;
+    static constexpr int kThreads = 32 * (kWarps + 1);
+    static constexpr int kTile = kCmC * kCmBN * 2;  // 8 KB
+    static constexpr int kWP = kCmC + 8;
+    static constexpr int kW = kRoHid * kWP * 2;     // 18 KB
+    static constexpr size_t kWOff = (size_t)ST * kTile;
+    static constexpr size_t kBytes = kWOff + kW;
+    static constexpr size_t kAlloc = kBytes + 1024;
+};
+
+template <typename E, int ST, int MINB>
+__global__ void __launch_bounds__(RoLayout<ST>::kThreads, MINB)
+ro_ws_kernel(const __grid_constant__ CUtensorMap tH, const float *__restrict__ Q1,
+             const float *__restrict__ c1, const float *__restrict__ q2,
+             const float *__restrict__ c2, float *__restrict__ y, int Bp, int nb,
+             long long total, long long wait_limit, unsigned int *__restrict__ status)
+{
+    using L = RoLayout<ST>;
+    constexpr int FM = 4;  // 64 rows per warp
+    extern __shared__ unsigned char ro_smem_raw[];
+    unsigned char *smem = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(ro_smem_raw) + 1023) & ~(uintptr_t)1023);
+    __shared__ uint64_t full[ST], empty[ST];
+    E *sW = reinterpret_cast<E *>(smem + L::kWOff);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (tid == 0) {
+        for (int s = 0; s < ST; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], L::kWarps);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    for (int e = tid; e < kRoHid * kCmC; e += L::kThreads) {
+        const int m = e / kCmC, k = e % kCmC;
+        sW[m * L::kWP + k] = Elem<E>::cvt(Q1[e]);
+    }
+    __syncthreads();
+
+    if (warp == L::kWarps) {
+        if (lane != 0) return;
+        long long it = 0;
+        for (long long i = blockIdx.x; i < total; i += gridDim.x, it++) {
+            const int s = (int)(it % ST);
+            if (it >= ST &&
+                !mbar_wait_bounded(&empty[s], (uint32_t)(((it / ST) - 1) & 1), wait_limit)) {
+                atomicOr(status, kStatusTimeout);
+                for (long long j = it - ST + 1; j < it; j++)
+                    (void)mbar_wait_bounded(&full[j % ST], (uint32_t)((j / ST) & 1), wait_limit);
+                return;
+            }
+            const int p = (int)(i / nb), b0 = (int)(i % nb) * kCmBN;
+            mbar_expect_tx(&full[s], (uint32_t)L::kTile);
+            tma_load_2d(smem + (size_t)s * L::kTile, &tH, b0, p * kCmC, &full[s]);
+        }
+        return;
+    }
+
+    const int g = lane >> 2, t = lane & 3;
+    const int col0 = (warp & 3) * 16, row0 = (warp >> 2) * 64;
+    float cm[FM][2], qm[FM][2];
+#pragma unroll
+    for (int fm = 0; fm < FM; fm++)
+#pragma unroll
+        for (int hh = 0; hh < 2; hh++) {
+            cm[fm][hh] = c1[row0 + 16 * fm + g + 8 * hh];
+            qm[fm][hh] = q2[row0 + 16 * fm + g + 8 * hh];
+        }
+    const float cadd = row0 == 0 ? c2[0] : 0.f;
+    long long it = 0;
+    for (long long i = blockIdx.x; i < total; i += gridDim.x, it++) {
+        const int s = (int)(it % ST);
+        if (!mbar_wait_bounded(&full[s], (uint32_t)((it / ST) & 1), wait_limit)) {
+            atomicOr(status, kStatusTimeout);
+            for (long long j = it + 1; j < it + ST && j < total; j++)
+                (void)mbar_wait_bounded(&full[j % ST], (uint32_t)((j / ST) & 1), wait_limit);
+            return;
+        }
+        const unsigned char *sB = smem + (size_t)s * L::kTile;
+        float acc[FM][2][4];
+#pragma unroll
+        for (int fm = 0; fm < FM; fm++)
+#pragma unroll
+            for (int fn = 0; fn < 2; fn++)
+#pragma unroll
+                for (int r = 0; r < 4; r++) acc[fm][fn][r] = 0.f;
+#pragma unroll
+        for (int kk = 0; kk < kCmC; kk += 16) {
+            uint32_t a[FM][4], b[4];
+#pragma unroll
+            for (int fm = 0; fm < FM; fm++)
+                ldsm_x4(a[fm], sW + (row0 + 16 * fm + (lane & 15)) * L::kWP + kk + (lane >> 4) * 8);
+            const int krow = kk + (lane & 15);
+            const int chunk = (col0 >> 3) + (lane >> 4);
+            ldsm_x4_t(b, sB + krow * 128 + ((chunk ^ (krow & 7)) << 4));
+#pragma unroll
+            for (int fm = 0; fm < FM; fm++) {
+                mma16816<E>(acc[fm][0], a[fm], b[0], b[1]);
+                mma16816<E>(acc[fm][1], a[fm], b[2], b[3]);
+            }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[s]);  // the tile is in registers now
+        float part[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+#pragma unroll
+        for (int fm = 0; fm < FM; fm++)
+#pragma unroll
+            for (int hh = 0; hh < 2; hh++)
+#pragma unroll
+                for (int fn = 0; fn < 2; fn++) {
+                    part[fn][0] += qm[fm][hh] * gelu_f(acc[fm][fn][2 * hh] + cm[fm][hh]);
+                    part[fn][1] += qm[fm][hh] * gelu_f(acc[fm][fn][2 * hh + 1] + cm[fm][hh]);
+                }
+#pragma unroll
+        for (int fn = 0; fn < 2; fn++)
+#pragma unroll
+            for (int c = 0; c < 2; c++) {
+                float v = part[fn][c];
+                v += __shfl_xor_sync(0xffffffffu, v, 4);
+                v += __shfl_xor_sync(0xffffffffu, v, 8);
+                v += __shfl_xor_sync(0xffffffffu, v, 16);
+                part[fn][c] = v;
+            }
+        if (g == 0) {
+            const int p = (int)(i / nb), b0 = (int)(i % nb) * kCmBN;
+            float *yrow = y + (long long)p * Bp + b0 + col0;
+#pragma unroll
+            for (int fn = 0; fn < 2; fn++) {
+                atomicAdd(yrow + 8 * fn + 2 * t, part[fn][0] + cadd);
+                atomicAdd(yrow + 8 * fn + 2 * t + 1, part[fn][1] + cadd);
+            }
+        }
+    }
+}
+
 }  // namespace fno
 }  // namespace sbte

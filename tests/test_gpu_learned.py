@@ -416,3 +416,32 @@ def test_tma_channel_mix_matches_gemm(gpu, B, prec):
     assert net.status() == 0
     for mode in range(1, 6):
         assert np.abs(out[mode] - out[0]).max() <= 1e-6 * np.abs(out[0]).max(), mode
+
+
+@pytest.mark.parametrize("B,prec", [(64, 1), (128, 0)])
+def test_tma_readout_matches_gemm(gpu, B, prec):
+    """The inference readout through the TMA warp-specialised kernel (width
+    64, hidden 128, instances padded to a multiple of 64) against the general
+    GEMM: the hidden rows are summed in another order (two partial sums of 64
+    rows each, added atomically), so the outputs agree to FP32 rounding of the
+    readout, far below the 16-bit resolution of the activations."""
+    import torch
+    net = gpu.FourierOperator(16, 64, 8, 2, 128, seed=6, precision=prec)
+    net.output_scale = 0.5
+    rng = np.random.default_rng(B + 1)
+    f = torch.from_numpy(rng.uniform(0.05, 1.0, (B, 16 ** 3))).cuda()
+    out = {}
+    for tma in (True, False):
+        net.set_readout_kernel(tma)
+        Q = torch.empty_like(f)
+        net.predict(f, Q, B)
+        torch.cuda.synchronize()
+        out[tma] = Q.cpu().numpy()
+    assert net.status() == 0
+    assert np.abs(out[True] - out[False]).max() <= 1e-5 * np.abs(out[False]).max()
+    # deterministic: a second call gives the same bits
+    net.set_readout_kernel(True)
+    Q2 = torch.empty_like(f)
+    net.predict(f, Q2, B)
+    torch.cuda.synchronize()
+    assert np.array_equal(Q2.cpu().numpy(), out[True])
