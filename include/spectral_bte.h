@@ -388,6 +388,11 @@ int spectral_fno_set_channel_mix_kernel(spectral_fno *net, int tma);
    padded to a multiple of 64); 0 the general GEMM.  The two sum the hidden
    rows in a different order: the outputs agree to FP32 rounding. */
 int spectral_fno_set_readout_kernel(spectral_fno *net, int tma);
+/* Axis-k transforms of inference passes (the first forward and the last
+   inverse axis pass of every layer): 1 (default) runs the warp-specialised
+   TMA kernel where the shape allows (N = 32, modes <= 16); 0 the general
+   GEMM.  Same products, same K blocks: the same result. */
+int spectral_fno_set_axis_kernel(spectral_fno *net, int tma);
 /* Device status word of the network's kernels (bit 0: a bounded wait gave
    up); cleared by the read. */
 int spectral_fno_status(spectral_fno *net, unsigned int *status);

@@ -168,6 +168,7 @@ def lib() -> C.CDLL:
         "spectral_fno_set_equilibrium": (i, [v, i, _dp]),
         "spectral_fno_set_channel_mix_kernel": (i, [v, i]),
         "spectral_fno_set_readout_kernel": (i, [v, i]),
+        "spectral_fno_set_axis_kernel": (i, [v, i]),
         "spectral_fno_status": (i, [v, C.POINTER(C.c_uint)]),
         "spectral_fno_equilibrium": (i, [v]),
         "spectral_plan_set_learned_floor": (i, [v, d]),
@@ -584,6 +585,11 @@ class FourierOperator:
         warp-specialised kernel; 0 (or False) = the general GEMM."""
         _check(self.L.spectral_fno_set_channel_mix_kernel(self.h, int(mode)),
                "fno_set_channel_mix_kernel")
+
+    def set_axis_kernel(self, tma: bool):
+        """1: the TMA warp-specialised axis-k transforms in inference (default); 0: gemm_sa."""
+        _check(self.L.spectral_fno_set_axis_kernel(self.h, 1 if tma else 0),
+               "fno_set_axis_kernel")
 
     def set_readout_kernel(self, tma: bool):
         """1: the TMA warp-specialised readout in inference (default); 0: the general GEMM."""

@@ -736,6 +736,8 @@ struct spectral_fno_s {
     // 4 (8 consumer warps, 2 stages, 3 CTAs per SM) measured fastest on GB300
     int cm_tma = 4;
     int ro_tma = 1;  // readout of inference passes by ro_ws_kernel where the shape allows
+    int ax_tma = 1;  // axis-k transforms of inference passes by ax_ws_kernel
+    float *Afk = nullptr, *Aik = nullptr;  // their 32 x 32 A matrices (N = 32)
     unsigned int *d_status = nullptr;  // bounded-wait timeouts of that kernel
     float *params = nullptr, *grads = nullptr, *am = nullptr, *av = nullptr;
     long long adam_t = 0;
@@ -788,6 +790,8 @@ struct spectral_fno_s {
         cudaFree(d_v);
         cudaFree(fM);
         cudaFree(d_status);
+        cudaFree(Afk);
+        cudaFree(Aik);
     }
 };
 
@@ -891,6 +895,57 @@ void set_ext(SaArgs &a, long long eA, long long eB, long long eC)
     a.extC = eC;
 }
 
+bool act_map(CUtensorMap *m, const void *base, long long Bp, long long rows, int box_x,
+             int box_y, bool swizzle128);
+
+// The axis-k pass of an inference transform by ax_ws_kernel (N = 32,
+// 2 Km <= 32): forward (h -> T1) or inverse real part (U2 -> S).  ran tells
+// whether it ran (else the caller uses gemm_sa).
+template <typename E>
+int axis_k_tma(spectral_fno_s *n, bool inverse, const uint16_t *in, uint16_t *out, int Bp,
+               cudaStream_t st, bool &ran)
+{
+    ran = false;
+    const long long N = n->N, Km = n->Km, CB = (long long)n->C * Bp;
+    if (!n->ax_tma || N != 32 || 2 * Km > 32 || !n->Afk || !n->Aik || !n->d_status ||
+        CB % 128 != 0)
+        return kOk;
+    CUtensorMap tB, tC;
+    AxArgs a;
+    a.nb = (int)(CB / 64);
+    a.total = N * N * (CB / 128);
+    if (!inverse) {
+        if (!act_map(&tB, in, CB, N * N * N, 64, 32, true) ||
+            !act_map(&tC, out, CB, N * N * 2 * Km, 16, (int)(2 * Km), false))
+            return kOk;
+        a.A = n->Afk;
+        a.ld_rows = 32;
+        a.split = 0;
+        a.in_rows = 32;
+        a.out_rows = (int)(2 * Km);
+    } else {
+        if (!act_map(&tB, in, CB, N * N * 2 * Km, 64, (int)Km, true) ||
+            !act_map(&tC, out, CB, N * N * N, 16, 32, false))
+            return kOk;
+        a.A = n->Aik;
+        a.ld_rows = (int)Km;
+        a.split = 1;
+        a.in_rows = (int)(2 * Km);
+        a.out_rows = 32;
+    }
+    constexpr int ST = 4, MINB = 4;
+    using L = AxLayout<ST>;
+    auto kern = ax_ws_kernel<E, ST, MINB>;
+    FNO_LAUNCH(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)L::kAlloc));
+    const int grid = (int)std::min<long long>(a.total, 152LL * MINB);
+    kern<<<grid, L::kThreads, L::kAlloc, st>>>(tB, tC, a, kWaitLimitClocks, n->d_status);
+    add_launches(1);
+    FNO_LAUNCH(cudaGetLastError());
+    ran = true;
+    return kOk;
+}
+
 // The truncated forward transform of in ([p][c][b]) into out
 // ([mi][2][mj mk][c][b]): three axis passes with F (fno.cu header).  The
 // backward pass (bwd) keeps the 1/N of the first axis only and applies the
@@ -898,12 +953,14 @@ void set_ext(SaArgs &a, long long eA, long long eB, long long eC)
 // stay far from the 16-bit subnormal range: out is then N^2 times F3 in.
 template <typename E>
 int spectral_fwd(spectral_fno_s *n, const uint16_t *in, uint16_t *out, bool bwd, int Bp,
-                 cudaStream_t st, bool t1_ready = false)
+                 cudaStream_t st, bool t1_ready = false, bool tma = false)
 {
     const long long N = n->N, Km = n->Km, CB = (long long)n->C * Bp;
     const float *F = n->F, *F23 = bwd ? n->Fu : n->F;
     const Ext ext(n, Bp);
-    if (!t1_ready) {  // axis k, real input (T1 may come from the previous fused layer)
+    bool ran = false;
+    if (!t1_ready && tma && !bwd) FNO_TRY(axis_k_tma<E>(n, false, in, n->T1, Bp, st, ran));
+    if (!t1_ready && !ran) {  // axis k, real input (T1 may come from the previous fused layer)
         SaArgs a = sa_base(F, N, 1, Km * N, (int)Km, (int)N);
         a.B = sv(in, CB, CB, N * CB);
         a.C = sv(n->T1, CB, CB, 2 * Km * CB, Km * CB);
@@ -957,7 +1014,7 @@ int mode_mix(spectral_fno_s *n, const float *R, bool tr, const uint16_t *in, uin
 // or added, times alpha, into the FP32 out32 (the backward pass).
 template <typename E>
 int spectral_inv(spectral_fno_s *n, const uint16_t *in, uint16_t *out16, float *out32,
-                 float alpha, int Bp, cudaStream_t st, bool stop_at_u2 = false)
+                 float alpha, int Bp, cudaStream_t st, bool stop_at_u2 = false, bool tma = false)
 {
     const long long N = n->N, Km = n->Km, CB = (long long)n->C * Bp;
     const float *G = n->G;
@@ -980,6 +1037,11 @@ int spectral_inv(spectral_fno_s *n, const uint16_t *in, uint16_t *out16, float *
         FNO_LAUNCH((launch_sa<E, 32, 128, 1, 4, true, true, kEpiCplxBF16>(a, st)));
     }
     if (stop_at_u2) return kOk;
+    if (tma && out16 && !out32) {
+        bool ran = false;
+        FNO_TRY(axis_k_tma<E>(n, true, n->U2, out16, Bp, st, ran));
+        if (ran) return kOk;
+    }
     {  // axis k, real part
         SaArgs a = sa_base(G, Km, 1, N * Km, (int)N, (int)Km);
         a.B = sv(n->U2, CB, CB, 2 * Km * CB, Km * CB);
@@ -1191,7 +1253,7 @@ int forward(spectral_fno_s *n, const T *f, int B, int Bp, bool train, cudaStream
     for (int l = 0; l < n->L; l++) {
         uint16_t *hin = Hbuf(n, l, train), *hout = Hbuf(n, l + 1, train);
         uint16_t *xl = train ? n->X[l] : n->X[0];
-        FNO_TRY(spectral_fwd<E>(n, hin, xl, false, Bp, st, t1_ready));
+        FNO_TRY(spectral_fwd<E>(n, hin, xl, false, Bp, st, t1_ready, !train));
         t1_ready = false;
         FNO_TRY(mode_mix<E>(n, prm + n->oR[l], false, xl, n->Y, Bp, st));
         const bool gelu = n->kind == 0 && l < n->L - 1;
@@ -1203,7 +1265,7 @@ int forward(spectral_fno_s *n, const T *f, int B, int Bp, bool train, cudaStream
             t1_ready = t1_next;
             continue;
         }
-        FNO_TRY(spectral_inv<E>(n, n->Y, n->S, nullptr, 1.f, Bp, st));
+        FNO_TRY(spectral_inv<E>(n, n->Y, n->S, nullptr, 1.f, Bp, st, false, !train));
         if (!train) {
             auto *ev = prof_pair(n, st);
             if (ev) cudaEventRecord(ev->first, st);
@@ -1634,6 +1696,23 @@ int spectral_fno_create(spectral_fno **out, int N, int width, int modes, int lay
         const float one = 1.f;
         if ((rc = up(&n->gs, &one, 1)) != kOk) return fail(rc);
     }
+    if (N == 32 && 2 * Km <= 32) {
+        // A of the TMA axis-k passes (fno_cm.cuh): forward [Re F; Im F] (rows
+        // 0..2Km-1), inverse [Re G | 0 | -Im G | 0] with Im G from K row 16
+        std::vector<float> af(32 * 32, 0.f), ai(32 * 32, 0.f);
+        for (int r = 0; r < Km; r++)
+            for (int x = 0; x < N; x++) {
+                af[r * 32 + x] = Fh[r * N + x];
+                af[(Km + r) * 32 + x] = Fh[Km * N + r * N + x];
+            }
+        for (int x = 0; x < N; x++)
+            for (int q = 0; q < Km; q++) {
+                ai[x * 32 + q] = Gh[x * Km + q];
+                ai[x * 32 + 16 + q] = -Gh[N * Km + x * Km + q];
+            }
+        if ((rc = up(&n->Afk, af.data(), 32 * 32)) != kOk) return fail(rc);
+        if ((rc = up(&n->Aik, ai.data(), 32 * 32)) != kOk) return fail(rc);
+    }
     if (cudaMalloc((void **)&n->d_status, sizeof(unsigned)) != cudaSuccess ||
         cudaMemset(n->d_status, 0, sizeof(unsigned)) != cudaSuccess) {
         set_error(kErrNoMem, "spectral_fno_create: status word");
@@ -1779,6 +1858,16 @@ int spectral_fno_set_channel_mix_kernel(spectral_fno *n, int tma)
         return kErrArg;
     }
     n->cm_tma = tma;
+    return kOk;
+}
+
+int spectral_fno_set_axis_kernel(spectral_fno *n, int tma)
+{
+    if (!n) {
+        set_error(kErrArg, "spectral_fno_set_axis_kernel: null handle");
+        return kErrArg;
+    }
+    n->ax_tma = tma ? 1 : 0;
     return kOk;
 }
 

@@ -369,5 +369,161 @@ ro_ws_kernel(const __grid_constant__ CUtensorMap tH, const float *__restrict__ Q
     }
 }
 
+// ---------------------------------------------------------------------------
+// The axis-k transforms of an inference pass, the same warp-specialised
+// structure.  Both are small real products per slab s = (i, j) of the grid:
+//   forward  T1[s][r][cb] = sum_k A[r][k] h[s N + k][cb],  A = [Re F; Im F]
+//            (24 x 32 at 12 modes, N = 32: complex F times the real h),
+//   inverse  S[s N + k][cb] = sum_q A[k][q] U2[s][q][cb],  A = [Re G, -Im G]
+//            (the real part of complex G times complex U2),
+// with cb running over channels x instances (64-column blocks).  One work item
+// is one slab and two column blocks.  The 32 x 32 A (zero padded, laid out so
+// that the K blocks of 16 hold the same terms as in the general kernel: real
+// parts in K rows 0..15, imaginary parts in 16..31) stays in shared memory;
+// the producer loads the item's B rows with 2D TMA copies (one per column block
+// and K half when the input is split), eight consumer warps each multiply a
+// 32 x 16 block and store its first out_rows rows with a 2D TMA store.
+template <int ST> struct AxLayout {
+    static constexpr int kWarps = 8;
+    static constexpr int kThreads = 32 * (kWarps + 1);
+    static constexpr int kTile = 32 * 128;           // 32 K rows x 64 columns, 16-bit
+    static constexpr int kStage = 2 * kTile;         // two column blocks
+    static constexpr int kAP = 32 + 8;
+    static constexpr int kA = 32 * kAP * 2;
+    static constexpr int kStg = 32 * 16 * 2;         // 32 rows x 16 columns
+    static constexpr size_t kAOff = (size_t)ST * kStage;
+    static constexpr size_t kStgOff = kAOff + kA;
+    static constexpr size_t kBytes = kStgOff + (size_t)kWarps * 2 * kStg;
+    static constexpr size_t kAlloc = kBytes + 1024;
+};
+
+struct AxArgs {
+    const float *A;   // 32 x 32 FP32, row-major, already in the K layout above
+    int nb;           // 64-column blocks per slab row (even)
+    long long total;  // work items: slabs x nb / 2
+    int ld_rows;      // rows of one TMA load (= the box height of tB)
+    int split;        // 0: one load into K rows 0..ld_rows-1; 1: rows 0.. and 16..
+    int in_rows;      // input rows per slab
+    int out_rows;     // output rows per slab (= the box height of tC)
+};
+
+template <typename E, int ST, int MINB>
+__global__ void __launch_bounds__(AxLayout<ST>::kThreads, MINB)
+ax_ws_kernel(const __grid_constant__ CUtensorMap tB, const __grid_constant__ CUtensorMap tC,
+             const AxArgs a, long long wait_limit, unsigned int *__restrict__ status)
+{
+    using L = AxLayout<ST>;
+    using T2 = typename Elem<E>::T2;
+    extern __shared__ unsigned char ax_smem_raw[];
+    unsigned char *smem = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(ax_smem_raw) + 1023) & ~(uintptr_t)1023);
+    __shared__ uint64_t full[ST], empty[ST];
+    E *sA = reinterpret_cast<E *>(smem + L::kAOff);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (tid == 0) {
+        for (int s = 0; s < ST; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], L::kWarps);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    for (int e = tid; e < 32 * 32; e += L::kThreads)
+        sA[(e / 32) * L::kAP + (e % 32)] = Elem<E>::cvt(a.A[e]);
+    // K rows that no load writes stay zero (their A columns are zero too)
+    for (int e = tid; e < ST * L::kStage / 16; e += L::kThreads)
+        reinterpret_cast<uint4 *>(smem)[e] = make_uint4(0u, 0u, 0u, 0u);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+
+    if (warp == L::kWarps) {
+        if (lane != 0) return;
+        const uint32_t bytes = (uint32_t)(2 * (a.split ? 2 : 1) * a.ld_rows * 128);
+        long long it = 0;
+        for (long long i = blockIdx.x; i < a.total; i += gridDim.x, it++) {
+            const int s = (int)(it % ST);
+            if (it >= ST &&
+                !mbar_wait_bounded(&empty[s], (uint32_t)(((it / ST) - 1) & 1), wait_limit)) {
+                atomicOr(status, kStatusTimeout);
+                for (long long j = it - ST + 1; j < it; j++)
+                    (void)mbar_wait_bounded(&full[j % ST], (uint32_t)((j / ST) & 1), wait_limit);
+                return;
+            }
+            const int half = a.nb / 2;
+            const int slab = (int)(i / half), b0 = (int)(i % half) * 128;
+            unsigned char *st = smem + (size_t)s * L::kStage;
+            mbar_expect_tx(&full[s], bytes);
+            for (int cb = 0; cb < 2; cb++) {
+                tma_load_2d(st + cb * L::kTile, &tB, b0 + 64 * cb, slab * a.in_rows, &full[s]);
+                if (a.split)
+                    tma_load_2d(st + cb * L::kTile + 16 * 128, &tB, b0 + 64 * cb,
+                                slab * a.in_rows + a.ld_rows, &full[s]);
+            }
+        }
+        return;
+    }
+
+    const int g = lane >> 2, t = lane & 3;
+    const int cb = warp >> 2, col0 = (warp & 3) * 16;
+    E *stg0 = reinterpret_cast<E *>(smem + L::kStgOff + (size_t)warp * 2 * L::kStg);
+    long long it = 0;
+    for (long long i = blockIdx.x; i < a.total; i += gridDim.x, it++) {
+        const int s = (int)(it % ST);
+        if (!mbar_wait_bounded(&full[s], (uint32_t)((it / ST) & 1), wait_limit)) {
+            atomicOr(status, kStatusTimeout);
+            for (long long j = it + 1; j < it + ST && j < a.total; j++)
+                (void)mbar_wait_bounded(&full[j % ST], (uint32_t)((j / ST) & 1), wait_limit);
+            if (lane == 0) bulk_wait_all();
+            return;
+        }
+        const unsigned char *sB = smem + (size_t)s * L::kStage + cb * L::kTile;
+        float acc[2][2][4];
+#pragma unroll
+        for (int fm = 0; fm < 2; fm++)
+#pragma unroll
+            for (int fn = 0; fn < 2; fn++)
+#pragma unroll
+                for (int r = 0; r < 4; r++) acc[fm][fn][r] = 0.f;
+#pragma unroll
+        for (int kk = 0; kk < 32; kk += 16) {
+            uint32_t af[2][4], b[4];
+#pragma unroll
+            for (int fm = 0; fm < 2; fm++)
+                ldsm_x4(af[fm], sA + (16 * fm + (lane & 15)) * L::kAP + kk + (lane >> 4) * 8);
+            const int krow = kk + (lane & 15);
+            const int chunk = (col0 >> 3) + (lane >> 4);
+            ldsm_x4_t(b, sB + krow * 128 + ((chunk ^ (krow & 7)) << 4));
+#pragma unroll
+            for (int fm = 0; fm < 2; fm++) {
+                mma16816<E>(acc[fm][0], af[fm], b[0], b[1]);
+                mma16816<E>(acc[fm][1], af[fm], b[2], b[3]);
+            }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[s]);
+        E *stg = stg0 + (it & 1) * (32 * 16);
+        if (lane == 0) bulk_wait_read1();
+        __syncwarp();
+#pragma unroll
+        for (int fm = 0; fm < 2; fm++)
+#pragma unroll
+            for (int hh = 0; hh < 2; hh++) {
+                const int m = 16 * fm + g + 8 * hh;
+#pragma unroll
+                for (int fn = 0; fn < 2; fn++)
+                    *reinterpret_cast<T2 *>(stg + m * 16 + 8 * fn + 2 * t) =
+                        Elem<E>::cvt2(acc[fm][fn][2 * hh], acc[fm][fn][2 * hh + 1]);
+            }
+        fence_async_smem();
+        __syncwarp();
+        if (lane == 0) {
+            const int half = a.nb / 2;
+            const int slab = (int)(i / half), b0 = (int)(i % half) * 128;
+            tma_store_2d(&tC, stg, b0 + 64 * cb + col0, slab * a.out_rows);
+            bulk_commit();
+        }
+    }
+    if (lane == 0) bulk_wait_all();
+}
+
 }  // namespace fno
 }  // namespace sbte
