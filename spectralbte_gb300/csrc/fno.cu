@@ -1003,6 +1003,7 @@ int mode_mix(spectral_fno_s *n, const float *R, bool tr, const uint16_t *in, uin
     a.Nn = Bp;
     a.nz = (int)(2 * Km * Km * Km);
     a.nz2 = (int)(Km * Km);
+    a.contig = 1;  // A changes with the mode z: keep each CTA on consecutive z
     const Ext ext(n, Bp);
     set_ext(a, (long long)n->ncls * C * C, ext.xm, ext.xm);
     FNO_LAUNCH((launch_sa<E, 64, 64, 2, 2, false, false, kEpiBF16>(a, st)));

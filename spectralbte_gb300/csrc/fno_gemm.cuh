@@ -109,6 +109,10 @@ struct SaArgs {
     // epilogue arrays that share C's view); 0 skips the check
     long long extA, extB, extC;
     int a_tab_max;  // largest value in a_tab (host-side bounds check)
+    // 1: each CTA runs one contiguous range of work items instead of every
+    // gridDim-th item, so that a per-batch A (a_tab) is reloaded only when the
+    // batch changes, not on every item
+    int contig;
 };
 
 struct NtArgs {
@@ -264,8 +268,11 @@ __global__ void __launch_bounds__(WM *WN * 32) gemm_sa_kernel(const SaArgs a)
 
     const unsigned ntiles = (unsigned)((a.Nn + BN - 1) / BN);
     const unsigned total = ntiles * (unsigned)a.nz;
-    unsigned item = blockIdx.x;
-    if (item >= total) return;
+    const unsigned chunk = (total + gridDim.x - 1) / gridDim.x;
+    const unsigned step = a.contig ? 1u : gridDim.x;
+    unsigned item = a.contig ? blockIdx.x * chunk : blockIdx.x;
+    const unsigned end = a.contig ? min(total, item + chunk) : total;
+    if (item >= end) return;
 
     const E *Bb = static_cast<const E *>(a.B.p);
     auto issue = [&](unsigned it, int stage) {
@@ -299,8 +306,8 @@ __global__ void __launch_bounds__(WM *WN * 32) gemm_sa_kernel(const SaArgs a)
 
 #pragma unroll
     for (int s = 0; s < ST - 1; s++) {
-        const unsigned it = item + (unsigned)s * gridDim.x;
-        if (it < total) issue(it, s);
+        const unsigned it = item + (unsigned)s * step;
+        if (it < end) issue(it, s);
         cp_async_commit();
     }
 
@@ -309,9 +316,9 @@ __global__ void __launch_bounds__(WM *WN * 32) gemm_sa_kernel(const SaArgs a)
     const int g = lane >> 2, t = lane & 3;
     long long cur_z = -1;
     int stage = 0;
-    for (; item < total; item += gridDim.x) {
-        const unsigned pre = item + (unsigned)(ST - 1) * gridDim.x;
-        if (pre < total) issue(pre, (stage + ST - 1) % ST);
+    for (; item < end; item += step) {
+        const unsigned pre = item + (unsigned)(ST - 1) * step;
+        if (pre < end) issue(pre, (stage + ST - 1) % ST);
         cp_async_commit();
         const unsigned z = item / ntiles;
         const long long n0 = (long long)(item - z * ntiles) * BN;
