@@ -381,7 +381,8 @@ int spectral_fno_kernel_time(spectral_fno *net, double *ms_total, int *launches)
    consumer warps, 3 stages, 3 CTAs per SM; 2 the same with 8 consumer warps
    and 2 CTAs per SM; 3 with 4 stages and 2 CTAs per SM; 4 with 8 consumer
    warps, 2 stages and 3 CTAs per SM; 5 with 16 consumer warps and 2 CTAs per
-   SM; 0 runs the general tensor-core GEMM.  All give the same result. */
+   SM; 6 as 4 with one staging tile per warp and 4 CTAs per SM; 0 runs the
+   general tensor-core GEMM.  All give the same result. */
 int spectral_fno_set_channel_mix_kernel(spectral_fno *net, int tma);
 /* Readout kernel of inference passes: 1 (default) runs the warp-specialised
    TMA kernel where the shape allows (kind 0, width 64, hidden 128, instances

@@ -1139,13 +1139,14 @@ bool act_map(CUtensorMap *m, const void *base, long long Bp, long long rows, int
 // 3 stages, 3 CTAs per SM; 2 = 8 consumer warps (two row halves), 3 stages,
 // 2 CTAs per SM; 3 = 4 consumer warps, 4 stages, 2 CTAs per SM; 4 = 8
 // consumer warps, 2 stages, 3 CTAs per SM; 5 = 16 consumer warps (four row
-// quarters), 3 stages, 2 CTAs per SM.
-template <typename E, int ST, int RW, int MINB>
+// quarters), 3 stages, 2 CTAs per SM; 6 = as 4 with one staging tile per warp
+// and 4 CTAs per SM.
+template <typename E, int ST, int RW, int MINB, int SB = 2>
 int launch_cm(spectral_fno_s *n, int l, const CUtensorMap &tH, const CUtensorMap &tS,
               const CUtensorMap &tO, bool gelu, int nb, long long total, cudaStream_t st)
 {
-    using L = CmLayout<ST, RW>;
-    auto kern = cm_ws_kernel<E, ST, RW, MINB>;
+    using L = CmLayout<ST, RW, SB>;
+    auto kern = cm_ws_kernel<E, ST, RW, MINB, SB>;
     FNO_LAUNCH(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)L::kAlloc));
     const int grid = (int)std::min<long long>(total, 152LL * MINB);
@@ -1164,7 +1165,8 @@ int channel_mix_tma(spectral_fno_s *n, int l, const uint16_t *hin, const uint16_
     ran = false;
     if (n->cm_tma <= 0 || n->C != kCmC || Bp % kCmBN != 0 || !n->d_status) return kOk;
     const long long rows = n->P * kCmC;
-    const int rw = (n->cm_tma == 2 || n->cm_tma == 4) ? 2 : (n->cm_tma == 5 ? 4 : 1);
+    const int rw =
+        (n->cm_tma == 2 || n->cm_tma == 4 || n->cm_tma == 6) ? 2 : (n->cm_tma == 5 ? 4 : 1);
     CUtensorMap tH, tS, tO;
     if (!act_map(&tH, hin, Bp, rows, kCmBN, kCmC, true) ||
         !act_map(&tS, S, Bp, rows, kCmBN, kCmC, true) ||
@@ -1178,6 +1180,8 @@ int channel_mix_tma(spectral_fno_s *n, int l, const uint16_t *hin, const uint16_
         FNO_TRY((launch_cm<E, 2, 2, 3>(n, l, tH, tS, tO, gelu, nb, total, st)));
     else if (n->cm_tma == 5)
         FNO_TRY((launch_cm<E, 3, 4, 2>(n, l, tH, tS, tO, gelu, nb, total, st)));
+    else if (n->cm_tma == 6)
+        FNO_TRY((launch_cm<E, 2, 2, 4, 1>(n, l, tH, tS, tO, gelu, nb, total, st)));
     else if (n->cm_tma == 3)
         FNO_TRY((launch_cm<E, 4, 1, 2>(n, l, tH, tS, tO, gelu, nb, total, st)));
     else
@@ -1854,8 +1858,8 @@ int spectral_fno_set_channel_mix_kernel(spectral_fno *n, int tma)
         set_error(kErrArg, "spectral_fno_set_channel_mix_kernel: null handle");
         return kErrArg;
     }
-    if (tma < 0 || tma > 5) {
-        set_error(kErrArg, "spectral_fno_set_channel_mix_kernel: 0 .. 5");
+    if (tma < 0 || tma > 6) {
+        set_error(kErrArg, "spectral_fno_set_channel_mix_kernel: 0 .. 6");
         return kErrArg;
     }
     n->cm_tma = tma;

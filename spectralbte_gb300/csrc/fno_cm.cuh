@@ -42,7 +42,7 @@ namespace fno {
 constexpr int kCmC = 64;        // channels in and out
 constexpr int kCmBN = 64;       // instances per item
 
-template <int ST, int RW> struct CmLayout {
+template <int ST, int RW, int SB = 2> struct CmLayout {
     static constexpr int kWarps = 4 * RW;                     // consumer warps
     static constexpr int kThreads = 32 * (kWarps + 1);
     static constexpr int kRows = kCmC / RW;                   // output rows per warp
@@ -54,7 +54,7 @@ template <int ST, int RW> struct CmLayout {
     static constexpr size_t kStageOff = 0;
     static constexpr size_t kWOff = (size_t)ST * kStage;
     static constexpr size_t kStgOff = kWOff + kW;
-    static constexpr size_t kBytes = kStgOff + (size_t)kWarps * 2 * kStg;
+    static constexpr size_t kBytes = kStgOff + (size_t)kWarps * SB * kStg;
     static constexpr size_t kAlloc = kBytes + 1024;           // room to align the base
 };
 
@@ -79,21 +79,25 @@ __device__ __forceinline__ void bulk_wait_read1()
 {
     asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
 }
+__device__ __forceinline__ void bulk_wait_read0()
+{
+    asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
 __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem()
 {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
-template <typename E, int ST, int RW, int MINB>
-__global__ void __launch_bounds__(CmLayout<ST, RW>::kThreads, MINB)
+template <typename E, int ST, int RW, int MINB, int SB = 2>
+__global__ void __launch_bounds__(CmLayout<ST, RW, SB>::kThreads, MINB)
 cm_ws_kernel(const __grid_constant__ CUtensorMap tH, const __grid_constant__ CUtensorMap tS,
              const __grid_constant__ CUtensorMap tO, const float *__restrict__ W,
              const float *__restrict__ bias, int act, int nb, long long total,
              long long wait_limit, unsigned int *__restrict__ status)
 {
     using T2 = typename Elem<E>::T2;
-    using L = CmLayout<ST, RW>;
+    using L = CmLayout<ST, RW, SB>;
     constexpr int kCmWarps = L::kWarps, kCmThreads = L::kThreads, FM = L::kRows / 16;
     extern __shared__ unsigned char cm_smem_raw[];
     unsigned char *smem = reinterpret_cast<unsigned char *>(
@@ -149,7 +153,7 @@ cm_ws_kernel(const __grid_constant__ CUtensorMap tH, const __grid_constant__ CUt
         bm[fm][0] = bias[row0 + 16 * fm + g];
         bm[fm][1] = bias[row0 + 16 * fm + g + 8];
     }
-    E *stg0 = reinterpret_cast<E *>(smem + L::kStgOff + (size_t)warp * 2 * L::kStg);
+    E *stg0 = reinterpret_cast<E *>(smem + L::kStgOff + (size_t)warp * SB * L::kStg);
     long long it = 0;
     for (long long i = blockIdx.x; i < total; i += gridDim.x, it++) {
         const int s = (int)(it % ST);
@@ -186,9 +190,14 @@ cm_ws_kernel(const __grid_constant__ CUtensorMap tH, const __grid_constant__ CUt
                 mma16816<E>(acc[fm][1], a[fm], b[2], b[3]);
             }
         }
-        // the staging tile of this item: its store two items ago has read it
-        E *stg = stg0 + (it & 1) * (L::kRows * 16);
-        if (lane == 0) bulk_wait_read1();
+        // the staging tile of this item: the store that last used it has read it
+        E *stg = stg0 + (SB == 2 ? (it & 1) : 0) * (L::kRows * 16);
+        if (lane == 0) {
+            if (SB == 2)
+                bulk_wait_read1();
+            else
+                bulk_wait_read0();
+        }
         __syncwarp();
 #pragma unroll
         for (int fm = 0; fm < FM; fm++)

@@ -407,14 +407,14 @@ def test_tma_channel_mix_matches_gemm(gpu, B, prec):
     rng = np.random.default_rng(B)
     f = torch.from_numpy(rng.uniform(0.05, 1.0, (B, 16 ** 3))).cuda()
     out = {}
-    for mode in range(6):   # 0: the general GEMM; 1-5: shapes of the TMA kernel
+    for mode in range(7):   # 0: the general GEMM; 1-6: shapes of the TMA kernel
         net.set_channel_mix_kernel(mode)
         Q = torch.empty_like(f)
         net.predict(f, Q, B)
         torch.cuda.synchronize()
         out[mode] = Q.cpu().numpy()
     assert net.status() == 0
-    for mode in range(1, 6):
+    for mode in range(1, 7):
         assert np.abs(out[mode] - out[0]).max() <= 1e-6 * np.abs(out[0]).max(), mode
 
 
