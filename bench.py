@@ -55,10 +55,13 @@ NCU_TRAFFIC = {
         "kernel": "conv_ws_kernel"},
 }
 # The same kernel in its symmetric (row-pair) form streams the partner-summed
-# table, N^2 (N^4 + N^2)/2 FP32 values (ncu at N=24, B=128, bg=32).
+# table, N^2 (N^4 + N^2)/2 FP32 values: ncu at N=24, B=128, bg=32 (variant 3)
+# and at N=32, B=128, bg=64 (variant 5, the register-capped shape).
 NCU_TRAFFIC_SYM = {
     3: {"bytes": 1.551603e9 + 45.4912e6, "N": 24, "B": 128, "bg": 32,
         "kernel": "conv_ws_kernel (row-pair form)"},
+    5: {"bytes": 4.611454e9 + 151.776512e6, "N": 32, "B": 128, "bg": 64,
+        "kernel": "conv_ws_kernel (row-pair form, 3 CTAs per SM)"},
 }
 # DRAM bytes (read + write) of one channel-mix launch of the learned operator
 # at 256 instances, measured by ncu on the network alone at N=32.
@@ -74,7 +77,8 @@ KERNEL_NAME = {1: "conv_f32_kernel", 2: "conv_ws_kernel", 3: "conv_ws_kernel",
 
 def scaled_traffic(variant: int, N: int, B: int, bg: int, sym: bool = False):
     """Per-launch DRAM bytes at (N, B, bg) from the capture of the same kernel."""
-    cap = (NCU_TRAFFIC_SYM if sym else NCU_TRAFFIC).get(1 if variant == 1 else 3)
+    table = NCU_TRAFFIC_SYM if sym else NCU_TRAFFIC
+    cap = table.get(variant) or table.get(1 if variant == 1 else 3)
     if cap is None:
         return None, None
     groups = -(-B // bg)
@@ -470,7 +474,7 @@ def run_learned(args, plan, fd, Qd, B, flags, peaks):
                          "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 8 * B * net.n3,
                                  "d2h_bytes_per_step": 8 * B * net.n3,
                                  "fallbacks": st_e2e["fallbacks"], "calls": st_e2e["calls"]}},
-        "roofline": {"bound": "hbm", "kernel": "gemm_sa_kernel (channel mix, kEpiLayer)",
+        "roofline": {"bound": "hbm", "kernel": "cm_ws_kernel (channel mix: TMA tiles, bias + spectral sum + GELU fused)",
                      "achieved": cm_gbs, "peak": float(peaks["hbm_gbs"]), "unit": "GB/s",
                      "frac": (cm_gbs / float(peaks["hbm_gbs"])) if cm_gbs else None,
                      "traffic": cm_traffic,
@@ -501,7 +505,9 @@ def run_learned_only(args):
     N, L_v, lam, B = args.n, LV_DEF, LAM_DEF, args.batch
     v, zeta = sb.grid_0d(N, L_v)
     plan = sb.Plan(N, L_v, v, zeta, B)
-    plan.generate_weights_iso(lam)
+    # the network path reads no weights; the plan only needs a table, and the
+    # closed-form row-pair FP32 table is the cheapest (no FP64 table)
+    plan.generate_weights_closed(lam, fp64_table=False)
     path = args.learned or os.path.join(ROOT, "spectralbte_gb300", "models", f"fno_n{N}.npz")
     trained = os.path.exists(path)
     net = sb.FourierOperator.load(path) if trained else sb.FourierOperator(N)
@@ -930,7 +936,7 @@ def run_ours(args):
             "launch_ms": conv_avg_s * 1e3,
             "traffic": traffic,
             "traffic_note": ((f"bytes per launch, scaled by N^6 x instance groups from the ncu "
-                              f"capture of {tcap['kernel']} at N=24, B=128, bg={tcap['bg']}; "
+                              f"capture of {tcap['kernel']} at N={tcap['N']}, B={tcap['B']}, bg={tcap['bg']}; "
                               f"the weight table is re-read once per instance group of "
                               f"{tuned[1]}, from HBM, far below the HBM peak") if tcap else
                              "no ncu capture of this form yet"),

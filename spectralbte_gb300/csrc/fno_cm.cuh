@@ -210,11 +210,15 @@ cm_ws_kernel(const __grid_constant__ CUtensorMap tH, const __grid_constant__ CUt
                     const int c = col0 + 8 * fn + 2 * t;  // column in the 64-wide tile
                     const T2 sv = *reinterpret_cast<const T2 *>(
                         sS + m * 128 + ((((c >> 3) ^ (m & 7))) << 4) + (c & 7) * 2);
-                    const float2 ad = Elem<E>::f2(sv);
-                    const float z0 = acc[fm][fn][2 * hh] + bm[fm][hh] + ad.x;
-                    const float z1 = acc[fm][fn][2 * hh + 1] + bm[fm][hh] + ad.y;
+                    // (acc + bias) + S, then GELU: the general GEMM's
+                    // epilogue in FP32x2 instructions, lane for lane
+                    const float2 z = __fadd2_rn(
+                        __fadd2_rn(make_float2(acc[fm][fn][2 * hh], acc[fm][fn][2 * hh + 1]),
+                                   make_float2(bm[fm][hh], bm[fm][hh])),
+                        Elem<E>::f2(sv));
+                    const float2 o = act ? gelu2_f(z) : z;
                     *reinterpret_cast<T2 *>(stg + ml * 16 + 8 * fn + 2 * t) =
-                        act ? Elem<E>::cvt2(gelu_f(z0), gelu_f(z1)) : Elem<E>::cvt2(z0, z1);
+                        Elem<E>::cvt2(o.x, o.y);
                 }
             }
         fence_async_smem();
@@ -346,33 +350,39 @@ ro_ws_kernel(const __grid_constant__ CUtensorMap tH, const float *__restrict__ Q
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[s]);  // the tile is in registers now
-        float part[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+        // part += q2 gelu(acc + c1) on column pairs, in FP32x2 instructions
+        float2 part[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
 #pragma unroll
         for (int fm = 0; fm < FM; fm++)
 #pragma unroll
             for (int hh = 0; hh < 2; hh++)
 #pragma unroll
                 for (int fn = 0; fn < 2; fn++) {
-                    part[fn][0] += qm[fm][hh] * gelu_f(acc[fm][fn][2 * hh] + cm[fm][hh]);
-                    part[fn][1] += qm[fm][hh] * gelu_f(acc[fm][fn][2 * hh + 1] + cm[fm][hh]);
+                    const float2 u =
+                        __fadd2_rn(make_float2(acc[fm][fn][2 * hh], acc[fm][fn][2 * hh + 1]),
+                                   make_float2(cm[fm][hh], cm[fm][hh]));
+                    part[fn] = __ffma2_rn(make_float2(qm[fm][hh], qm[fm][hh]), gelu2_f(u), part[fn]);
                 }
 #pragma unroll
         for (int fn = 0; fn < 2; fn++)
 #pragma unroll
             for (int c = 0; c < 2; c++) {
-                float v = part[fn][c];
+                float v = c ? part[fn].y : part[fn].x;
                 v += __shfl_xor_sync(0xffffffffu, v, 4);
                 v += __shfl_xor_sync(0xffffffffu, v, 8);
                 v += __shfl_xor_sync(0xffffffffu, v, 16);
-                part[fn][c] = v;
+                if (c)
+                    part[fn].y = v;
+                else
+                    part[fn].x = v;
             }
         if (g == 0) {
             const int p = (int)(i / nb), b0 = (int)(i % nb) * kCmBN;
             float *yrow = y + (long long)p * Bp + b0 + col0;
 #pragma unroll
             for (int fn = 0; fn < 2; fn++) {
-                atomicAdd(yrow + 8 * fn + 2 * t, part[fn][0] + cadd);
-                atomicAdd(yrow + 8 * fn + 2 * t + 1, part[fn][1] + cadd);
+                atomicAdd(yrow + 8 * fn + 2 * t, part[fn].x + cadd);
+                atomicAdd(yrow + 8 * fn + 2 * t + 1, part[fn].y + cadd);
             }
         }
     }

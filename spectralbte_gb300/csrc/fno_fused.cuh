@@ -201,8 +201,12 @@ __global__ void __launch_bounds__(256) fused_layer_kernel(const FusedArgs a)
                                 ((long long)ij * NN + k) * CB + (long long)d * Bp + b0 + b;
                             *reinterpret_cast<float2 *>(a.zst + off) = make_float2(z0, z1);
                         }
-                        *slot = a.act ? Elem<E>::cvt2(gelu_f(z0), gelu_f(z1))
-                                      : Elem<E>::cvt2(z0, z1);
+                        if (a.act) {
+                            const float2 o = gelu2_f(make_float2(z0, z1));
+                            *slot = Elem<E>::cvt2(o.x, o.y);
+                        } else {
+                            *slot = Elem<E>::cvt2(z0, z1);
+                        }
                     }
                 }
         }

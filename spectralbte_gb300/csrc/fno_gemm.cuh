@@ -137,9 +137,9 @@ struct NtArgs {
 // erf(x) = 1 - t (a1 + t (a2 + t (a3 + t (a4 + t a5)))) e^{-x^2},
 // t = 1 / (1 + p x), x >= 0, odd extension; |error| <= 1.5e-7 in exact
 // arithmetic and 6.1e-7 evaluated in FP32 on [-12, 12] (tests check the
-// constants against scipy's erf).  About a dozen instructions where the
-// network's GELU epilogues would otherwise spend most of their issue slots;
-// the error is far below the 16-bit resolution of the activations.
+// constants against scipy's erf); the error is far below the 16-bit
+// resolution of the activations.  The training backward's GELU derivative
+// uses it.
 __device__ __forceinline__ float erf_as(float x)
 {
     const float ax = fabsf(x);
@@ -150,9 +150,65 @@ __device__ __forceinline__ float erf_as(float x)
     const float r = fmaf(-poly, __expf(-ax * ax), 1.0f);
     return copysignf(r, x);
 }
-__device__ __forceinline__ float gelu_f(float x)
+// The forward GELU, z Phi(z) = 0.5 z (1 + erf(z / sqrt 2)), written with the
+// same rational approximation in its erfc form: for u = |z| / sqrt 2,
+//   erfc(u) = t (a1 + t (a2 + ...)) e^{-u^2},   t = 1 / (1 + p u),
+//   GELU(z) = max(z, 0) - |z| (erfc(u) / 2)
+// (z >= 0: z - z erfc / 2; z < 0: z erfc / 2).  The coefficients are halved
+// (exact in binary), the reciprocal and 2^x are the single PTX approximations
+// (rcp.approx, ex2.approx; relative error about 1 ulp), and the tail needs no
+// cancellation 1 - erf for negative z.  About a dozen instructions, two of
+// them on the transcendental unit.  gelu2_f does two lanes with FP32x2
+// instructions in the same order, so its lanes equal gelu_f bit for bit.
+namespace gelu_c {
+constexpr float kInvSqrt2 = 0.70710678118654752f;
+constexpr float kP = 0.3275911f;
+constexpr float kH1 = 0.5f * 0.254829592f, kH2 = 0.5f * -0.284496736f,
+                kH3 = 0.5f * 1.421413741f, kH4 = 0.5f * -1.453152027f,
+                kH5 = 0.5f * 1.061405429f;
+constexpr float kNegLog2e = -1.4426950408889634f;
+}  // namespace gelu_c
+__device__ __forceinline__ float rcp_approx(float x)
 {
-    return 0.5f * x * (1.0f + erf_as(x * 0.70710678118654752f));
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float ex2_approx(float x)
+{
+    float r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float gelu_f(float z)
+{
+    using namespace gelu_c;
+    const float a = fabsf(z);
+    const float u = a * kInvSqrt2;
+    const float t = rcp_approx(fmaf(u, kP, 1.0f));
+    float h = fmaf(kH5, t, kH4);
+    h = fmaf(h, t, kH3);
+    h = fmaf(h, t, kH2);
+    h = fmaf(h, t, kH1);
+    h = h * t;
+    const float e = ex2_approx(u * (u * kNegLog2e));
+    return fmaf(-a, h * e, fmaxf(z, 0.0f));
+}
+__device__ __forceinline__ float2 gelu2_f(float2 z)
+{
+    using namespace gelu_c;
+    const float2 a = make_float2(fabsf(z.x), fabsf(z.y));
+    const float2 u = __fmul2_rn(a, make_float2(kInvSqrt2, kInvSqrt2));
+    const float2 d = __ffma2_rn(u, make_float2(kP, kP), make_float2(1.0f, 1.0f));
+    const float2 t = make_float2(rcp_approx(d.x), rcp_approx(d.y));
+    float2 h = __ffma2_rn(make_float2(kH5, kH5), t, make_float2(kH4, kH4));
+    h = __ffma2_rn(h, t, make_float2(kH3, kH3));
+    h = __ffma2_rn(h, t, make_float2(kH2, kH2));
+    h = __ffma2_rn(h, t, make_float2(kH1, kH1));
+    h = __fmul2_rn(h, t);
+    const float2 m = __fmul2_rn(u, __fmul2_rn(u, make_float2(kNegLog2e, kNegLog2e)));
+    const float2 he = __fmul2_rn(h, make_float2(ex2_approx(m.x), ex2_approx(m.y)));
+    return __ffma2_rn(make_float2(-a.x, -a.y), he, make_float2(fmaxf(z.x, 0.0f), fmaxf(z.y, 0.0f)));
 }
 __device__ __forceinline__ float gelu_grad(float x)
 {
@@ -499,8 +555,12 @@ __global__ void __launch_bounds__(WM *WN * 32) gemm_sa_kernel(const SaArgs a)
                             if (a.zst && m < a.M && n < a.Nn)
                                 *reinterpret_cast<float2 *>(a.zst + zc + view_off(a.C, m, n)) =
                                     make_float2(z0, z1);
-                            *dst = a.act ? Elem<E>::cvt2(gelu_f(z0), gelu_f(z1))
-                                         : Elem<E>::cvt2(z0, z1);
+                            if (a.act) {
+                                const float2 o = gelu2_f(make_float2(z0, z1));
+                                *dst = Elem<E>::cvt2(o.x, o.y);
+                            } else {
+                                *dst = Elem<E>::cvt2(z0, z1);
+                            }
                         } else {
                             *dst = Elem<E>::cvt2(v0, v1);
                             if constexpr (CO)

@@ -147,6 +147,39 @@ def test_gelu_erf_approximation_bound():
     assert np.abs(r - erf(x.astype(np.float64))).max() < 1e-6
 
 
+def test_gelu_forward_approximation_bound():
+    """The device forward GELU (fno_gemm.cuh gelu_f / gelu2_f: the erfc form
+    of the same rational approximation, max(z, 0) - |z| erfc(|z|/sqrt 2)/2,
+    with halved coefficients), evaluated in float32 with the constants parsed
+    from the source, against the exact z Phi(z) on [-12, 12]: within
+    2.5e-7 max(1, |z|).  (The device takes the reciprocal and 2^x from the
+    PTX approximations, about 1 ulp each; numpy rounds them exactly.)"""
+    import os
+    import re
+    from scipy.special import erf
+    src = open(os.path.join(os.path.dirname(__file__), "..", "spectralbte_gb300", "csrc",
+                            "fno_gemm.cuh")).read()
+    body = src[src.index("namespace gelu_c {"):src.index("}  // namespace gelu_c")]
+    c = {k: float(v) for k, v in re.findall(r"(k\w+) = (-?[\d.]+)f", body)}
+    h = [float(v) for v in re.findall(r"kH\d = 0\.5f \* (-?[\d.]+)f", body)]
+    assert len(h) == 5 and {"kInvSqrt2", "kP", "kNegLog2e"} <= set(c)
+    f32 = np.float32
+    H = [f32(0.5) * f32(x) for x in h]
+    z = np.linspace(-12, 12, 400001).astype(f32)
+    a = np.abs(z)
+    u = (a * f32(c["kInvSqrt2"])).astype(f32)
+    t = (f32(1) / (u * f32(c["kP"]) + f32(1))).astype(f32)
+    p = H[4] * t + H[3]
+    for k in (2, 1, 0):
+        p = (p * t + H[k]).astype(f32)
+    p = (p * t).astype(f32)
+    e = np.exp2((u * (u * f32(c["kNegLog2e"]))).astype(f32)).astype(f32)
+    g = (np.maximum(z, f32(0)) - a * (p * e)).astype(f32)
+    z64 = z.astype(np.float64)
+    exact = 0.5 * z64 * (1.0 + erf(z64 / np.sqrt(2.0)))
+    assert (np.abs(g - exact) / np.maximum(1.0, np.abs(z64))).max() < 2.5e-7
+
+
 def test_equilibrium_form_gradients_match_finite_differences():
     """The equilibrium-exact loss (network on [f; M_f], output difference)
     against central finite differences of itself, every parameter."""
