@@ -64,8 +64,9 @@ NCU_TRAFFIC_SYM = {
         "kernel": "conv_ws_kernel (row-pair form, 3 CTAs per SM)"},
 }
 # DRAM bytes (read + write) of one channel-mix launch of the learned operator
-# at 256 instances, measured by ncu on the network alone at N=32.
-LEARNED_CM_TRAFFIC = {"bytes": 2.15e9 + 1.04e9, "B": 256}
+# (the TMA kernel, default shape) at 64 instances, measured by ncu on the
+# network alone at N=32.
+LEARNED_CM_TRAFFIC = {"bytes": 536.932096e6 + 237.808128e6, "B": 64}
 # Floor of the learned operator's spot check and acceptance: the distance
 # |Q_net - Q| / sqrt(|Q|^2 + eps mean_b |Q_b|^2), with the eps of the training
 # loss.  Near equilibrium Q -> 0, and the floor measures the error against the

@@ -9,6 +9,8 @@ namespace sbte {
 namespace {
 
 constexpr int kThreads = 256;
+// largest grid side of the separable conservation kernel (its per-axis tables)
+constexpr int kConsMaxN = 128;
 
 __device__ __forceinline__ double wt(int i, int N)
 {
@@ -62,27 +64,59 @@ __device__ void solve_cct(const ConsParams &cp, double *b)
     }
 }
 
-// One species, one CTA per instance.
+// One species, one CTA per instance.  Grid point (i, j, k) carries the
+// prefactor c wt_i wt_j wt_k (c = dv^3 mass, the trapezoid weights of
+// conserve.c:207-264), and the moment weights 1, v_i, v_j, v_k, |v|^2 / 2 are
+// separable.  So each thread takes (i, k) columns and runs down j against
+// the per-j tables e0_j = wt_j, e1_j = wt_j v_j, e2_j = wt_j v_j^2:
+//   T0 = sum_j e0_j q,  T1 = sum_j e1_j q,  T2 = sum_j e2_j q,
+// then folds the column into the moments with s = c wt_i wt_k:
+//   m0 += s T0,  m_x += s v_i T0,  m_y += s T1,  m_z += s v_k T0,
+//   m_e += s ((v_i^2 + v_k^2) T0 + T2) / 2.
+// The correction prefact (l0 + l1 v_i + l2 v_j + l3 v_k + l4 |v|^2 / 2) is
+// s (a e0_j + h_j) with a = l0 + l1 v_i + l3 v_k + l4 (v_i^2 + v_k^2) / 2 and
+// h_j = wt_j (l2 v_j + l4 v_j^2 / 2).  That is five FP64 operations per grid
+// point, where the direct form spends about forty; FP64 runs at 1/64 of the
+// FP32 rate on this GPU, so the count sets the time.  Columns of one i are
+// adjacent in k, so each step of j reads contiguous runs of N doubles.
 __global__ void __launch_bounds__(kThreads)
 conserve_batch_kernel(double *__restrict__ Q, const double *__restrict__ v,
                       ConsParams cp, unsigned int *__restrict__ status)
 {
     __shared__ double red[32 * 5];
     __shared__ double lam[8];
+    __shared__ double e0[kConsMaxN], e1[kConsMaxN], e2[kConsMaxN], hj[kConsMaxN];
     const int N = cp.N;
-    const long long n3 = (long long)N * N * N;
-    double *Qb = Q + (long long)blockIdx.x * n3;
-    const double dv = cp.dv, mass = cp.mass[0];
+    const int NN = N * N;
+    double *Qb = Q + (long long)blockIdx.x * NN * N;
+    const double c = cp.dv * cp.dv * cp.dv * cp.mass[0];
+    for (int j = threadIdx.x; j < N; j += blockDim.x) {
+        const double w = wt(j, N), vj = v[j];
+        e0[j] = w;
+        e1[j] = w * vj;
+        e2[j] = w * vj * vj;
+    }
+    __syncthreads();
     double m[5] = {0, 0, 0, 0, 0};
-    for (int x = threadIdx.x; x < (int)n3; x += blockDim.x) {
-        const int i = x / (N * N), j = (x / N) % N, k = x % N;
-        const double prefact = wt(i, N) * wt(j, N) * wt(k, N) * dv * dv * dv * mass;
-        const double q = Qb[x];
-        m[0] += q * prefact;
-        m[1] += q * (prefact * v[i]);
-        m[2] += q * (prefact * v[j]);
-        m[3] += q * (prefact * v[k]);
-        m[4] += q * (prefact * 0.5 * (v[i] * v[i] + v[j] * v[j] + v[k] * v[k]));
+    for (int p = threadIdx.x; p < NN; p += blockDim.x) {
+        const int i = p / N, k = p - (p / N) * N;
+        const double *col = Qb + (long long)i * NN + k;
+        double t0 = 0.0, t1 = 0.0, t2 = 0.0;
+#pragma unroll 8
+        for (int j = 0; j < N; j++) {
+            const double q = col[(long long)j * N];
+            t0 = fma(e0[j], q, t0);
+            t1 = fma(e1[j], q, t1);
+            t2 = fma(e2[j], q, t2);
+        }
+        const double vi = v[i], vk = v[k];
+        const double s = c * wt(i, N) * wt(k, N);
+        const double st0 = s * t0;
+        m[0] += st0;
+        m[1] = fma(vi, st0, m[1]);
+        m[2] = fma(s, t1, m[2]);
+        m[3] = fma(vk, st0, m[3]);
+        m[4] = fma(0.5 * s, fma(vi * vi + vk * vk, t0, t2), m[4]);
     }
     block_sum<5>(m, red);
     if (threadIdx.x == 0) {
@@ -99,13 +133,22 @@ conserve_batch_kernel(double *__restrict__ Q, const double *__restrict__ v,
     }
     __syncthreads();
     const double l0 = lam[0], l1 = lam[1], l2 = lam[2], l3 = lam[3], l4 = lam[4];
-    for (int x = threadIdx.x; x < (int)n3; x += blockDim.x) {
-        const int i = x / (N * N), j = (x / N) % N, k = x % N;
-        const double prefact = wt(i, N) * wt(j, N) * wt(k, N) * dv * dv * dv * mass / 1;
-        const double t0 = prefact, t1 = prefact * v[i], t2 = prefact * v[j],
-                     t3 = prefact * v[k],
-                     t4 = prefact * 0.5 * (v[i] * v[i] + v[j] * v[j] + v[k] * v[k]);
-        Qb[x] -= (t0 * l0 + t1 * l1 + t2 * l2 + t3 * l3 + t4 * l4);
+    for (int j = threadIdx.x; j < N; j += blockDim.x) {
+        const double vj = v[j];
+        hj[j] = wt(j, N) * fma(0.5 * l4, vj * vj, l2 * vj);
+    }
+    __syncthreads();
+    for (int p = threadIdx.x; p < NN; p += blockDim.x) {
+        const int i = p / N, k = p - (p / N) * N;
+        const double vi = v[i], vk = v[k];
+        const double s = c * wt(i, N) * wt(k, N);
+        const double a = fma(0.5 * l4, vi * vi + vk * vk, fma(l1, vi, fma(l3, vk, l0)));
+        double *col = Qb + (long long)i * NN + k;
+#pragma unroll 8
+        for (int j = 0; j < N; j++) {
+            const double t = fma(a, e0[j], hj[j]);
+            col[(long long)j * N] = fma(-s, t, col[(long long)j * N]);
+        }
     }
 }
 
@@ -291,6 +334,7 @@ cudaError_t conserve_batch(double *Q, int B, const double *v,
                            const ConsParams &cp, cudaStream_t st, unsigned int *status)
 {
     if (B < 1) return cudaSuccess;
+    if (cp.N < 2 || cp.N > kConsMaxN) return cudaErrorInvalidValue;
     conserve_batch_kernel<<<B, kThreads, 0, st>>>(Q, v, cp, status);
     return cudaGetLastError();
 }
