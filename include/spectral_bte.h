@@ -415,6 +415,11 @@ int spectral_fno_predict(spectral_fno *net, const double *f_dev, double *Q_dev,
    |y - Q~|^2 / (|Q~|^2 + eps * mean over the batch of |Q~|^2), so that
    near-equilibrium instances with |Q~| -> 0 do not dominate. */
 int spectral_fno_set_loss_floor(spectral_fno *net, float eps);
+/* Loss power 1 <= k <= 8 (default 1): the training loss becomes
+   mean_b e_b^k, e_b the instance's loss above, so that each instance's
+   gradient is weighted by k e_b^(k-1) and the worst instances of a batch count
+   for more.  Plain form only (kErrArg with the equilibrium form on). */
+int spectral_fno_set_loss_power(spectral_fno *net, float k);
 /* Equilibrium-exact form (on = 1): the operator becomes
    Q(f) = s_f^2 sigma y(f / s_f) - s_M^2 sigma y(M_f / s_M), where M_f is the
    Maxwellian with the density, bulk velocity and temperature of f

@@ -217,13 +217,17 @@ class Net:
         of each f (fno.cu header)."""
         return self.predict(f) - self.predict(M)
 
-    def loss_grad(self, f, Q, floor: float = 0.0, M=None):
-        """Mean over instances of |y - t|^2/(|t|^2 + floor mean_b |t_b|^2),
+    def loss_grad(self, f, Q, floor: float = 0.0, M=None, power: float = 1.0):
+        """Mean over instances of e_b = |y - t|^2/(|t|^2 + floor mean_b |t_b|^2),
         t = Q / (s^2 sigma), and its gradient as a dict of arrays shaped like
         the parameters.  With M (the Maxwellian of each f) the equilibrium-
         exact form: y is replaced by y(f) - (s_M / s_f)^2 y(M), both halves
         run as one batch [f; M], and the M half receives the output gradient
-        times -(s_M / s_f)^2."""
+        times -(s_M / s_f)^2.  With power k > 1 (plain form only) the loss is
+        mean_b e_b^k, which weights each instance's gradient by k e_b^(k-1):
+        the worst instances count for more.  The device then divides its loss
+        scale by the batch mean of those weights, and so does this oracle, so
+        that the 16-bit rounding points see the same magnitudes."""
         p, sp = self.p, self.spec
         B = f.shape[0]
         if M is None:
@@ -241,10 +245,19 @@ class Net:
         den = (t.reshape(B, -1) ** 2).sum(axis=1)
         den = den + floor * den.mean()
         r = y - t
-        loss = float(((r.reshape(B, -1) ** 2).sum(axis=1) / den).sum() / B)
+        e = (r.reshape(B, -1) ** 2).sum(axis=1) / den
         # the device carries gradients times the loss scale gs = B mean(den) / 2
         gs = 0.5 * den.sum()
-        dy = 2.0 * r / (den * B)[:, None, None, None] * gs
+        if power == 1.0:
+            loss = float(e.sum() / B)
+            w = np.ones(B)
+        else:
+            if M is not None:
+                raise ValueError("the power loss is for the plain form")
+            loss = float((e ** power).sum() / B)
+            w = power * e ** (power - 1.0)
+            gs = gs / w.mean()
+        dy = 2.0 * r / (den * B)[:, None, None, None] * (w * gs)[:, None, None, None]
         if M is not None:
             dy = np.concatenate([dy, -rho[:, None, None, None] * dy])
         return loss, self._backward(c, dy, gs)

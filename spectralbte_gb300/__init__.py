@@ -165,6 +165,7 @@ def lib() -> C.CDLL:
         "spectral_fno_set_output_scale": (i, [v, C.c_float]),
         "spectral_fno_output_scale": (C.c_float, [v]),
         "spectral_fno_set_loss_floor": (i, [v, C.c_float]),
+        "spectral_fno_set_loss_power": (i, [v, C.c_float]),
         "spectral_fno_set_equilibrium": (i, [v, i, _dp]),
         "spectral_fno_set_channel_mix_kernel": (i, [v, i]),
         "spectral_fno_set_readout_kernel": (i, [v, i]),
@@ -617,6 +618,11 @@ class FourierOperator:
 
     def set_loss_floor(self, eps: float):
         _check(self.L.spectral_fno_set_loss_floor(self.h, float(eps)), "fno_set_loss_floor")
+
+    def set_loss_power(self, k: float):
+        """Training loss mean_b e_b^k (spectral_fno_set_loss_power); k > 1
+        weights the worst instances of each batch up."""
+        _check(self.L.spectral_fno_set_loss_power(self.h, float(k)), "fno_set_loss_power")
 
     def set_equilibrium(self, on: bool, v=None):
         """Equilibrium-exact form Q(f) = P(f) - P(M_f) (spectral_fno_set_equilibrium);

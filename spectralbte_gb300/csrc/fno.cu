@@ -389,12 +389,66 @@ __global__ void den_kernel(const float *__restrict__ t, float *den, long long P,
     }
 }
 
-// dy = 2 (y - t) / (den_b B) for b < B (0 for padding); loss += sum (y-t)^2 / (den_b B);
-// dc2 += sum dy.
+// err[b] = sum_p (y[p][b] - t[p][b])^2 (err zeroed by the caller).
+__global__ void inst_err_kernel(const float *__restrict__ y, const float *__restrict__ t,
+                                float *err, long long P, int Bp)
+{
+    const long long rows = (P + gridDim.x - 1) / gridDim.x;
+    const long long p0 = blockIdx.x * rows, p1 = min(P, p0 + rows);
+    for (int b = threadIdx.x; b < Bp; b += blockDim.x) {
+        float s = 0.f;
+        for (long long p = p0; p < p1; p++) {
+            const float r = y[p * Bp + b] - t[p * Bp + b];
+            s += r * r;
+        }
+        atomicAdd(err + b, s);
+    }
+}
+
+// The power loss L = mean_b e_b^k, e_b = err_b / den_b (one block): its
+// gradient weights instance b by w_b = k e_b^(k-1).  The loss scale gs is
+// divided by mean_b w_b, so that w_b gs stays at the plain loss's gradient
+// magnitudes in the 16-bit backward pass; Adam and the read-back divide by the
+// same gs, which makes their gradient exactly that of L.  loss = L.
+__global__ void loss_power_kernel(const float *__restrict__ err, const float *__restrict__ den,
+                                  float *__restrict__ w, float *gs, double *loss, int B, float k)
+{
+    __shared__ double r1[32], r2[32];
+    double sw = 0.0, sl = 0.0;
+    for (int b = threadIdx.x; b < B; b += blockDim.x) {
+        const double e = (double)err[b] / (double)den[b];
+        const double wb = (double)k * pow(e, (double)k - 1.0);
+        w[b] = (float)wb;
+        sw += wb;
+        sl += pow(e, (double)k);
+    }
+    for (int o = 16; o; o >>= 1) {
+        sw += __shfl_xor_sync(0xffffffffu, sw, o);
+        sl += __shfl_xor_sync(0xffffffffu, sl, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        r1[threadIdx.x >> 5] = sw;
+        r2[threadIdx.x >> 5] = sl;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, l = 0.0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); i++) {
+            a += r1[i];
+            l += r2[i];
+        }
+        const double mean_w = a / (double)B;
+        if (mean_w > 0.0) gs[0] = (float)((double)gs[0] / mean_w);
+        loss[0] = l / (double)B;
+    }
+}
+
+// dy = 2 (y - t) / (den_b B) w_b gs for b < B (0 for padding; w_b = 1 without
+// weights); loss += sum (y-t)^2 / (den_b B) when loss is given; dc2 += sum dy.
 __global__ void loss_kernel(const float *__restrict__ y, const float *__restrict__ t,
                             const float *__restrict__ den, const float *__restrict__ gs,
-                            float *__restrict__ dy, double *loss, float *dc2, long long n, int B,
-                            int Bp)
+                            const float *__restrict__ w, float *__restrict__ dy, double *loss,
+                            float *dc2, long long n, int B, int Bp)
 {
     const float scale = gs[0];
     __shared__ double r1[32];
@@ -408,7 +462,7 @@ __global__ void loss_kernel(const float *__restrict__ y, const float *__restrict
         if (b < B) {
             const float r = y[i] - t[i];
             const float inv = 1.f / (den[b] * (float)B);
-            d = 2.f * r * inv * scale;
+            d = 2.f * r * inv * (w ? w[b] * scale : scale);
             l += (double)r * r * inv;
         }
         dy[i] = d;
@@ -430,7 +484,7 @@ __global__ void loss_kernel(const float *__restrict__ y, const float *__restrict
             a += r1[w];
             b2 += r2[w];
         }
-        atomicAdd(loss, a);
+        if (loss) atomicAdd(loss, a);
         atomicAdd(dc2, b2);
     }
 }
@@ -725,6 +779,7 @@ struct spectral_fno_s {
               oc2 = 0;
     float sigma = 1.f;
     float floor_eps = 0.f;  // loss: |y - t|^2 / (|t|^2 + floor_eps * mean_b |t_b|^2)
+    float loss_k = 1.f;     // loss power: mean_b e_b^loss_k (spectral_fno_set_loss_power)
     // equilibrium-exact form (spectral_fno_set_equilibrium): the velocity
     // nodes for the Maxwellian of f, and the FP64 input batch [f; M_f]
     int eq = 0;
@@ -750,6 +805,7 @@ struct spectral_fno_s {
     int cap = 0;
     bool cap_train = false;
     float *s = nullptr, *x = nullptr, *t = nullptr, *den = nullptr, *y = nullptr, *dy = nullptr;
+    float *errb = nullptr, *wb = nullptr;  // per-instance error and weight of the power loss
     // 16-bit elements (BF16 or FP16, by prec)
     uint16_t *H[9] = {};
     float *Z[8] = {};
@@ -769,6 +825,7 @@ struct spectral_fno_s {
         for (void *q : owned) cudaFree(q);
         owned.clear();
         s = x = t = den = y = dy = Up = dH = nullptr;
+        errb = wb = nullptr;
         S = nullptr;
         for (auto &q : H) q = nullptr;
         for (auto &q : Z) q = nullptr;
@@ -854,6 +911,8 @@ int ensure(spectral_fno_s *n, int Bp, bool train)
             for (int l = 0; l < n->L - 1; l++) FNO_TRY(nalloc(n, &n->Z[l], act));
         FNO_TRY(nalloc(n, &n->t, P * Bp));
         FNO_TRY(nalloc(n, &n->den, Bp));
+        FNO_TRY(nalloc(n, &n->errb, Bp));
+        FNO_TRY(nalloc(n, &n->wb, Bp));
         FNO_TRY(nalloc(n, &n->dy, P * Bp));
         FNO_TRY(nalloc(n, &n->Up, P * Hd * Bp));
         FNO_TRY(nalloc(n, &n->dU, P * Hd * Bp));
@@ -1335,9 +1394,20 @@ int backward(spectral_fno_s *n, int B, int Bp, cudaStream_t st)
     if (n->eq)  // B real instances at 0..B-1, their Maxwellians at B..2B-1
         loss_diff_kernel<<<ew_grid(P * Bp / 8), kEw, 0, st>>>(
             n->y, n->t, n->den, n->gs, n->s, n->dy, n->d_loss, gr + n->oc2, P, B, Bp);
-    else
-        loss_kernel<<<ew_grid(P * Bp / 8), kEw, 0, st>>>(n->y, n->t, n->den, n->gs, n->dy,
-                                                          n->d_loss, gr + n->oc2, P * Bp, B, Bp);
+    else if (n->loss_k == 1.f)
+        loss_kernel<<<ew_grid(P * Bp / 8), kEw, 0, st>>>(n->y, n->t, n->den, n->gs, nullptr,
+                                                          n->dy, n->d_loss, gr + n->oc2, P * Bp,
+                                                          B, Bp);
+    else {
+        FNO_LAUNCH(cudaMemsetAsync(n->errb, 0, sizeof(float) * Bp, st));
+        inst_err_kernel<<<152, 256, 0, st>>>(n->y, n->t, n->errb, P, Bp);
+        loss_power_kernel<<<1, 256, 0, st>>>(n->errb, n->den, n->wb, n->gs, n->d_loss, B,
+                                             n->loss_k);
+        loss_kernel<<<ew_grid(P * Bp / 8), kEw, 0, st>>>(n->y, n->t, n->den, n->gs, n->wb,
+                                                          n->dy, nullptr, gr + n->oc2, P * Bp, B,
+                                                          Bp);
+        add_launches(2);
+    }
     E *dU = reinterpret_cast<E *>(n->dU);
     if (n->kind == 1)
         proj_bwd_bil_kernel<E><<<ew_grid(P * Hd * Bp / 8), kEw, 0, st>>>(
@@ -1824,9 +1894,9 @@ float spectral_fno_output_scale(spectral_fno *n) { return n ? n->sigma : 0.f; }
 
 int spectral_fno_set_equilibrium(spectral_fno *n, int on, const double *v)
 {
-    if (!n || (on && !v)) {
-        set_error(kErrArg, "spectral_fno_set_equilibrium: need a handle and, to switch on, "
-                           "the N velocity nodes");
+    if (!n || (on && !v) || (on && n->loss_k != 1.f)) {
+        set_error(kErrArg, "spectral_fno_set_equilibrium: need a handle, to switch on the N "
+                           "velocity nodes, and the plain loss (power 1)");
         return kErrArg;
     }
     if (cudaSetDevice(n->device) != cudaSuccess) return kErrCuda;
@@ -1895,6 +1965,17 @@ int spectral_fno_status(spectral_fno *n, unsigned int *status)
     if (cudaSetDevice(n->device) != cudaSuccess) return kErrCuda;
     FNO_LAUNCH(cudaMemcpy(status, n->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost));
     FNO_LAUNCH(cudaMemset(n->d_status, 0, sizeof(unsigned)));
+    return kOk;
+}
+
+int spectral_fno_set_loss_power(spectral_fno *n, float k)
+{
+    if (!n || !(k >= 1.f && k <= 8.f) || (n->eq && k != 1.f)) {
+        set_error(kErrArg, "spectral_fno_set_loss_power: need a handle and 1 <= k <= 8 "
+                           "(k = 1 only in the equilibrium form)");
+        return kErrArg;
+    }
+    n->loss_k = k;
     return kOk;
 }
 

@@ -266,6 +266,9 @@ def main(argv=None):
     ap.add_argument("--hidden", type=int, default=128)
     ap.add_argument("--kind", type=int, default=0, help="0: GELU network, 1: bilinear")
     ap.add_argument("--floor", type=float, default=0.1)
+    ap.add_argument("--loss-power", type=float, default=1.0,
+                    help="train on mean_b e_b^k (k > 1 weights the worst instances up; "
+                         "plain form only)")
     ap.add_argument("--precision", type=int, default=1, help="0: BF16, 1: FP16 elements")
     ap.add_argument("--pairs", type=int, default=200000)
     ap.add_argument("--heldout", type=int, default=512)
@@ -318,6 +321,10 @@ def main(argv=None):
     if a.equilibrium and not net.equilibrium:
         net.set_equilibrium(True, v)
     net.set_loss_floor(a.floor)
+    if a.loss_power != 1.0:
+        if net.equilibrium:
+            ap.error("--loss-power needs --equilibrium 0")
+        net.set_loss_power(a.loss_power)
     e0 = evaluate(net, plan, Fe, Qe)
     c0 = evaluate(net, plan, Fc, Qc) if Fc is not None else None
     log = train(net, F, Q, a.steps, batch=a.batch, lr=a.lr, seed=a.seed,
@@ -343,7 +350,7 @@ def main(argv=None):
                                    "max": e1.max().item()},
         "heldout_by_family": family_stats(e1, fam),
         "heldout_by_family_floored": family_stats(e1f, fam),
-        "floor": a.floor, "equilibrium_form": net.equilibrium,
+        "floor": a.floor, "loss_power": a.loss_power, "equilibrium_form": net.equilibrium,
         "out": a.out}))
 
 

@@ -57,9 +57,13 @@ def test_learned_layer_bytes_match_ncu():
     layer = sum(b for name, b in _passes(32, 64, 12, 4) if name.startswith("0:"))
     measured = 9.93e9 / 256
     assert abs(layer - measured) / measured < 0.05
-    # and the channel mix alone: 3.19 GB at 256 instances
+    # and the channel mix alone, captured at LEARNED_CM_TRAFFIC["B"] instances:
+    # the reads equal the algorithmic reads, and part of the 16-bit output is
+    # still in L2 when the kernel ends, so DRAM traffic sits a few percent
+    # below the algorithmic bytes
     cm = bench.learned_work(32, 64, 12, 4, 128)["channel_mix_bytes"]
-    assert abs(cm * 256 - bench.LEARNED_CM_TRAFFIC["bytes"]) / bench.LEARNED_CM_TRAFFIC["bytes"] < 0.02
+    cap = bench.LEARNED_CM_TRAFFIC
+    assert 0.9 < cap["bytes"] / (cm * cap["B"]) <= 1.0
 
 
 @pytest.mark.parametrize("N", [8, 16, 24, 32])

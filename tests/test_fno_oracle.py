@@ -180,6 +180,29 @@ def test_gelu_forward_approximation_bound():
     assert (np.abs(g - exact) / np.maximum(1.0, np.abs(z64))).max() < 2.5e-7
 
 
+@pytest.mark.parametrize("power", [2.0, 3.0])
+def test_power_loss_gradients_match_finite_differences(power):
+    """mean_b e_b^k (k > 1 weights the worst instances up) against central
+    finite differences of itself, every parameter, with the loss floor."""
+    spec, theta, net = _small(seed=5)
+    f, Q = _data(spec, 3, 6)
+    loss, g = net.loss_grad(f, Q, floor=0.1, power=power)
+    l1, _ = net.loss_grad(f, Q, floor=0.1)
+    assert loss > 0 and abs(loss - l1) > 1e-6 * l1   # not the plain loss
+    ga = fo.pack(spec, g)
+    eps = 1e-6
+    gn = np.empty_like(theta)
+    for i in range(theta.size):
+        tp, tm = theta.copy(), theta.copy()
+        tp[i] += eps
+        tm[i] -= eps
+        lp, _ = fo.Net(spec, tp, sigma=0.7).loss_grad(f, Q, floor=0.1, power=power)
+        lm, _ = fo.Net(spec, tm, sigma=0.7).loss_grad(f, Q, floor=0.1, power=power)
+        gn[i] = (lp - lm) / (2 * eps)
+    err = np.abs(ga - gn).max() / np.abs(gn).max()
+    assert err < 1e-6, err
+
+
 def test_equilibrium_form_gradients_match_finite_differences():
     """The equilibrium-exact loss (network on [f; M_f], output difference)
     against central finite differences of itself, every parameter."""

@@ -96,6 +96,40 @@ def test_gradients_match_oracle(gpu, B, shape, floor):
         assert rel_l2(gk, g64[k].reshape(-1)) < 5e-2, k
 
 
+@pytest.mark.parametrize("B,shape,power", [(5, "small", 2.0), (6, "small16", 3.0),
+                                           (4, "wide16", 2.0), (7, "bil", 2.0)])
+def test_power_loss_gradients_match_oracle(gpu, B, shape, power):
+    """The power loss mean_b e_b^k (spectral_fno_set_loss_power): the loss
+    and every parameter block's gradient against the oracle, with the loss
+    scale divided by the mean instance weight on both sides."""
+    import torch
+    net, spec, prec = _net(gpu, seed=19, shape=shape)
+    net.set_loss_floor(0.1)
+    net.set_loss_power(power)
+    theta = net.get_params().astype(np.float64)
+    f, Q = _data(B, 200 + B, spec.N)
+    loss, g = net.loss_grad(torch.from_numpy(f).cuda(), torch.from_numpy(Q).cuda(), B)
+    lr_, gr = fo.Net(spec, theta, sigma=0.5, rounding=True, precision=prec).loss_grad(
+        f.astype(np.float64), Q.astype(np.float64), 0.1, power=power)
+    l64, g64 = fo.Net(spec, theta, sigma=0.5).loss_grad(f.astype(np.float64),
+                                                        Q.astype(np.float64), 0.1, power=power)
+    assert abs(loss - lr_) <= 1e-4 * lr_
+    off, _ = spec.layout()
+    for k, (o, n) in off.items():
+        gk = g[o:o + n].astype(np.float64)
+        gap = rel_l2(gr[k].reshape(-1), g64[k].reshape(-1))
+        assert rel_l2(gk, gr[k].reshape(-1)) < max(5e-3, 2 * gap), (k, gap)
+        assert rel_l2(gk, g64[k].reshape(-1)) < 5e-2, k
+    # back to the plain loss: the result equals a fresh plain evaluation
+    net.set_loss_power(1.0)
+    l1, _ = net.loss_grad(torch.from_numpy(f).cuda(), torch.from_numpy(Q).cuda(), B)
+    lo, _ = fo.Net(spec, theta, sigma=0.5, rounding=True, precision=prec).loss_grad(
+        f.astype(np.float64), Q.astype(np.float64), 0.1)
+    assert abs(l1 - lo) <= 1e-4 * lo
+    with pytest.raises(gpu.SpectralError):
+        net.set_loss_power(0.5)
+
+
 def _plan(gpu, n=N, L_v=6.0, lam=1.0):
     v, zeta = gpu.grid_0d(n, L_v)
     plan = gpu.Plan(n, L_v, v, zeta, 256)
