@@ -61,7 +61,7 @@ NCU_TRAFFIC_SYM = {
     3: {"bytes": 1.551603e9 + 45.4912e6, "N": 24, "B": 128, "bg": 32,
         "kernel": "conv_ws_kernel (row-pair form)"},
     5: {"bytes": 4.611454e9 + 151.776512e6, "N": 32, "B": 128, "bg": 64,
-        "kernel": "conv_ws_kernel (row-pair form, 3 CTAs per SM)"},
+        "kernel": "conv_ws_kernel (row-pair form, register-capped shape)"},
 }
 # DRAM bytes (read + write) of one channel-mix launch of the learned operator
 # (the TMA kernel, default shape) at 64 instances, measured by ncu on the

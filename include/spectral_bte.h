@@ -261,7 +261,7 @@ int spectral_graph_launch(spectral_plan *plan, void *stream);
 /* FP32 convolution tuning.  variant 1 = block-barrier kernel; 2 = warp-
    specialised kernel with packed FP32x2 math; 3 = warp-specialised, scalar
    math; 4 = warp-specialised, FP32x2 on pre-expanded operands; 5 = as 3 with
-   the registers capped so that three CTAs share an SM (one-pair form only:
+   the registers capped so that two CTAs share an SM (one-pair form only:
    maxPreserve calls run variant 3's shape instead).  bg = instances per
    CTA (32, 64, 128); zs = zeta_z values per thread (variants 2-5: 8 or 16);
    stages = copy pipeline depth; flush = xi-rows per FP64 flush.  Shapes
@@ -418,7 +418,9 @@ int spectral_fno_set_loss_floor(spectral_fno *net, float eps);
 /* Loss power 1 <= k <= 8 (default 1): the training loss becomes
    mean_b e_b^k, e_b the instance's loss above, so that each instance's
    gradient is weighted by k e_b^(k-1) and the worst instances of a batch count
-   for more.  Plain form only (kErrArg with the equilibrium form on). */
+   for more.  The gradient used (and returned by spectral_fno_loss_grad) is
+   that of the loss divided by the batch mean of those weights, the plain
+   loss's scale.  Plain form only (kErrArg with the equilibrium form on). */
 int spectral_fno_set_loss_power(spectral_fno *net, float k);
 /* Equilibrium-exact form (on = 1): the operator becomes
    Q(f) = s_f^2 sigma y(f / s_f) - s_M^2 sigma y(M_f / s_M), where M_f is the

@@ -224,10 +224,10 @@ class Net:
         exact form: y is replaced by y(f) - (s_M / s_f)^2 y(M), both halves
         run as one batch [f; M], and the M half receives the output gradient
         times -(s_M / s_f)^2.  With power k > 1 (plain form only) the loss is
-        mean_b e_b^k, which weights each instance's gradient by k e_b^(k-1):
-        the worst instances count for more.  The device then divides its loss
-        scale by the batch mean of those weights, and so does this oracle, so
-        that the 16-bit rounding points see the same magnitudes."""
+        mean_b e_b^k, which weights each instance's gradient by
+        w_b = k e_b^(k-1): the worst instances count for more.  As on the
+        device, the returned gradient is that of the loss divided by mean_b
+        w_b, the plain loss's gradient scale."""
         p, sp = self.p, self.spec
         B = f.shape[0]
         if M is None:
@@ -256,7 +256,7 @@ class Net:
                 raise ValueError("the power loss is for the plain form")
             loss = float((e ** power).sum() / B)
             w = power * e ** (power - 1.0)
-            gs = gs / w.mean()
+            w = w / w.mean()
         dy = 2.0 * r / (den * B)[:, None, None, None] * (w * gs)[:, None, None, None]
         if M is not None:
             dy = np.concatenate([dy, -rho[:, None, None, None] * dy])

@@ -1691,6 +1691,7 @@ int spectral_plan_autotune(spectral_plan *p, int B, int flags, int *chosen)
         {32, 2, 16},       {64, 2, 16},       {64, 3, 16},       {128, 2, 16},
         {32, 2, 16, 2, 8}, {64, 2, 16, 2, 8}, {32, 3, 16, 3, 8}, {64, 2, 16, 3, 8},
         {64, 3, 16, 3, 8}, {64, 2, 16, 3, 16}, {64, 3, 16, 3, 16}, {64, 2, 16, 5, 8},
+        {64, 3, 16, 5, 8},
         {32, 2, 16, 4, 8}, {64, 2, 16, 4, 8}, {32, 3, 16, 4, 8}};
     cudaEvent_t e0, e1;
     SBTE_CUDA(cudaEventCreate(&e0));

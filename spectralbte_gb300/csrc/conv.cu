@@ -414,7 +414,7 @@ bool conv_f32_supported(int N, ConvF32Config cfg, bool two_pairs)
 {
     if (cfg.variant == 2 || cfg.variant == 3 || cfg.variant == 5)
         return conv_ws_supported(N, cfg.bg, cfg.zs, cfg.variant == 2, cfg.stages, two_pairs,
-                                 cfg.variant == 5 ? 3 : 1);
+                                 cfg.variant == 5 ? 2 : 1);
     if (cfg.variant == 4) return conv_x4_supported(N, cfg.bg, cfg.zs, cfg.stages, two_pairs);
     if (cfg.variant != 1) return false;
     if (!(N == 8 || N == 16 || N == 24 || N == 32)) return false;
@@ -440,7 +440,7 @@ cudaError_t conv_f32_batched(const float *Wblk, const float2 *P,
     if (!conv_f32_supported(N, cfg, two) || B < 1) return cudaErrorInvalidValue;
     if (cfg.variant == 2 || cfg.variant == 3 || cfg.variant == 5)
         return conv_ws(Wblk, P, R, S, T, qacc, N, B, cfg.bg, cfg.zs, cfg.variant == 2,
-                       cfg.stages, cfg.flush, cfg.sym, cfg.variant == 5 ? 3 : 1, status, st,
+                       cfg.stages, cfg.flush, cfg.sym, cfg.variant == 5 ? 2 : 1, status, st,
                        cfg.stall_slot, cfg.stall_limit);
     if (cfg.sym) return cudaErrorInvalidValue;  // the symmetric form is variants 2, 3, 5 only
     switch (N) {

@@ -351,15 +351,17 @@ size_t ws_smem()
 // Shapes instantiated for the warp-specialised kernel:
 // (N, bg, zs, packed, stages, minb); variant 2 = packed FP32x2, 3 = scalar,
 // N = 48 for the row-pair table of the closed-form weights (no FP64 table);
-// 5 = scalar with the registers capped so that minb = 3 CTAs fit on an SM
-// (65536 / (3 x 288 threads) -> 72 registers at N = 32, bg = 64).
+// 5 = scalar with the registers capped so that minb = 2 CTAs fit on an SM
+// (96 registers at N = 32, bg = 64, no spill; uncapped, variant 3 takes 146
+// and one CTA per SM).  A cap of 3 CTAs (72 registers) spilled and ran 3%
+// slower.
 #define SBTE_WS_SHAPES(X)                                                                 \
     X(8, 32, 8, 1, 2, 1) X(8, 32, 8, 0, 3, 1) X(8, 64, 8, 0, 3, 1)                        \
     X(16, 32, 8, 1, 2, 1) X(16, 32, 8, 0, 3, 1) X(16, 64, 8, 0, 3, 1) X(16, 64, 16, 0, 3, 1) \
     X(24, 32, 8, 1, 2, 1) X(24, 32, 8, 0, 3, 1) X(24, 64, 8, 0, 2, 1) X(24, 64, 8, 0, 3, 1)  \
     X(32, 32, 8, 1, 2, 1) X(32, 64, 8, 1, 2, 1) X(32, 32, 8, 0, 3, 1) X(32, 64, 8, 0, 2, 1)  \
     X(32, 64, 8, 0, 3, 1) X(32, 64, 16, 0, 2, 1) X(32, 64, 16, 0, 3, 1)                   \
-    X(32, 64, 8, 0, 2, 3) X(48, 32, 8, 0, 3, 1) X(48, 64, 8, 0, 2, 1)
+    X(32, 64, 8, 0, 2, 2) X(32, 64, 8, 0, 3, 2) X(48, 32, 8, 0, 3, 1) X(48, 64, 8, 0, 2, 1)
 
 bool conv_ws_supported(int N, int bg, int zs, bool packed, int stages, bool two, int minb)
 {

@@ -406,14 +406,16 @@ __global__ void inst_err_kernel(const float *__restrict__ y, const float *__rest
 }
 
 // The power loss L = mean_b e_b^k, e_b = err_b / den_b (one block): its
-// gradient weights instance b by w_b = k e_b^(k-1).  The loss scale gs is
-// divided by mean_b w_b, so that w_b gs stays at the plain loss's gradient
-// magnitudes in the 16-bit backward pass; Adam and the read-back divide by the
-// same gs, which makes their gradient exactly that of L.  loss = L.
+// gradient weights instance b by w_b = k e_b^(k-1).  The backward pass gets
+// the normalised weights w_b / mean_b w_b, so the gradient it returns is
+// grad L / mean_b w_b: the plain loss's gradient scale, which keeps the
+// 16-bit backward pass in range and Adam's step (and its epsilon) as for the
+// plain loss, while the worst instances of the batch count for more.
+// loss = L.
 __global__ void loss_power_kernel(const float *__restrict__ err, const float *__restrict__ den,
-                                  float *__restrict__ w, float *gs, double *loss, int B, float k)
+                                  float *__restrict__ w, double *loss, int B, float k)
 {
-    __shared__ double r1[32], r2[32];
+    __shared__ double r1[32], r2[32], lam_w[1];
     double sw = 0.0, sl = 0.0;
     for (int b = threadIdx.x; b < B; b += blockDim.x) {
         const double e = (double)err[b] / (double)den[b];
@@ -437,10 +439,11 @@ __global__ void loss_power_kernel(const float *__restrict__ err, const float *__
             a += r1[i];
             l += r2[i];
         }
-        const double mean_w = a / (double)B;
-        if (mean_w > 0.0) gs[0] = (float)((double)gs[0] / mean_w);
+        lam_w[0] = a > 0.0 ? (double)B / a : 1.0;
         loss[0] = l / (double)B;
     }
+    __syncthreads();
+    for (int b = threadIdx.x; b < B; b += blockDim.x) w[b] = (float)((double)w[b] * lam_w[0]);
 }
 
 // dy = 2 (y - t) / (den_b B) w_b gs for b < B (0 for padding; w_b = 1 without
@@ -1401,8 +1404,7 @@ int backward(spectral_fno_s *n, int B, int Bp, cudaStream_t st)
     else {
         FNO_LAUNCH(cudaMemsetAsync(n->errb, 0, sizeof(float) * Bp, st));
         inst_err_kernel<<<152, 256, 0, st>>>(n->y, n->t, n->errb, P, Bp);
-        loss_power_kernel<<<1, 256, 0, st>>>(n->errb, n->den, n->wb, n->gs, n->d_loss, B,
-                                             n->loss_k);
+        loss_power_kernel<<<1, 256, 0, st>>>(n->errb, n->den, n->wb, n->d_loss, B, n->loss_k);
         loss_kernel<<<ew_grid(P * Bp / 8), kEw, 0, st>>>(n->y, n->t, n->den, n->gs, n->wb,
                                                           n->dy, nullptr, gr + n->oc2, P * Bp, B,
                                                           Bp);

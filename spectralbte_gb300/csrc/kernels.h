@@ -63,7 +63,7 @@ struct ConvF32Config {
     int variant = 1;  // 1: block-barrier kernel; 2: warp-specialised with
                       // packed FP32x2 math; 3: warp-specialised, scalar math;
                       // 4: warp-specialised, FP32x2 on expanded operands;
-                      // 5: as 3, registers capped for 3 CTAs per SM
+                      // 5: as 3, registers capped for 2 CTAs per SM
     int zs = 0;       // variants 2, 3: zeta_z values per thread (8 or 16)
     int sym = 0;      // variants 2, 3, 5: symmetric form over partner xi-rows
                       // (Wblk is then the table of weights_to_sym_f32)
@@ -83,7 +83,7 @@ bool conv_f32_supported(int N, ConvF32Config cfg, bool two_pairs);
 
 // The warp-specialised FP32x2 variant (conv_ws.cu); writes qacc on its
 // first flush, so it needs no zeroed accumulator.
-// minb: CTAs per SM the kernel's register budget is sized for (1, or 3 for
+// minb: CTAs per SM the kernel's register budget is sized for (1, or 2 for
 // variant 5).
 bool conv_ws_supported(int N, int bg, int zs, bool packed, int stages,
                        bool two_pairs, int minb);

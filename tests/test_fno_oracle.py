@@ -183,13 +183,22 @@ def test_gelu_forward_approximation_bound():
 @pytest.mark.parametrize("power", [2.0, 3.0])
 def test_power_loss_gradients_match_finite_differences(power):
     """mean_b e_b^k (k > 1 weights the worst instances up) against central
-    finite differences of itself, every parameter, with the loss floor."""
+    finite differences of itself, every parameter, with the loss floor.  The
+    oracle returns the gradient divided by the batch mean of the instance
+    weights k e_b^(k-1), as the device does."""
     spec, theta, net = _small(seed=5)
     f, Q = _data(spec, 3, 6)
     loss, g = net.loss_grad(f, Q, floor=0.1, power=power)
     l1, _ = net.loss_grad(f, Q, floor=0.1)
     assert loss > 0 and abs(loss - l1) > 1e-6 * l1   # not the plain loss
-    ga = fo.pack(spec, g)
+    # the instance errors e_b and weights of the same batch
+    y, c = net.forward(f)
+    t = Q.reshape(3, -1) / (c["s"] ** 2 * 0.7)[:, None]
+    den = (t ** 2).sum(axis=1)
+    den = den + 0.1 * den.mean()
+    eb = ((y.reshape(3, -1) - t) ** 2).sum(axis=1) / den
+    mean_w = (power * eb ** (power - 1.0)).mean()
+    ga = fo.pack(spec, g) * mean_w
     eps = 1e-6
     gn = np.empty_like(theta)
     for i in range(theta.size):

@@ -183,7 +183,7 @@ def test_plan_fp32_matches_fp64(gpu, oracle, N, L_v, lam, B, mp):
     shapes = [(1, 32, 0, 2), (1, 64, 0, 3), (1, 128, 0, 2), (2, 32, 8, 2), (3, 32, 8, 3),
               (3, 64, 8, 3), (4, 32, 8, 2)]
     if N == 32:
-        shapes += [(2, 64, 8, 2), (3, 64, 16, 2), (4, 64, 8, 2), (5, 64, 8, 2)]
+        shapes += [(2, 64, 8, 2), (3, 64, 16, 2), (4, 64, 8, 2), (5, 64, 8, 2), (5, 64, 8, 3)]
     for variant, bg, zs, stages in shapes:
         plan.set_tuning(bg, stages, 16, variant=variant, zs=zs)
         plan.computeQ_device(fd, Q32, B, gpu.FP32 | gpu.CONSERVE | extra)
@@ -212,7 +212,8 @@ def test_fp32_symmetric_form_matches_plain_rows(gpu, oracle, N, L_v, lam, B, mp)
     extra = gpu.MAXPRESERVE if mp else 0
     plan.computeQ_device(fd, Q64, B, gpu.FP64 | extra)
     b = Q64.cpu().numpy()
-    shapes = [(3, 64, 8, 3), (2, 32, 8, 2), (3, 32, 8, 3)] + ([(5, 64, 8, 2)] if N == 32 else [])
+    shapes = [(3, 64, 8, 3), (2, 32, 8, 2), (3, 32, 8, 3)] + \
+        ([(5, 64, 8, 2), (5, 64, 8, 3)] if N == 32 else [])
     for variant, bg, zs, stages in shapes:
         plan.set_tuning(bg, stages, 16, variant=variant, zs=zs)
         plan.set_symmetric(True)
