@@ -923,8 +923,9 @@ def run_ours(args):
             "kernel": KERNEL_NAME[tuned[0]],
             "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
             "frac": achieved / fp32_peak,
-            "peak_source": ("measured: sustained FP32 FMA rate of this GPU from the library's "
-                            "register-FMA probe (spectral_fp32_fma_rate), run in this process; "
+            "peak_source": ("measured: sustained FP32 FMA rate of this GPU from the "
+                            "register-FMA probe (spectral_calib_fp32_fma_rate in "
+                            "libspectral_calib.so), run in this process; "
                             "MEASURED_PEAKS.json carries no FP32 figure, and no dense GEMM "
                             "exists in this operator, so neither its HBM copy nor its bf16 "
                             "tensor peak binds"),
