@@ -1008,8 +1008,11 @@ static int q_fp64(spectral_plan_s *p, const WeightsDev &W, const double *fdev,
 // where the two-pair form does not fit in shared memory, a narrower instance
 // group; plus the symmetric form where the variant has it and the plan
 // allows it.  Builds the weight table that configuration reads.
+// A call of at most 32 instances (B > 0) runs an instance group of 32 where
+// the shape has one: a wider group would leave the rest of its threads idle.
+// Each instance's sum keeps its order, so the result is the same bit for bit.
 static int resolve_f32(spectral_plan_s *p, bool maxpreserve, ConvF32Config &cfg,
-                       const float *&Wt, cudaStream_t st)
+                       const float *&Wt, cudaStream_t st, int B = 0)
 {
     const int N = p->N;
     cfg = p->tune;
@@ -1033,6 +1036,11 @@ static int resolve_f32(spectral_plan_s *p, bool maxpreserve, ConvF32Config &cfg,
             return kErrUnsupported;
         }
     }
+    if (B > 0 && B <= 32 && cfg.bg > 32) {
+        ConvF32Config narrow = cfg;
+        narrow.bg = 32;
+        if (conv_f32_supported(N, narrow, maxpreserve)) cfg = narrow;
+    }
     cfg.sym = (p->sym && (cfg.variant == 2 || cfg.variant == 3 || cfg.variant == 5)) ? 1 : 0;
     Wt = nullptr;
     if (cfg.variant == 4) {
@@ -1054,7 +1062,7 @@ static int q_fp32(spectral_plan_s *p, const double *fdev, double *Qdev, int B,
     const int N = p->N;
     ConvF32Config cfg;
     const float *Wt = nullptr;
-    SBTE_TRY(resolve_f32(p, maxpreserve, cfg, Wt, st));
+    SBTE_TRY(resolve_f32(p, maxpreserve, cfg, Wt, st, B));
     if (p->stall_slot >= 0) {
         if (cfg.variant != 2 && cfg.variant != 3 && cfg.variant != 5) {
             p->stall_slot = -1;
@@ -1691,7 +1699,7 @@ int spectral_plan_autotune(spectral_plan *p, int B, int flags, int *chosen)
         {32, 2, 16},       {64, 2, 16},       {64, 3, 16},       {128, 2, 16},
         {32, 2, 16, 2, 8}, {64, 2, 16, 2, 8}, {32, 3, 16, 3, 8}, {64, 2, 16, 3, 8},
         {64, 3, 16, 3, 8}, {64, 2, 16, 3, 16}, {64, 3, 16, 3, 16}, {64, 2, 16, 5, 8},
-        {64, 3, 16, 5, 8},
+        {64, 3, 16, 5, 8}, {32, 2, 16, 5, 8}, {32, 3, 16, 5, 8},
         {32, 2, 16, 4, 8}, {64, 2, 16, 4, 8}, {32, 3, 16, 4, 8}};
     cudaEvent_t e0, e1;
     SBTE_CUDA(cudaEventCreate(&e0));

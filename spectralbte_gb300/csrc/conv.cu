@@ -109,7 +109,6 @@ conv_f32_kernel(const float *__restrict__ Wblk, const float2 *__restrict__ P,
     using L = F32Layout<N, BG, TWO>;
     constexpr int NN = N * N;
     constexpr int H = N / 2;
-    constexpr int NT = BG * (N / ZS);
     constexpr long long N3 = (long long)NN * N;
     static_assert(N % 8 == 0, "xi_z chunks of 8");
     static_assert(N % ZS == 0, "zeta_z split");
@@ -410,11 +409,18 @@ cudaError_t conv_f64(const double *W, const double2 *P, const double2 *R,
     return cudaGetLastError();
 }
 
+// CTAs per SM the register budget of a warp-specialised shape is sized for:
+// variant 5 caps it for two CTAs of 64 instances or three of 32.
+static int ws_minb(const ConvF32Config &cfg)
+{
+    return cfg.variant == 5 ? (cfg.bg == 32 ? 3 : 2) : 1;
+}
+
 bool conv_f32_supported(int N, ConvF32Config cfg, bool two_pairs)
 {
     if (cfg.variant == 2 || cfg.variant == 3 || cfg.variant == 5)
         return conv_ws_supported(N, cfg.bg, cfg.zs, cfg.variant == 2, cfg.stages, two_pairs,
-                                 cfg.variant == 5 ? 2 : 1);
+                                 ws_minb(cfg));
     if (cfg.variant == 4) return conv_x4_supported(N, cfg.bg, cfg.zs, cfg.stages, two_pairs);
     if (cfg.variant != 1) return false;
     if (!(N == 8 || N == 16 || N == 24 || N == 32)) return false;
@@ -440,7 +446,7 @@ cudaError_t conv_f32_batched(const float *Wblk, const float2 *P,
     if (!conv_f32_supported(N, cfg, two) || B < 1) return cudaErrorInvalidValue;
     if (cfg.variant == 2 || cfg.variant == 3 || cfg.variant == 5)
         return conv_ws(Wblk, P, R, S, T, qacc, N, B, cfg.bg, cfg.zs, cfg.variant == 2,
-                       cfg.stages, cfg.flush, cfg.sym, cfg.variant == 5 ? 2 : 1, status, st,
+                       cfg.stages, cfg.flush, cfg.sym, ws_minb(cfg), status, st,
                        cfg.stall_slot, cfg.stall_limit);
     if (cfg.sym) return cudaErrorInvalidValue;  // the symmetric form is variants 2, 3, 5 only
     switch (N) {

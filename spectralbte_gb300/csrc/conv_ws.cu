@@ -353,15 +353,17 @@ size_t ws_smem()
 // N = 48 for the row-pair table of the closed-form weights (no FP64 table);
 // 5 = scalar with the registers capped so that minb = 2 CTAs fit on an SM
 // (96 registers at N = 32, bg = 64, no spill; uncapped, variant 3 takes 146
-// and one CTA per SM).  A cap of 3 CTAs (72 registers) spilled and ran 3%
-// slower.
+// and one CTA per SM; a cap of 3 CTAs (72 registers) spilled and ran 3%
+// slower), or minb = 3 at bg = 32 (128 registers, the same speed per
+// instance), which serves calls of at most 32 instances.
 #define SBTE_WS_SHAPES(X)                                                                 \
     X(8, 32, 8, 1, 2, 1) X(8, 32, 8, 0, 3, 1) X(8, 64, 8, 0, 3, 1)                        \
     X(16, 32, 8, 1, 2, 1) X(16, 32, 8, 0, 3, 1) X(16, 64, 8, 0, 3, 1) X(16, 64, 16, 0, 3, 1) \
     X(24, 32, 8, 1, 2, 1) X(24, 32, 8, 0, 3, 1) X(24, 64, 8, 0, 2, 1) X(24, 64, 8, 0, 3, 1)  \
     X(32, 32, 8, 1, 2, 1) X(32, 64, 8, 1, 2, 1) X(32, 32, 8, 0, 3, 1) X(32, 64, 8, 0, 2, 1)  \
     X(32, 64, 8, 0, 3, 1) X(32, 64, 16, 0, 2, 1) X(32, 64, 16, 0, 3, 1)                   \
-    X(32, 64, 8, 0, 2, 2) X(32, 64, 8, 0, 3, 2) X(48, 32, 8, 0, 3, 1) X(48, 64, 8, 0, 2, 1)
+    X(32, 64, 8, 0, 2, 2) X(32, 64, 8, 0, 3, 2) X(32, 32, 8, 0, 2, 3) X(32, 32, 8, 0, 3, 3)     \
+    X(48, 32, 8, 0, 3, 1) X(48, 64, 8, 0, 2, 1)
 
 bool conv_ws_supported(int N, int bg, int zs, bool packed, int stages, bool two, int minb)
 {

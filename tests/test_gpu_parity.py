@@ -230,6 +230,32 @@ def test_fp32_symmetric_form_matches_plain_rows(gpu, oracle, N, L_v, lam, B, mp)
     plan.close()
 
 
+@pytest.mark.parametrize("N,L_v,lam,shape", [(32, 6.0, 1.0, (64, 2, 16, 5, 8)),
+                                              (16, 5.0, 0.0, (64, 3, 16, 3, 8))])
+def test_fp32_small_calls_equal_the_batch(gpu, oracle, N, L_v, lam, shape):
+    """A call of at most 32 instances runs an instance group of 32 where the
+    plan's shape has that width (variant 5: three CTAs per SM instead of
+    two).  Each instance's sum keeps its order, so calls of 1 and 20
+    instances equal the same instances of a 70-instance call bit for bit,
+    in both the row-pair form and over every row."""
+    import torch
+    g, plan, _ = plan_for(gpu, oracle, N, L_v, lam, 70)
+    bg, stages, flush, variant, zs = shape
+    plan.set_tuning(bg, stages, flush, variant=variant, zs=zs)
+    fd = torch.from_numpy(_two_max_batch(g, 70, 21)).cuda()
+    for sym in (True, False):
+        plan.set_symmetric(sym)
+        Q = torch.empty_like(fd)
+        plan.computeQ_device(fd, Q, 70, gpu.FP32 | gpu.CONSERVE)
+        for b in (1, 20):
+            Qb = torch.empty_like(fd[:b])
+            plan.computeQ_device(fd[:b].contiguous(), Qb, b, gpu.FP32 | gpu.CONSERVE)
+            torch.cuda.synchronize()
+            assert torch.equal(Qb, Q[:b]), (sym, b)
+    assert plan.status() == 0
+    plan.close()
+
+
 def test_fp32_unsupported_n_is_an_error(gpu, oracle):
     import torch
     g = oracle.Grid(7, 4.5, "0d")
