@@ -264,8 +264,9 @@ int spectral_graph_launch(spectral_plan *plan, void *stream);
    the registers capped so that two CTAs of 64 instances (or three of 32)
    share an SM (one-pair form only: maxPreserve calls run variant 3's shape
    instead).  A call of at most 32 instances runs the plan's shape with a
-   group of 32 where one exists; the result is the same bit for bit.  bg = instances per
-   CTA (32, 64, 128); zs = zeta_z values per thread (variants 2-5: 8 or 16);
+   group of 32 where one exists; the result is the same bit for bit.
+   bg = instances per CTA (32, 64, 128); zs = zeta_z values per thread
+   (variants 2-5: 8 or 16);
    stages = copy pipeline depth; flush = xi-rows per FP64 flush.  Shapes
    that are not instantiated return SPECTRAL_ERR_UNSUPPORTED.  The
    autotuner times the supported shapes on B instances and keeps the
