@@ -561,3 +561,34 @@ def test_learned_path_gain_over_plain_fp32(gpu):
     assert max(res.values()) <= 1e-12
     plan.set_learned(None)
     plan.close()
+
+
+def test_committed_network_accuracy_by_family(gpu):
+    """The committed N = 32 network against the plain FP32 operator on 1,024
+    fresh instances of each training family (a seed no training or selection
+    used), floored distance with eps = 0.1 over each family's batch.  The
+    thresholds record what the network does, with margin: the two-Maxwellian
+    family (the benchmark's) at a mean of about 4e-4 with its worst instance
+    near 1e-3; shock blends and Maxwellian mixtures well above 1e-3, which is
+    why the spot check returns those calls to the plain operator."""
+    import os
+    import torch
+    from spectralbte_gb300.learned import evaluate, make_dataset
+    sb = gpu
+    path = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                        "spectralbte_gb300", "models", "fno_n32.npz")
+    net = sb.FourierOperator.load(path)
+    N, L_v = 32, 6.0
+    v, zeta = sb.grid_0d(N, L_v)
+    plan = sb.Plan(N, L_v, v, zeta, 512)
+    plan.generate_weights_closed(1.0, fp64_table=False)
+    bounds = {"two_maxwellian": (6e-4, 1.5e-3), "shock": (2e-2, 1e-1), "mixture": (6e-3, 5e-2)}
+    got = {}
+    for fam, (mean_max, worst_max) in bounds.items():
+        F, Q, _ = make_dataset(plan, 1024, seed=130001, families=(fam,), out_dtype=torch.float64)
+        e = evaluate(net, plan, F, Q, floor=0.1).cpu().numpy()
+        got[fam] = (float(e.mean()), float(e.max()))
+        assert e.mean() <= mean_max and e.max() <= worst_max, (fam, got[fam])
+    print(got)
+    assert got["two_maxwellian"][0] < 1e-3 < got["shock"][0]
+    plan.close()
