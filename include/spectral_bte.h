@@ -363,12 +363,6 @@ int spectral_fno_create(spectral_fno **net, int N, int width, int modes,
                         int layers, int hidden, int kind, int precision,
                         unsigned long long seed);
 int spectral_fno_precision(spectral_fno *net);
-/* At N = 32, width 64, 12 modes, on = 1 runs the last inverse transform of
-   each layer fused with its channel mix and the next layer's first forward
-   axis pass (fewer bytes, fewer launches, the same time on a GB300 as the
-   separate kernels; off by default).  Every other shape uses the separate
-   kernels. */
-int spectral_fno_set_fused(spectral_fno *net, int on);
 /* Channel-mix timing: with profiling on, CUDA events are recorded on the
    launching stream around every channel-mix launch (the separate-kernel
    path, outside graph captures); spectral_fno_kernel_time returns their

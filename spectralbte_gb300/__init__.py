@@ -154,7 +154,6 @@ def lib() -> C.CDLL:
         # learned operator
         "spectral_fno_create": (i, [pp, i, i, i, i, i, i, i, C.c_ulonglong]),
         "spectral_fno_precision": (i, [v]),
-        "spectral_fno_set_fused": (i, [v, i]),
         "spectral_fno_set_profiling": (i, [v, i]),
         "spectral_fno_kernel_time": (i, [v, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
         "spectral_fno_destroy": (i, [v]),
@@ -602,8 +601,6 @@ class FourierOperator:
         _check(self.L.spectral_fno_status(self.h, C.byref(s)), "fno_status")
         return s.value
 
-    def set_fused(self, on: bool):
-        _check(self.L.spectral_fno_set_fused(self.h, 1 if on else 0), "fno_set_fused")
 
     def set_profiling(self, on: bool):
         """Time every channel-mix launch with CUDA events on its stream."""

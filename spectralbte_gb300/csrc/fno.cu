@@ -37,7 +37,6 @@
 #include "common.cuh"
 #include "fno.h"
 #include "fno_cm.cuh"
-#include "fno_fused.cuh"
 #include "fno_gemm.cuh"
 #include "kernels.h"
 #include "../../include/spectral_bte.h"
@@ -775,7 +774,6 @@ struct spectral_fno_s {
     int device = 0;
     int N = 0, C = 0, Km = 0, L = 0, Hd = 0, ncls = 0;
     int kind = 0;  // 0: GELU layers and readout; 1: linear layers, bilinear readout
-    bool fused = false;  // fused last inverse pass + channel mix (spectral_fno_set_fused)
     long long P = 0;
     long long nparams = 0;
     long long oP = 0, obP = 0, oW[8] = {}, ob[8] = {}, oR[8] = {}, oQ1 = 0, oc1 = 0, oq2 = 0,
@@ -1015,14 +1013,14 @@ int axis_k_tma(spectral_fno_s *n, bool inverse, const uint16_t *in, uint16_t *ou
 // stay far from the 16-bit subnormal range: out is then N^2 times F3 in.
 template <typename E>
 int spectral_fwd(spectral_fno_s *n, const uint16_t *in, uint16_t *out, bool bwd, int Bp,
-                 cudaStream_t st, bool t1_ready = false, bool tma = false)
+                 cudaStream_t st, bool tma = false)
 {
     const long long N = n->N, Km = n->Km, CB = (long long)n->C * Bp;
     const float *F = n->F, *F23 = bwd ? n->Fu : n->F;
     const Ext ext(n, Bp);
     bool ran = false;
-    if (!t1_ready && tma && !bwd) FNO_TRY(axis_k_tma<E>(n, false, in, n->T1, Bp, st, ran));
-    if (!t1_ready && !ran) {  // axis k, real input (T1 may come from the previous fused layer)
+    if (tma && !bwd) FNO_TRY(axis_k_tma<E>(n, false, in, n->T1, Bp, st, ran));
+    if (!ran) {  // axis k, real input
         SaArgs a = sa_base(F, N, 1, Km * N, (int)Km, (int)N);
         a.B = sv(in, CB, CB, N * CB);
         a.C = sv(n->T1, CB, CB, 2 * Km * CB, Km * CB);
@@ -1077,7 +1075,7 @@ int mode_mix(spectral_fno_s *n, const float *R, bool tr, const uint16_t *in, uin
 // or added, times alpha, into the FP32 out32 (the backward pass).
 template <typename E>
 int spectral_inv(spectral_fno_s *n, const uint16_t *in, uint16_t *out16, float *out32,
-                 float alpha, int Bp, cudaStream_t st, bool stop_at_u2 = false, bool tma = false)
+                 float alpha, int Bp, cudaStream_t st, bool tma = false)
 {
     const long long N = n->N, Km = n->Km, CB = (long long)n->C * Bp;
     const float *G = n->G;
@@ -1099,7 +1097,6 @@ int spectral_inv(spectral_fno_s *n, const uint16_t *in, uint16_t *out16, float *
         set_ext(a, ext.G, ext.t2, ext.t1);
         FNO_LAUNCH((launch_sa<E, 32, 128, 1, 4, true, true, kEpiCplxBF16>(a, st)));
     }
-    if (stop_at_u2) return kOk;
     if (tma && out16 && !out32) {
         bool ran = false;
         FNO_TRY(axis_k_tma<E>(n, true, n->U2, out16, Bp, st, ran));
@@ -1117,45 +1114,6 @@ int spectral_inv(spectral_fno_s *n, const uint16_t *in, uint16_t *out16, float *
         else
             FNO_LAUNCH((launch_sa<E, 32, 128, 1, 4, true, true, kEpiBF16>(a, st)));
     }
-    return kOk;
-}
-
-bool fused_shape(const spectral_fno_s *n)
-{
-    return n->fused && n->N == 32 && n->C == 64 && n->Km == 12;
-}
-
-// Last inverse axis pass + channel mix + bias + activation of layer l
-// (fno_fused.cuh), from U2 and the layer input to the layer output.
-template <typename E>
-int fused_layer(spectral_fno_s *n, int l, const uint16_t *hin, uint16_t *hout, float *zst,
-                bool act, bool t1_next, int Bp, cudaStream_t st)
-{
-    using L = FusedLayout<E, 32, 64, 12>;
-    if (Bp % 8 || n->N != 32 || n->C != 64 || n->Km != 12) {
-        set_error(kErrArg, "fused layer: shape N=%d C=%d Km=%d Bp=%d", n->N, n->C, n->Km, Bp);
-        return kErrArg;
-    }
-    auto kern = fused_layer_kernel<E, 32, 64, 12>;
-    FNO_LAUNCH(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)L::bytes));
-    FusedArgs a;
-    a.U2 = n->U2;
-    a.H = hin;
-    a.Hout = hout;
-    a.zst = zst;
-    a.G = n->G;
-    a.F = n->F;
-    a.T1 = t1_next ? n->T1 : nullptr;
-    a.W = n->params + n->oW[l];
-    a.bias = n->params + n->ob[l];
-    a.act = act ? 1 : 0;
-    a.Bp = Bp;
-    const long long items = 32LL * 32 * (Bp / 8);
-    const int grid = (int)std::min<long long>(items, 152LL * 2);
-    kern<<<grid, L::NTH, L::bytes, st>>>(a);
-    add_launches(1);
-    FNO_LAUNCH(cudaGetLastError());
     return kOk;
 }
 
@@ -1316,23 +1274,13 @@ int forward(spectral_fno_s *n, const T *f, int B, int Bp, bool train, cudaStream
                                                  (int)C, Bp);
     add_launches(3);
     FNO_LAUNCH(cudaGetLastError());
-    bool t1_ready = false;  // T1 of this layer written by the previous fused layer
     for (int l = 0; l < n->L; l++) {
         uint16_t *hin = Hbuf(n, l, train), *hout = Hbuf(n, l + 1, train);
         uint16_t *xl = train ? n->X[l] : n->X[0];
-        FNO_TRY(spectral_fwd<E>(n, hin, xl, false, Bp, st, t1_ready, !train));
-        t1_ready = false;
+        FNO_TRY(spectral_fwd<E>(n, hin, xl, false, Bp, st, !train));
         FNO_TRY(mode_mix<E>(n, prm + n->oR[l], false, xl, n->Y, Bp, st));
         const bool gelu = n->kind == 0 && l < n->L - 1;
-        if (fused_shape(n)) {
-            FNO_TRY(spectral_inv<E>(n, n->Y, nullptr, nullptr, 1.f, Bp, st, true));
-            const bool t1_next = l < n->L - 1;
-            FNO_TRY(fused_layer<E>(n, l, hin, hout, (train && gelu) ? n->Z[l] : nullptr, gelu,
-                                   t1_next, Bp, st));
-            t1_ready = t1_next;
-            continue;
-        }
-        FNO_TRY(spectral_inv<E>(n, n->Y, n->S, nullptr, 1.f, Bp, st, false, !train));
+        FNO_TRY(spectral_inv<E>(n, n->Y, n->S, nullptr, 1.f, Bp, st, !train));
         if (!train) {
             auto *ev = prof_pair(n, st);
             if (ev) cudaEventRecord(ev->first, st);
@@ -1816,16 +1764,6 @@ long long spectral_fno_num_params(spectral_fno *n) { return n ? n->nparams : 0; 
 int spectral_fno_num_classes(spectral_fno *n) { return n ? n->ncls : 0; }
 
 int spectral_fno_precision(spectral_fno *n) { return n ? n->prec : -1; }
-
-int spectral_fno_set_fused(spectral_fno *n, int on)
-{
-    if (!n) {
-        set_error(kErrArg, "spectral_fno_set_fused: null handle");
-        return kErrArg;
-    }
-    n->fused = on != 0;
-    return kOk;
-}
 
 int spectral_fno_set_profiling(spectral_fno *n, int on)
 {
