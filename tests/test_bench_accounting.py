@@ -93,6 +93,19 @@ def test_row_pair_traffic_scaling():
     assert t_all == pytest.approx(cap_all["bytes"] / 4 * 16 * (32 / 24) ** 6)
 
 
+def test_variant5_traffic_capture():
+    """The register-capped variant has its own capture at the headline N
+    (N=32, 128 instances in groups of 64): DRAM bytes per launch scale with the
+    number of instance groups, and one group reads the 2.15 GB row-pair table
+    once, plus the transforms."""
+    t128, cap = bench.scaled_traffic(5, 32, 128, 64, sym=True)
+    assert cap["N"] == 32 and t128 == pytest.approx(cap["bytes"])
+    t1024, _ = bench.scaled_traffic(5, 32, 1024, 64, sym=True)
+    assert t1024 == pytest.approx(8 * cap["bytes"])
+    table = 32 ** 2 * (32 ** 4 + 32 ** 2) / 2 * 4
+    assert 1.0 < cap["bytes"] / (2 * table) < 1.2
+
+
 def test_both_arms_describe_one_workload():
     c = bench.headline_config(32, 6.0, 1.0, 1024, 1)
     assert c["N"] == 32 and c["batch_per_gpu"] == 1024
